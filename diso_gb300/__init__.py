@@ -1,0 +1,15 @@
+"""GB300-native differentiable iso-surface extraction (DiffMC / DiffDMC).
+
+Drop-in for the reference package's public API (diso/__init__.py):
+
+    from diso_gb300 import DiffMC, DiffDMC
+    verts, faces = DiffMC(dtype=torch.float32)(sdf, deform, isovalue=0.0, normalize=True)
+    verts, faces = DiffDMC(dtype=torch.float32)(sdf, deform, isovalue=0.0, return_quads=False, normalize=True)
+
+The compute path is hand-written sm_103a CUDA behind the C ABI of
+include/diso_gb300.h; there is no CPU path.
+"""
+from .extract import DiffDMC, DiffMC, extract  # noqa: F401
+
+__all__ = ["DiffMC", "DiffDMC", "extract"]
+__version__ = "0.1.0"

@@ -1,0 +1,156 @@
+"""ctypes binding of the C ABI in include/diso_gb300.h (libdiso_gb300.so).
+
+The library is built in-tree by ``diso_gb300.build.build()`` (called from
+``__graft_entry__.build()``).  There is no fallback: if the library is missing
+or fails to load, every extraction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdiso_gb300.so")
+
+MC, DMC = 0, 1
+F32, F64 = 0, 1
+GRAD_EXACT = 1
+
+_lock = threading.Lock()
+_lib = None
+
+
+class Counts(ctypes.Structure):
+    _fields_ = [
+        ("n_verts", ctypes.c_int64),
+        ("n_faces", ctypes.c_int64),
+        ("sdf_min", ctypes.c_double),
+        ("sdf_max", ctypes.c_double),
+        ("empty", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("n_active_tiles", ctypes.c_int64),
+    ]
+
+
+EXPORTS = {
+    # name: (restype, argtypes)
+    "diso_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "diso_destroy": (None, [ctypes.c_void_p]),
+    "diso_segment_slots": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "diso_forward_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.POINTER(Counts)]),
+    "diso_forward_emit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
+    "diso_split_quads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
+    "diso_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p]),
+    "diso_last_error": (ctypes.c_char_p, []),
+    "diso_version": (ctypes.c_char_p, []),
+}
+
+
+def lib():
+    """The loaded library; raises RuntimeError when it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"diso_gb300: CUDA library {LIB_PATH} is missing; build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'`")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in EXPORTS.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        msg = lib().diso_last_error().decode(errors="replace")
+        raise RuntimeError(f"diso_gb300 {what} failed (status {rc}): {msg}")
+
+
+def dtype_tag(dtype: torch.dtype) -> int:
+    if dtype == torch.float32:
+        return F32
+    if dtype == torch.float64:
+        return F64
+    raise ValueError(f"diso_gb300 supports float32 and float64, got {dtype}")
+
+
+def iso_values(isovalue: float, dtype: torch.dtype):
+    """(iso, padval) as the reference's kernels see them: the isovalue in the
+    grid's dtype and the pad value isovalue + 1 computed in Python and then
+    rounded to that dtype (diso/__init__.py:52)."""
+    iso = float(isovalue)
+    if dtype == torch.float32:
+        return float(np.float32(iso)), float(np.float32(iso + 1.0))
+    return iso, iso + 1.0
+
+
+def ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_of(device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class Extractor:
+    """Owner of one native extractor (method x dtype) and its scratch."""
+
+    def __init__(self, method: int, dtype: torch.dtype):
+        self.method = method
+        self.dtype = dtype
+        self._h = ctypes.c_void_p()
+        check(lib().diso_create(method, dtype_tag(dtype), ctypes.byref(self._h)), "create")
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().diso_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def segment_slots(shape) -> int:
+        return int(lib().diso_segment_slots(*shape))
+
+    def count(self, sdf, iso, pad, seg) -> Counts:
+        c = Counts()
+        check(lib().diso_forward_count(self._h, ptr(sdf), *sdf.shape, iso, pad, ptr(seg),
+                                       stream_of(sdf.device), ctypes.byref(c)), "forward count")
+        return c
+
+    def emit(self, sdf, deform, iso, pad, seg, normalize, verts, faces):
+        check(lib().diso_forward_emit(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),
+                                      int(bool(normalize)), ptr(verts), ptr(faces), stream_of(sdf.device)),
+              "forward emit")
+
+    def split(self, verts, quads, tris) -> int:
+        n = ctypes.c_int64(0)
+        check(lib().diso_split_quads(self._h, ptr(verts), ptr(quads), quads.shape[0], ptr(tris), ctypes.byref(n),
+                                     stream_of(verts.device)), "quad split")
+        return int(n.value)
+
+    def backward(self, sdf, deform, iso, pad, seg, normalize, grad_verts, grad_sdf, grad_deform, exact=False):
+        check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),
+                                  int(bool(normalize)), GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_sdf),
+                                  ptr(grad_deform), stream_of(sdf.device)), "backward")

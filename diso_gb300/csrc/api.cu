@@ -1,0 +1,332 @@
+// Host side of the C ABI declared in include/diso_gb300.h: argument checks,
+// scratch management and kernel launches on the caller's stream.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <new>
+
+#include "../../include/diso_gb300.h"
+#include "kernels.cuh"
+#include "scan.cuh"
+
+using namespace diso;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess) return fail(DISO_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+}  // namespace
+
+struct diso_extractor {
+  int method = 0, dtype = 0, device = -1;
+  Stats* stats = nullptr;        // device status words
+  Stats* stats_host = nullptr;   // pinned mirror
+  uint32_t* scan_flag = nullptr; // look-back state
+  uint64_t* scan_agg = nullptr;
+  uint64_t* scan_incl = nullptr;
+  int64_t scan_cap = 0;          // look-back tiles
+  int* active = nullptr;         // tiles with crossings (forward)
+  int64_t active_cap = 0;
+  uint64_t* split = nullptr;     // split counts (n_quads + 1)
+  int64_t split_cap = 0;
+  int64_t last_active = 0;       // from the last forward count
+
+  void release() {
+    cudaFree(stats);
+    cudaFreeHost(stats_host);
+    cudaFree(scan_flag);
+    cudaFree(scan_agg);
+    cudaFree(scan_incl);
+    cudaFree(active);
+    cudaFree(split);
+    stats = nullptr;
+    stats_host = nullptr;
+    scan_flag = nullptr;
+    scan_agg = scan_incl = split = nullptr;
+    active = nullptr;
+    scan_cap = active_cap = split_cap = 0;
+  }
+};
+
+namespace {
+
+template <class T>
+int grow(T*& p, int64_t& cap, int64_t need) {
+  if (need <= cap) return DISO_OK;
+  int64_t n = need + need / 4 + 1024;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  CUDA_TRY(cudaMalloc((void**)&p, (size_t)n * sizeof(T)));
+  cap = n;
+  return DISO_OK;
+}
+
+int bind_device(diso_extractor* ex) {
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (ex->device != dev) {
+    ex->release();
+    ex->device = dev;
+  }
+  if (!ex->stats) {
+    CUDA_TRY(cudaMalloc((void**)&ex->stats, sizeof(Stats)));
+    CUDA_TRY(cudaMallocHost((void**)&ex->stats_host, sizeof(Stats)));
+  }
+  return DISO_OK;
+}
+
+int reset_stats(diso_extractor* ex, cudaStream_t s) {
+  CUDA_TRY(cudaMemsetAsync(ex->stats, 0, sizeof(Stats), s));
+  CUDA_TRY(cudaMemsetAsync(&ex->stats->min_key, 0xff, sizeof(unsigned long long), s));
+  return DISO_OK;
+}
+
+// exclusive look-back scan of a[0..n) in place, a[n] = total
+int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s) {
+  const int64_t tiles = (n + 1 + SCAN_TILE - 1) / SCAN_TILE;
+  if (tiles > ex->scan_cap) {
+    cudaFree(ex->scan_flag);
+    cudaFree(ex->scan_agg);
+    cudaFree(ex->scan_incl);
+    ex->scan_flag = nullptr;
+    ex->scan_agg = ex->scan_incl = nullptr;
+    ex->scan_cap = 0;
+    const int64_t cap = tiles + tiles / 4 + 64;
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_flag, (size_t)cap * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_agg, (size_t)cap * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_incl, (size_t)cap * sizeof(uint64_t)));
+    ex->scan_cap = cap;
+  }
+  CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
+  CUDA_TRY(cudaMemsetAsync(&ex->stats->scan_tile, 0, sizeof(unsigned long long), s));
+  ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+int check_common(diso_extractor* ex, const void* sdf, int nx, int ny, int nz) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (!sdf) return fail(DISO_ERR_ARG, "null sdf");
+  if (nx < 1 || ny < 1 || nz < 1) return fail(DISO_ERR_ARG, "grid dims must be >= 1 (got %d x %d x %d)", nx, ny, nz);
+  // crossings are counted in 32 bits per half of the scan value: at most 3 per cell
+  double cells = (double)(nx + 1) * (ny + 1) * (nz + 1);
+  if (3.0 * cells >= 2147483647.0) return fail(DISO_ERR_ARG, "grid too large: %d x %d x %d", nx, ny, nz);
+  return bind_device(ex);
+}
+
+template <class S>
+Field<S> make_field(const void* sdf, const void* deform, int nx, int ny, int nz, double iso, double padval) {
+  Field<S> f;
+  f.sdf = (const S*)sdf;
+  f.def = (const S*)deform;
+  f.n0 = nx;
+  f.n1 = ny;
+  f.n2 = nz;
+  f.iso = (S)iso;
+  f.pad = (S)padval;
+  return f;
+}
+
+template <class S>
+int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double iso, double padval,
+                  uint64_t* seg, cudaStream_t s, diso_counts* out) {
+  Geom g;
+  g.init(nx, ny, nz);
+  int rc;
+  if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
+  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
+  if (ex->method == DISO_MC)
+    count_kernel<S, MC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, ex->stats, ex->active);
+  else
+    count_kernel<S, DMC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, ex->stats, ex->active);
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  uint64_t total = 0;
+  CUDA_TRY(cudaMemcpyAsync(&total, seg + g.nseg, sizeof total, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  const Stats& h = *ex->stats_host;
+  if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
+  // the low half counts crossings, the high half triangles (MC) or patches (DMC)
+  if (ex->method == DISO_MC) {
+    out->n_verts = Counts::lo(total);
+    out->n_faces = Counts::hi(total);
+  } else {
+    out->n_verts = Counts::hi(total);
+    out->n_faces = Counts::lo(total);
+  }
+  out->sdf_min = key_to_double(h.min_key);
+  out->sdf_max = key_to_double(h.max_key);
+  const double isoS = (double)(S)iso;
+  out->empty = (out->sdf_min >= isoS || out->sdf_max <= isoS) ? 1 : 0;
+  out->pad_ = 0;
+  out->n_active_tiles = (int64_t)h.n_active;
+  ex->last_active = out->n_active_tiles;
+  return DISO_OK;
+}
+
+template <class S>
+int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
+                 double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, cudaStream_t s) {
+  Geom g;
+  g.init(nx, ny, nz);
+  if (ex->last_active <= 0) return DISO_OK;
+  Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
+  const unsigned grid = (unsigned)ex->last_active;
+  if (ex->method == DISO_MC)
+    mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize);
+  else
+    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+template <class S>
+int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
+             double padval, const uint64_t* seg, int normalize, int flags, const void* gv, void* gsdf, void* gdef,
+             cudaStream_t s) {
+  Geom g;
+  g.init(nx, ny, nz);
+  Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
+  const unsigned grid = (unsigned)g.nptiles();
+  if (ex->method == DISO_MC)
+    mc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, (const S*)gv, normalize, (S*)gsdf, (S*)gdef);
+  else
+    dmc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, (const S*)gv, normalize,
+                                                     (flags & DISO_GRAD_EXACT) ? 1 : 0, (S*)gsdf, (S*)gdef);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+template <class S>
+int split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int64_t nq, int64_t* tris,
+                int64_t* n_tris, cudaStream_t s) {
+  int rc;
+  if ((rc = grow(ex->split, ex->split_cap, nq + 1)) != DISO_OK) return rc;
+  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((nq + threads - 1) / threads);
+  split_count_kernel<S><<<blocks, threads, 0, s>>>((const S*)verts, quads, nq, ex->split);
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = run_scan(ex, ex->split, nq, s)) != DISO_OK) return rc;
+  split_scatter_kernel<<<blocks, threads, 0, s>>>(quads, nq, ex->split, tris);
+  CUDA_TRY(cudaGetLastError());
+  uint64_t total = 0;
+  CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(&total, ex->split + nq, sizeof total, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (ex->stats_host->error & 1ull) return fail(DISO_ERR_SCAN, "split scan: look-back wait gave up");
+  *n_tris = 2 * ((int64_t)Counts::lo(total) + (int64_t)Counts::hi(total));
+  return DISO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int diso_create(int method, int dtype, diso_extractor** out) {
+  if (!out) return fail(DISO_ERR_ARG, "null output pointer");
+  if (method != DISO_MC && method != DISO_DMC) return fail(DISO_ERR_ARG, "unknown method %d", method);
+  if (dtype != DISO_F32 && dtype != DISO_F64) return fail(DISO_ERR_ARG, "unknown dtype %d", dtype);
+  diso_extractor* ex = new (std::nothrow) diso_extractor();
+  if (!ex) return fail(DISO_ERR_ARG, "out of host memory");
+  ex->method = method;
+  ex->dtype = dtype;
+  *out = ex;
+  return DISO_OK;
+}
+
+void diso_destroy(diso_extractor* ex) {
+  if (!ex) return;
+  if (ex->device >= 0) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(ex->device);
+    ex->release();
+    cudaSetDevice(cur);
+  }
+  delete ex;
+}
+
+int64_t diso_segment_slots(int nx, int ny, int nz) {
+  if (nx < 1 || ny < 1 || nz < 1) return 0;
+  Geom g;
+  g.init(nx, ny, nz);
+  return g.nseg + 1;
+}
+
+int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double isovalue, double padval,
+                       uint64_t* seg, void* stream, diso_counts* out) {
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc) return rc;
+  if (!seg || !out) return fail(DISO_ERR_ARG, "null seg or counts");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? forward_count<float>(ex, sdf, nx, ny, nz, isovalue, padval, seg, s, out)
+                               : forward_count<double>(ex, sdf, nx, ny, nz, isovalue, padval, seg, s, out);
+}
+
+int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
+                      double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
+                      int64_t* faces, void* stream) {
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc) return rc;
+  if (!seg || !verts || !faces) return fail(DISO_ERR_ARG, "null seg, verts or faces");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32
+             ? forward_emit<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, verts, faces, s)
+             : forward_emit<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, verts, faces, s);
+}
+
+int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int64_t n_quads, int64_t* tris,
+                     int64_t* n_tris, void* stream) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (ex->method != DISO_DMC) return fail(DISO_ERR_ARG, "quad split needs a DMC extractor");
+  if (!n_tris || n_quads < 0) return fail(DISO_ERR_ARG, "bad quad count");
+  *n_tris = 0;
+  if (n_quads == 0) return DISO_OK;
+  if (!verts || !quads || !tris) return fail(DISO_ERR_ARG, "null verts, quads or tris");
+  int rc = bind_device(ex);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? split_quads<float>(ex, verts, quads, n_quads, tris, n_tris, s)
+                               : split_quads<double>(ex, verts, quads, n_quads, tris, n_tris, s);
+}
+
+int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
+                  double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
+                  void* grad_sdf, void* grad_deform, void* stream) {
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc) return rc;
+  if (!seg || !grad_sdf) return fail(DISO_ERR_ARG, "null seg or grad_sdf");
+  if (deform && !grad_deform) return fail(DISO_ERR_ARG, "deform given without grad_deform");
+  if (!grad_verts) return fail(DISO_ERR_ARG, "null grad_verts");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? backward<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, flags,
+                                                 grad_verts, grad_sdf, deform ? grad_deform : nullptr, s)
+                               : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
+                                                  flags, grad_verts, grad_sdf, deform ? grad_deform : nullptr, s);
+}
+
+const char* diso_last_error(void) { return g_err; }
+
+const char* diso_version(void) { return "diso_gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

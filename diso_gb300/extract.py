@@ -1,0 +1,132 @@
+"""DiffMC / DiffDMC: drop-in replacements of the reference's nn.Modules
+(diso/__init__.py:9-147) over the native extractor.
+
+Differences that are invisible to callers of the reference API:
+
+* the one-voxel pad (diso/__init__.py:52-54) is virtual, so no padded copies of
+  the grid or the deform are made, and the gradients come back unpadded
+  directly;
+* the empty-surface guard (diso/__init__.py:49, 103) reuses the min/max that the
+  counting kernel computes, so a forward synchronises with the host once (the
+  reference syncs for min, max and three output sizes);
+* the backward does not re-run the forward (diso/__init__.py:32, 86): it
+  recomputes crossings, codes and vertex indices from the SDF inside one kernel
+  that writes every gradient element once, deterministically (no atomics);
+* vertices are shifted and normalised, and faces written as int64, inside the
+  kernels; the DMC quad split runs on the GPU in one pass plus a scan.
+
+The outputs are the reference's: the same vertex, face and quad order, the same
+dtypes, including the int32 empty faces of the guard.
+"""
+from __future__ import annotations
+
+import torch
+from torch import nn
+from torch.autograd import Function
+
+from . import _native as N
+
+
+def _check_inputs(grid, deform, dtype):
+    if not grid.is_cuda:
+        raise RuntimeError("grid must be a CUDA tensor")
+    if grid.dim() != 3:
+        raise RuntimeError(f"grid must be [X, Y, Z], got shape {tuple(grid.shape)}")
+    if grid.dtype != dtype:
+        raise RuntimeError("grid type must match the mc class")
+    if deform is not None:
+        if not deform.is_cuda or deform.device != grid.device:
+            raise RuntimeError("deform must be a CUDA tensor on the grid's device")
+        if deform.dtype != dtype:
+            raise RuntimeError("deformation type must match the mc class")
+        if tuple(deform.shape) != tuple(grid.shape) + (3,):
+            raise RuntimeError(f"deform must be [X, Y, Z, 3], got {tuple(deform.shape)}")
+
+
+class _ExtractFunction(Function):
+    """Autograd node of one extraction; the counterpart of DMCFunction /
+    DDMCFunction (diso/__init__.py:18-46, 72-100)."""
+
+    @staticmethod
+    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad):
+        g = grid.detach().contiguous()
+        d = deform.detach().contiguous() if deform is not None else None
+        nv, nf = int(counts.n_verts), int(counts.n_faces)
+        width = 3 if ex.method == N.MC else 4
+        verts = torch.empty((nv, 3), dtype=g.dtype, device=g.device)
+        faces = torch.empty((nf, width), dtype=torch.int64, device=g.device)
+        ex.emit(g, d, iso, pad, seg, normalize, verts, faces)
+        if ex.method == N.DMC and not return_quads:
+            tris = torch.empty((2 * nf, 3), dtype=torch.int64, device=g.device)
+            n = ex.split(verts, faces, tris)
+            faces = tris[:n]
+        ctx.ex = ex
+        ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
+        ctx.has_deform = deform is not None
+        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg)
+        ctx.mark_non_differentiable(faces)
+        return verts, faces
+
+    @staticmethod
+    def backward(ctx, grad_verts, grad_faces):
+        grid, deform, seg = ctx.saved_tensors
+        g = grid.detach().contiguous()
+        d = deform.detach().contiguous() if ctx.has_deform else None
+        with torch.cuda.device(g.device):
+            if grad_verts is None:
+                grad_verts = torch.zeros(0, 3, dtype=g.dtype, device=g.device)
+            gv = grad_verts.contiguous()
+            gs = torch.empty_like(g)
+            gd = torch.empty_like(d) if d is not None else None
+            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, ctx.normalize, gv, gs, gd, ctx.exact_grad)
+        return gs, gd, None, None, None, None, None, None, None, None
+
+
+def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
+            exact_grad=False):
+    """One differentiable extraction with the reference's semantics.
+
+    exact_grad (DMC only) replaces the reference's backward in cells with several
+    patches, where every patch receives the first patch's gradient
+    (src/cudualmc.cu:990), by the true derivative."""
+    _check_inputs(grid, deform, ex.dtype)
+    iso, pad = N.iso_values(isovalue, ex.dtype)
+    with torch.cuda.device(grid.device):
+        g = grid.detach().contiguous()
+        seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=g.device)
+        counts = ex.count(g, iso, pad, seg)
+        if counts.empty:
+            width = 3 if ex.method == N.MC else 4
+            return (torch.zeros((0, 3), dtype=ex.dtype, device=grid.device),
+                    torch.zeros((0, width), dtype=torch.int32, device=grid.device))
+        return _ExtractFunction.apply(grid, deform, ex, seg, counts, iso, pad, bool(normalize), bool(return_quads),
+                                      bool(exact_grad))
+
+
+class DiffMC(nn.Module):
+    """Differentiable marching cubes (diso/__init__.py:9-61)."""
+
+    def __init__(self, dtype=torch.float32):
+        super().__init__()
+        self.dtype = dtype
+        self._ex = N.Extractor(N.MC, dtype)
+
+    def forward(self, grid, deform=None, isovalue=0.0, normalize=True):
+        return extract(self._ex, grid, deform, isovalue, normalize)
+
+
+class DiffDMC(nn.Module):
+    """Differentiable dual marching cubes (diso/__init__.py:63-147).
+
+    ``exact_grad=True`` (keyword only, not in the reference) gives the true
+    derivative in cells with several patches; the default reproduces the
+    reference's gradient there (every patch gets the first patch's gradient)."""
+
+    def __init__(self, dtype=torch.float32, *, exact_grad=False):
+        super().__init__()
+        self.dtype = dtype
+        self.exact_grad = exact_grad
+        self._ex = N.Extractor(N.DMC, dtype)
+
+    def forward(self, grid, deform=None, isovalue=0.0, return_quads=False, normalize=True):
+        return extract(self._ex, grid, deform, isovalue, normalize, return_quads, self.exact_grad)

@@ -1,0 +1,125 @@
+/*
+ * C ABI of the GB300 differentiable iso-surface extractor.
+ *
+ * This is the boundary a binding of the reference's extension would call instead
+ * of its pybind11 classes CUMCFloat / CUMCDouble / CUDMCFloat / CUDMCDouble
+ * (src/pybind.cpp:13-397, registered at src/pybind.cpp:419-447).  Every entry
+ * point takes plain device pointers, sizes, the isovalue and a CUDA stream
+ * (cudaStream_t passed as void*; NULL = the legacy default stream), and returns
+ * a status code (DISO_OK = 0); diso_last_error() gives the message of the last
+ * failure on the calling thread.  No exception crosses the ABI.
+ *
+ * Layouts are the reference's: sdf [nx][ny][nz] (z fastest), deform
+ * [nx][ny][nz][3], verts [V][3], faces [F][3] (MC, DMC triangles) or [F][4]
+ * (DMC quads) as int64.  The pad of one voxel that the reference's Python layer
+ * adds (diso/__init__.py:52-54) is applied virtually: pass the unpadded grid and
+ * padval = isovalue + 1 rounded to the grid's dtype.  Vertices come out already
+ * shifted and, with normalize != 0, divided by (dim - 1) (diso/__init__.py:56-60).
+ *
+ * A forward is two calls.  diso_forward_count classifies every cell, scans the
+ * per-row-segment counts into the caller's `seg` array and returns the output
+ * sizes (one device-to-host copy, the only synchronisation of the forward);
+ * the caller then allocates verts/faces and calls diso_forward_emit with the
+ * same inputs and `seg`.  `seg` (diso_segment_slots() uint64 values) is all the
+ * per-call state: keep it to run diso_backward later; the backward recomputes
+ * every crossing, case code and vertex index from the SDF.
+ *
+ * An extractor owns small scratch buffers (scan look-back state, the list of
+ * tiles with crossings, status words) that grow on demand; calls on one
+ * extractor must not overlap, and diso_forward_emit must follow the
+ * diso_forward_count of the same grid on that extractor.
+ */
+#ifndef DISO_GB300_H
+#define DISO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { DISO_MC = 0, DISO_DMC = 1 };
+enum { DISO_F32 = 0, DISO_F64 = 1 };
+enum { DISO_GRAD_EXACT = 1 }; /* diso_backward flag, see there */
+enum {
+  DISO_OK = 0,
+  DISO_ERR_ARG = 1,      /* bad argument (size, null pointer, method, dtype) */
+  DISO_ERR_CUDA = 2,     /* a CUDA call failed */
+  DISO_ERR_SCAN = 3,     /* the look-back scan gave up waiting on a predecessor */
+  DISO_ERR_CAPACITY = 4, /* an output would exceed the caller's capacity */
+};
+
+typedef struct diso_extractor diso_extractor;
+
+typedef struct {
+  int64_t n_verts;        /* MC: crossing edges; DMC: patches (dual vertices) */
+  int64_t n_faces;        /* MC: triangles; DMC: quads (= crossing edges) */
+  double sdf_min;         /* min and max of the (unpadded) SDF */
+  double sdf_max;
+  int32_t empty;          /* 1 when the reference's guard returns an empty mesh:
+                             min >= isovalue or max <= isovalue (diso/__init__.py:49, 103) */
+  int32_t pad_;
+  int64_t n_active_tiles; /* 4x8x32-cell tiles holding at least one crossing */
+} diso_counts;
+
+/* Create an extractor for method DISO_MC / DISO_DMC and dtype DISO_F32 / DISO_F64.
+ * Replaces constructing CUMCFloat, CUMCDouble, CUDMCFloat or CUDMCDouble
+ * (src/pybind.cpp:419-447; diso/__init__.py:10-16, 64-70). */
+int diso_create(int method, int dtype, diso_extractor** out);
+
+/* Free the extractor's scratch (the reference's ~CUMC / ~CUDMC, src/pybind.cpp:27-39, 219-232). */
+void diso_destroy(diso_extractor* ex);
+
+/* Number of uint64 slots of the per-call `seg` array for an nx*ny*nz grid. */
+int64_t diso_segment_slots(int nx, int ny, int nz);
+
+/* Forward, phase 1: case codes, counts, scan and the empty-surface guard.
+ * Replaces CuMC::forward / CUDualMC::forward up to their last scan
+ * (src/cumc.cu:651-723, src/cudualmc.cu:1058-1122), the guard's min/max
+ * (diso/__init__.py:49, 103) and the pad (diso/__init__.py:52-54). */
+int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double isovalue, double padval,
+                       uint64_t* seg, void* stream, diso_counts* out);
+
+/* Forward, phase 2: writes verts [n_verts][3] (grid dtype) and faces as int64
+ * [n_faces][3] (MC) or [n_faces][4] (DMC quads).  deform may be NULL.
+ * Replaces create_cell_mc_verts / create_cell_mc_tris (src/cumc.cu:370-410, 564-649),
+ * index_cell_mc_verts / create_dmc_verts / create_quads (src/cudualmc.cu:753-794,
+ * 907-955, 1027-1056), the outputs' clone (src/pybind.cpp:78-87, 271-280) and the
+ * shift / normalisation (diso/__init__.py:56-60). */
+int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
+                      double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
+                      int64_t* faces, void* stream);
+
+/* DMC quads -> triangles: for each quad the triangle pair with the smaller largest
+ * corner cosine, config (0,1,3),(1,2,3) first for all quads that pick it, then
+ * (0,1,2),(0,2,3) (diso/__init__.py:118-147).  tris must hold 2*n_quads rows;
+ * *n_tris receives the rows written (fewer only when a quad's angles are NaN,
+ * which the reference also drops).  Synchronises the stream. */
+int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int64_t n_quads, int64_t* tris,
+                     int64_t* n_tris, void* stream);
+
+/* Backward: dL/dsdf [nx][ny][nz] and dL/ddeform [nx][ny][nz][3] (when deform is
+ * not NULL) from dL/dverts [n_verts][3] of the final (shifted, normalised)
+ * vertices.  Every element of both outputs is written; nothing needs zeroing.
+ * flags = 0 reproduces the reference's gradients exactly, including its DMC
+ * backward, which hands every patch of a multi-patch cell the gradient of the
+ * cell's first patch (src/cudualmc.cu:990); flags = DISO_GRAD_EXACT gives the
+ * true derivative there instead.  MC is unaffected by the flag.
+ * Replaces DMCFunction.backward / DDMCFunction.backward (diso/__init__.py:30-44,
+ * 84-98: the forward re-run, the zero fills and the F.pad backward) and
+ * CuMC::backward / CUDualMC::backward (src/cumc.cu:734-743, src/cudualmc.cu:1130-1138). */
+int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
+                  double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
+                  void* grad_sdf, void* grad_deform, void* stream);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* diso_last_error(void);
+
+/* Library version string. */
+const char* diso_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DISO_GB300_H */

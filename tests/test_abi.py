@@ -1,0 +1,80 @@
+"""The C ABI library loads and exports every symbol include/diso_gb300.h declares;
+argument errors come back as status codes without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from helpers import ROOT
+
+HEADER = os.path.join(ROOT, "include", "diso_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*[a-z_0-9 ]+[ \*]+(diso_[a-z_0-9]+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from diso_gb300.build import build
+
+    build()
+    from diso_gb300 import _native
+
+    return _native.lib()
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    for want in ("diso_create", "diso_destroy", "diso_forward_count", "diso_forward_emit", "diso_backward",
+                 "diso_split_quads", "diso_segment_slots", "diso_last_error"):
+        assert want in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} missing from libdiso_gb300.so"
+
+
+def test_bindings_cover_the_header():
+    from diso_gb300 import _native
+
+    assert set(declared_functions()) <= set(_native.EXPORTS)
+
+
+def test_argument_errors_are_status_codes(lib):
+    h = ctypes.c_void_p()
+    assert lib.diso_create(7, 0, ctypes.byref(h)) == 1
+    assert b"unknown method" in lib.diso_last_error()
+    assert lib.diso_create(0, 5, ctypes.byref(h)) == 1
+    assert lib.diso_create(0, 0, ctypes.byref(h)) == 0 and h.value
+    from diso_gb300._native import Counts
+
+    c = Counts()
+    # invalid dims are rejected before any CUDA call
+    assert lib.diso_forward_count(h, ctypes.c_void_p(16), 0, 4, 4, 0.0, 1.0, ctypes.c_void_p(16), None,
+                                  ctypes.byref(c)) == 1
+    assert b"grid dims" in lib.diso_last_error()
+    assert lib.diso_forward_count(h, None, 4, 4, 4, 0.0, 1.0, ctypes.c_void_p(16), None, ctypes.byref(c)) == 1
+    n = ctypes.c_int64(5)
+    assert lib.diso_split_quads(h, None, None, 3, None, ctypes.byref(n), None) == 1  # MC extractor
+    lib.diso_destroy(h)
+
+
+def test_segment_slots(lib):
+    # cells (n+1)^3, rows cut into 32-cell chunks, plus the total slot
+    assert lib.diso_segment_slots(64, 64, 64) == 65 * 65 * 3 + 1
+    assert lib.diso_segment_slots(31, 5, 7) == 32 * 6 * 1 + 1
+    assert lib.diso_segment_slots(0, 5, 7) == 0
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from diso_gb300 import _native
+
+    monkeypatch.setattr(_native, "_lib", None)
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "nope.so"))
+    with pytest.raises(RuntimeError, match="missing"):
+        _native.lib()

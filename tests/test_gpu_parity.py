@@ -1,0 +1,201 @@
+"""Parity of the CUDA path (through the public DiffMC / DiffDMC API and the C ABI)
+with the reference's own outputs (golden fixtures) and with the CPU oracle."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import (assert_faces_equal, assert_grads_close, assert_verts_close, fixture_names, load_fixture)
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DT = {"float32": torch.float32, "float64": torch.float64}
+
+
+def run(case, sdf_np, def_np, weights=None, exact_grad=False, device="cuda:0"):
+    from diso_gb300 import DiffDMC, DiffMC
+
+    dt = DT[case["dtype"]]
+    sdf = torch.tensor(sdf_np, device=device, requires_grad=True)
+    deform = torch.tensor(def_np, device=device, requires_grad=True) if def_np is not None else None
+    if case["method"] == "mc":
+        verts, faces = DiffMC(dt)(sdf, deform, isovalue=case["iso"], normalize=case["normalize"])
+    else:
+        verts, faces = DiffDMC(dt, exact_grad=exact_grad)(sdf, deform, isovalue=case["iso"],
+                                                           return_quads=case["return_quads"],
+                                                           normalize=case["normalize"])
+    out = dict(verts=verts.detach().cpu().numpy(), faces=faces.cpu().numpy(), faces_dtype=str(faces.dtype))
+    if weights is not None and verts.shape[0]:
+        (verts * torch.tensor(weights, device=device)).sum().backward()
+        out["grad_sdf"] = sdf.grad.cpu().numpy()
+        if deform is not None:
+            out["grad_deform"] = deform.grad.cpu().numpy()
+    return out
+
+
+@pytest.mark.parametrize("name", fixture_names())
+def test_matches_reference_fixture(cuda_device, name):
+    fx = load_fixture(name)
+    c = fx["case"]
+    out = run(c, fx["sdf"], fx["deform"], fx.get("weights"))
+    assert out["faces_dtype"] == fx["faces_dtype"]
+    assert_verts_close(out["verts"], fx["verts"], c)
+    assert_faces_equal(out["faces"], fx["faces"], c, fx["verts"])
+    if "grad_sdf" in fx:
+        assert_grads_close(out["grad_sdf"], fx["grad_sdf"], c["dtype"], "grad_sdf")
+        if fx["deform"] is not None:
+            assert_grads_close(out["grad_deform"], fx["grad_deform"], c["dtype"], "grad_deform")
+
+
+def _field(kind, shape, rng):
+    if kind == "uniform":
+        return rng.uniform(-1, 1, shape)
+    axes = [np.linspace(-1, 1, n) for n in shape]
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+    if kind == "sphere":
+        return np.sqrt(X * X + Y * Y + Z * Z) - 0.5 + 0.02 * rng.standard_normal(shape)
+    if kind == "spheres":
+        s = np.full(shape, np.inf)
+        for _ in range(6):
+            c = rng.uniform(-0.7, 0.7, 3)
+            s = np.minimum(s, np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) - rng.uniform(0.1, 0.3))
+        return s + 0.01 * rng.standard_normal(shape)
+    raise ValueError(kind)
+
+
+ORACLE_CASES = [
+    # (method, dtype, field, shape, deform, iso, normalize, return_quads)
+    ("mc", "float32", "uniform", (48, 48, 48), 0.45, 0.0, True, False),
+    ("dmc", "float32", "uniform", (48, 48, 48), 0.45, 0.0, True, True),
+    ("dmc", "float32", "uniform", (33, 40, 35), 0.45, 0.1, True, False),
+    ("mc", "float64", "spheres", (37, 20, 65), 0.3, 0.0, True, False),
+    ("dmc", "float64", "spheres", (37, 20, 65), 0.3, 0.0, False, True),
+    ("dmc", "float64", "uniform", (70, 9, 33), None, -0.2, True, False),
+    ("mc", "float32", "sphere", (1, 1, 1), None, 0.0, True, False),
+    ("mc", "float32", "uniform", (1, 5, 3), None, 0.0, False, False),
+    ("dmc", "float32", "uniform", (2, 1, 64), 0.45, 0.0, True, True),
+    ("mc", "float32", "spheres", (128, 128, 128), 0.45, 0.0, True, False),
+    ("dmc", "float32", "spheres", (128, 128, 128), 0.45, 0.0, True, True),
+]
+
+
+@pytest.mark.parametrize("method,dtype,field,shape,deform,iso,normalize,rq", ORACLE_CASES)
+def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, normalize, rq):
+    rng = np.random.default_rng(abs(hash((method, dtype, field, shape))) % 2**32)
+    sdf = _field(field, shape, rng).astype(dtype)
+    dfm = rng.uniform(-deform, deform, shape + (3,)).astype(dtype) if deform else None
+    case = dict(method=method, dtype=dtype, iso=iso, normalize=normalize, return_quads=rq, shape=shape)
+    m = O.MC if method == "mc" else O.DMC
+    v_ref, f_ref, info = O.extract(m, sdf, dfm, iso, normalize, rq, dtype)
+    w = rng.standard_normal(v_ref.shape).astype(dtype)
+    out = run(case, sdf, dfm, w)
+    if info["empty_guard"]:
+        assert out["verts"].shape == (0, 3) and out["faces_dtype"] == "torch.int32"
+        return
+    assert_verts_close(out["verts"], v_ref, case)
+    assert_faces_equal(out["faces"], f_ref, case, v_ref)
+    gs, gd = O.backward(m, sdf, dfm, w, iso, normalize, dtype)
+    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf")
+    if dfm is not None:
+        assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform")
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_dmc_exact_gradient_matches_oracle(cuda_device, dtype):
+    rng = np.random.default_rng(4)
+    shape = (20, 21, 22)
+    sdf = rng.uniform(-1, 1, shape).astype(dtype)
+    dfm = rng.uniform(-0.4, 0.4, shape + (3,)).astype(dtype)
+    case = dict(method="dmc", dtype=dtype, iso=0.0, normalize=True, return_quads=True, shape=shape)
+    v_ref, _, _ = O.extract(O.DMC, sdf, dfm, 0.0, True, True, dtype)
+    w = rng.standard_normal(v_ref.shape).astype(dtype)
+    out = run(case, sdf, dfm, w, exact_grad=True)
+    gs, gd = O.backward(O.DMC, sdf, dfm, w, 0.0, True, dtype, exact=True)
+    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf")
+    assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform")
+
+
+@pytest.mark.parametrize("method", ["mc", "dmc"])
+def test_finite_differences_fp64(cuda_device, method):
+    """Central differences (h = 1e-6, float64) on 8 random SDF entries next to
+    crossings of a 32^3 grid, and on deform entries."""
+    from diso_gb300 import DiffDMC, DiffMC
+
+    rng = np.random.default_rng(8)
+    n = 32
+    base = torch.tensor(_field("spheres", (n, n, n), rng), device=cuda_device)
+    dfm = torch.tensor(rng.uniform(-0.3, 0.3, (n, n, n, 3)), device=cuda_device)
+    ext = DiffMC(torch.float64) if method == "mc" else DiffDMC(torch.float64, exact_grad=True)
+
+    def loss(s, d, w):
+        v = ext(s, d, return_quads=True)[0] if method == "dmc" else ext(s, d)[0]
+        return (v * w).sum()
+
+    s = base.clone().requires_grad_(True)
+    d = dfm.clone().requires_grad_(True)
+    v = ext(s, d)[0]
+    w = torch.tensor(rng.standard_normal(tuple(v.shape)), device=cuda_device)
+    loss(s, d, w).backward()
+    gs, gd = s.grad, d.grad
+    h = 1e-6
+    cand = torch.nonzero(gs.abs() > 1e-3).cpu().numpy()
+    for i in cand[rng.choice(len(cand), 8, replace=False)]:
+        i = tuple(int(k) for k in i)
+        sp, sm = base.clone(), base.clone()
+        sp[i] += h
+        sm[i] -= h
+        with torch.no_grad():
+            fd = (loss(sp, dfm, w) - loss(sm, dfm, w)).item() / (2 * h)
+        assert abs(fd - gs[i].item()) <= 1e-5 * max(1.0, abs(fd)), (i, fd, gs[i].item())
+    cand = torch.nonzero(gd.abs() > 1e-3).cpu().numpy()
+    for j in cand[rng.choice(len(cand), 4, replace=False)]:
+        j = tuple(int(k) for k in j)
+        dp, dm = dfm.clone(), dfm.clone()
+        dp[j] += h
+        dm[j] -= h
+        with torch.no_grad():
+            fd = (loss(base, dp, w) - loss(base, dm, w)).item() / (2 * h)
+        assert abs(fd - gd[j].item()) <= 1e-6 * max(1.0, abs(fd)), (j, fd, gd[j].item())
+
+
+def test_noncontiguous_inputs_and_side_stream(cuda_device):
+    from diso_gb300 import DiffMC
+
+    rng = np.random.default_rng(1)
+    base = torch.tensor(_field("spheres", (24, 30, 26), rng).astype(np.float32), device=cuda_device)
+    t = base.permute(2, 0, 1)  # non-contiguous view [26, 24, 30]
+    ref_v, ref_f, _ = O.extract(O.MC, t.contiguous().cpu().numpy(), None, 0.0, True, False, "float32")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        v, f = DiffMC(torch.float32)(t)
+    s.synchronize()
+    assert np.array_equal(f.cpu().numpy(), ref_f)
+    assert np.abs(v.cpu().numpy() - ref_v).max() < 1e-6
+
+
+def test_backward_is_deterministic(cuda_device):
+    from diso_gb300 import DiffDMC
+
+    rng = np.random.default_rng(2)
+    sdf = torch.tensor(rng.uniform(-1, 1, (40, 40, 40)).astype(np.float32), device=cuda_device)
+    grads = []
+    for _ in range(2):
+        s = sdf.clone().requires_grad_(True)
+        v, _ = DiffDMC(torch.float32)(s, return_quads=True)
+        (v * v).sum().backward()
+        grads.append(s.grad.clone())
+    assert torch.equal(grads[0], grads[1])
+
+
+def test_empty_guard_and_errors(cuda_device):
+    from diso_gb300 import DiffDMC, DiffMC
+
+    g = torch.ones(5, 6, 7, device=cuda_device)
+    v, f = DiffMC(torch.float32)(g)
+    assert v.shape == (0, 3) and f.shape == (0, 3) and f.dtype == torch.int32
+    v, f = DiffDMC(torch.float32)(g - 2, return_quads=False)
+    assert v.shape == (0, 3) and f.shape == (0, 4) and f.dtype == torch.int32
+    with pytest.raises(RuntimeError):
+        DiffMC(torch.float64)(g)
+    with pytest.raises(RuntimeError):
+        DiffMC(torch.float32)(g.cpu())
