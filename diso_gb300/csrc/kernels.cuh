@@ -99,7 +99,9 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
     }
     const uint32_t snv = warp_sum(nv), snf = warp_sum(nf);
     if (lane == 0 && row) seg[g.seg(X, Y, tz)] = Counts::pack(snv, snf);
-    tile_nv += snv;
+    // a cell can emit faces / patches without owning a crossing edge (its
+    // crossings may all sit on edges owned by its +1 neighbours)
+    tile_nv += snv + snf;
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) {

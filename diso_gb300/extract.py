@@ -26,6 +26,16 @@ from torch.autograd import Function
 
 from . import _native as N
 
+# Optional phase timer: when set to a callable, it is called as timer(name, "start"
+# | "end") around each native phase (count, emit, split, backward) on the
+# current stream; bench.py uses it to record CUDA events inside its timed region.
+phase_timer = None
+
+
+def _mark(name, what):
+    if phase_timer is not None:
+        phase_timer(name, what)
+
 
 def _check_inputs(grid, deform, dtype):
     if not grid.is_cuda:
@@ -55,10 +65,14 @@ class _ExtractFunction(Function):
         width = 3 if ex.method == N.MC else 4
         verts = torch.empty((nv, 3), dtype=g.dtype, device=g.device)
         faces = torch.empty((nf, width), dtype=torch.int64, device=g.device)
+        _mark("emit", "start")
         ex.emit(g, d, iso, pad, seg, normalize, verts, faces)
+        _mark("emit", "end")
         if ex.method == N.DMC and not return_quads:
             tris = torch.empty((2 * nf, 3), dtype=torch.int64, device=g.device)
+            _mark("split", "start")
             n = ex.split(verts, faces, tris)
+            _mark("split", "end")
             faces = tris[:n]
         ctx.ex = ex
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
@@ -78,7 +92,9 @@ class _ExtractFunction(Function):
             gv = grad_verts.contiguous()
             gs = torch.empty_like(g)
             gd = torch.empty_like(d) if d is not None else None
+            _mark("backward", "start")
             ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, ctx.normalize, gv, gs, gd, ctx.exact_grad)
+            _mark("backward", "end")
         return gs, gd, None, None, None, None, None, None, None, None
 
 
@@ -94,7 +110,9 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
     with torch.cuda.device(grid.device):
         g = grid.detach().contiguous()
         seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=g.device)
+        _mark("count", "start")
         counts = ex.count(g, iso, pad, seg)
+        _mark("count", "end")
         if counts.empty:
             width = 3 if ex.method == N.MC else 4
             return (torch.zeros((0, 3), dtype=ex.dtype, device=grid.device),

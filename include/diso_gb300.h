@@ -59,7 +59,7 @@ typedef struct {
   int32_t empty;          /* 1 when the reference's guard returns an empty mesh:
                              min >= isovalue or max <= isovalue (diso/__init__.py:49, 103) */
   int32_t pad_;
-  int64_t n_active_tiles; /* 4x8x32-cell tiles holding at least one crossing */
+  int64_t n_active_tiles; /* 4x8x32-cell tiles holding a crossing, a face or a patch */
 } diso_counts;
 
 /* Create an extractor for method DISO_MC / DISO_DMC and dtype DISO_F32 / DISO_F64.
