@@ -172,7 +172,7 @@ def measured_peaks():
 
 def run_ours(args, rank, world, device):
     from diso_gb300 import DiffDMC
-    import diso_gb300.extract as X
+    import diso_gb300.extraction as X
 
     n = args.n
     sdf = spheres_field(n, device)

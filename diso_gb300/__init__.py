@@ -9,7 +9,7 @@ Drop-in for the reference package's public API (diso/__init__.py):
 The compute path is hand-written sm_103a CUDA behind the C ABI of
 include/diso_gb300.h; there is no CPU path.
 """
-from .extract import DiffDMC, DiffMC, extract  # noqa: F401
+from .extraction import DiffDMC, DiffMC, extract  # noqa: F401
 
 __all__ = ["DiffMC", "DiffDMC", "extract"]
 __version__ = "0.1.0"
