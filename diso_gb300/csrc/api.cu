@@ -131,6 +131,9 @@ int check_common(diso_extractor* ex, const void* sdf, int nx, int ny, int nz) {
   return bind_device(ex);
 }
 
+// the per-call record: segment bases [nseg], the total [1], then one activity byte per forward tile
+inline uint8_t* tile_flags(const uint64_t* seg, const Geom& g) { return (uint8_t*)(seg + g.nseg + 1); }
+
 template <class S>
 Field<S> make_field(const void* sdf, const void* deform, int nx, int ny, int nz, double iso, double padval) {
   Field<S> f;
@@ -154,9 +157,11 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   if (ex->method == DISO_MC)
-    count_kernel<S, MC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, ex->stats, ex->active);
+    count_kernel<S, MC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats,
+                                                                  ex->active);
   else
-    count_kernel<S, DMC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, ex->stats, ex->active);
+    count_kernel<S, DMC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats,
+                                                                   ex->active);
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
@@ -208,9 +213,10 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const unsigned grid = (unsigned)g.nptiles();
   if (ex->method == DISO_MC)
-    mc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, (const S*)gv, normalize, (S*)gsdf, (S*)gdef);
+    mc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
+                                                    (S*)gsdf, (S*)gdef);
   else
-    dmc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, (const S*)gv, normalize,
+    dmc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
                                                      (flags & DISO_GRAD_EXACT) ? 1 : 0, (S*)gsdf, (S*)gdef);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
@@ -270,7 +276,7 @@ int64_t diso_segment_slots(int nx, int ny, int nz) {
   if (nx < 1 || ny < 1 || nz < 1) return 0;
   Geom g;
   g.init(nx, ny, nz);
-  return g.nseg + 1;
+  return g.nseg + 1 + (g.ntiles() + 7) / 8;
 }
 
 int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double isovalue, double padval,

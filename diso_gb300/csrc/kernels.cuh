@@ -63,9 +63,10 @@ __device__ __forceinline__ void tile_coords(int64_t tile, const Geom& g, int& X0
 
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
-                                                         Stats* stats, int* __restrict__ active) {
+                                                         uint8_t* __restrict__ tile_flag, Stats* stats,
+                                                         int* __restrict__ active) {
   __shared__ Window<S, TX + 1, TY + 1, TZ + 1> win;
-  __shared__ double red_min[TY], red_max[TY];
+  __shared__ S red_min[TY], red_max[TY];
   __shared__ uint32_t red_nv[TY];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t tile = blockIdx.x;
@@ -76,7 +77,9 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
   auto get = [&](int X, int Y, int Z) { return win.get(f, X0, Y0, Z0, X, Y, Z); };
 
   uint32_t tile_nv = 0;
-  double mn = __longlong_as_double(0x7ff0000000000000ll), mx = -mn;
+  // min / max of the caller's grid (the guard of diso/__init__.py:49), in the grid's dtype
+  S mn = f.pad, mx = f.pad;
+  bool any = false;
   const int Y = Y0 + warp, Z = Z0 + lane;
 #pragma unroll 1
   for (int ix = 0; ix < TX; ++ix) {
@@ -92,9 +95,10 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
         nf = dmc_npatch(dmc_case(dmc_resolve<S>(get, m, X, Y, Z, g.c, f.iso)));
       }
       if (X >= 1 && Y >= 1 && Z >= 1) {
-        const double v = (double)get(X, Y, Z);
-        mn = fmin(mn, v);
-        mx = fmax(mx, v);
+        const S v = get(X, Y, Z);
+        mn = any ? (v < mn ? v : mn) : v;
+        mx = any ? (v > mx ? v : mx) : v;
+        any = true;
       }
     }
     const uint32_t snv = warp_sum(nv), snf = warp_sum(nf);
@@ -103,28 +107,46 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
     // crossings may all sit on edges owned by its +1 neighbours)
     tile_nv += snv + snf;
   }
+  // lanes without an interior point hold the pad value, which never decides the guard
+  // because the guard only asks min >= iso or max <= iso of the interior values;
+  // replace them by a value already seen in the warp
+  const unsigned have = __ballot_sync(0xffffffffu, any);
+  if (have) {
+    const int src = __ffs(have) - 1;
+    const S m0 = __shfl_sync(0xffffffffu, mn, src), x0 = __shfl_sync(0xffffffffu, mx, src);
+    if (!any) {
+      mn = m0;
+      mx = x0;
+    }
 #pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    for (int o = 16; o; o >>= 1) {
+      const S a = __shfl_xor_sync(0xffffffffu, mn, o), b = __shfl_xor_sync(0xffffffffu, mx, o);
+      mn = a < mn ? a : mn;
+      mx = b > mx ? b : mx;
+    }
   }
   if (lane == 0) {
     red_min[warp] = mn;
     red_max[warp] = mx;
-    red_nv[warp] = tile_nv;
+    red_nv[warp] = tile_nv | (have ? 0x80000000u : 0u);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t t = 0;
+    bool seen = false;
     for (int w = 0; w < TY; ++w) {
-      mn = fmin(mn, red_min[w]);
-      mx = fmax(mx, red_max[w]);
-      t += red_nv[w];
+      if (red_nv[w] & 0x80000000u) {
+        mn = seen ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
+        mx = seen ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
+        seen = true;
+      }
+      t += red_nv[w] & 0x7fffffffu;
     }
-    if (mn <= mx) {
-      atomicMin(&stats->min_key, ord_key(mn));
-      atomicMax(&stats->max_key, ord_key(mx));
+    if (seen) {
+      atomicMin(&stats->min_key, ord_key((double)mn));
+      atomicMax(&stats->max_key, ord_key((double)mx));
     }
+    tile_flag[tile] = t ? 1 : 0;
     if (t) active[atomicAdd(&stats->n_active, 1ull)] = (int)tile;
   }
 }
@@ -376,26 +398,51 @@ __device__ __forceinline__ void edge_adjoint(const Field<S>& f, Get get, int X, 
 
 // Per point tile (unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ)), the
 // cells [x0, x0+TX] x ... (padded coordinates; cell x0+i owns point x0+i as corner 0)
-// are the cells whose owned edges touch the tile's points.  Returns false when no
-// segment of those cells has a crossing.
-__device__ __forceinline__ bool ptile_active(const Geom& g, const uint64_t* __restrict__ seg, int X0, int Y0, int zc,
-                                             bool use_hi) {
-  __shared__ int any;
-  if (threadIdx.x == 0) any = 0;
-  __syncthreads();
-  constexpr int CX = TX + 1, CY = TY + 1;
-  for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
-    const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
-    const int X = X0 + x, Y = Y0 + y, c = zc + k;
-    if (X < g.c[0] && Y < g.c[1] && c < g.nzc) {
-      const int64_t s = g.seg(X, Y, c);
-      const uint64_t a = seg[s], b = seg[s + 1];
-      const uint32_t n = use_hi ? Counts::hi(b) - Counts::hi(a) : Counts::lo(b) - Counts::lo(a);
-      if (n) any = 1;
+// own every edge that touches the tile's points.  They lie in the forward tiles
+// (x0/TX + {0,1}, y0/TY + {0,1}, z0/TZ + {0,1}); the tile is inactive when none of
+// them holds a crossing.
+__device__ __forceinline__ bool ptile_active(const Geom& g, const uint8_t* __restrict__ tile_flag, int x0, int y0,
+                                             int z0) {
+  int a = 0;
+  if (threadIdx.x < 8) {
+    const int tx = x0 / TX + (threadIdx.x & 1), ty = y0 / TY + ((threadIdx.x >> 1) & 1),
+              tz = z0 / TZ + (threadIdx.x >> 2);
+    if (tx < g.tiles_x() && ty < g.tiles_y() && tz < g.nzc) a = tile_flag[((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz];
+  }
+  return __syncthreads_or(a) != 0;
+}
+
+// zero dL/dsdf and dL/ddeform of a point tile; float4 stores when rows are 16-byte aligned
+template <class S>
+__device__ __forceinline__ void zero_ptile(const Field<S>& f, S* __restrict__ gsdf, S* __restrict__ gdef, int x0, int y0,
+                                           int z0) {
+  const int nz = min(TZ, f.n2 - z0);
+  if (sizeof(S) == 4 && (f.n2 & 3) == 0) {
+    const int r = threadIdx.x >> 3, k = threadIdx.x & 7;  // 32 rows x 8 float4
+    const int x = x0 + r / TY, y = y0 + r % TY;
+    if (x < f.n0 && y < f.n1) {
+      const int64_t base = ((int64_t)x * f.n1 + y) * f.n2 + z0;
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (4 * k < nz) reinterpret_cast<float4*>(gsdf + base)[k] = z4;
+      if (gdef) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int q = k + 8 * j;
+          if (4 * q < 3 * nz) reinterpret_cast<float4*>(gdef + 3 * base)[q] = z4;
+        }
+      }
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int ix = 0; ix < TX; ++ix) {
+    const int x = x0 + ix, y = y0 + warp, z = z0 + lane;
+    if (x < f.n0 && y < f.n1 && z < f.n2) {
+      const int64_t i = ((int64_t)x * f.n1 + y) * f.n2 + z;
+      gsdf[i] = S(0);
+      if (gdef) gdef[3 * i] = gdef[3 * i + 1] = gdef[3 * i + 2] = S(0);
     }
   }
-  __syncthreads();
-  return any != 0;
 }
 
 template <class S>
@@ -425,6 +472,7 @@ __device__ __forceinline__ void write_point_grads(const Field<S>& f, S* __restri
 // (src/cumc.cu:474-512) plus the zero fills and the F.pad backward.
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                               const uint8_t* __restrict__ tile_flag,
                                                                const S* __restrict__ gv, int normalize,
                                                                S* __restrict__ gsdf, S* __restrict__ gdef) {
   constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0, X0+TX] x ...
@@ -436,9 +484,8 @@ __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom 
   int X0, Y0, Z0;  // padded cell origin = unpadded point origin
   ptile_coords<S>(blockIdx.x, g, X0, Y0, Z0);
   const int zc = Z0 / TZ;
-  const S zero3[3] = {S(0), S(0), S(0)};
-  if (!ptile_active(g, seg, X0, Y0, zc, false)) {
-    for (int ix = 0; ix < TX; ++ix) write_point_grads<S>(f, gsdf, gdef, X0 + 1 + ix, Y0 + 1 + warp, Z0 + 1 + lane, S(0), zero3);
+  if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
+    zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
     return;
   }
   win.load(f, X0, Y0, Z0);
@@ -500,6 +547,7 @@ __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom 
 // reproduces that, exact = 1 uses each patch's own gradient (the true derivative).
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) dmc_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                                const uint8_t* __restrict__ tile_flag,
                                                                 const S* __restrict__ gv, int normalize, int exact,
                                                                 S* __restrict__ gsdf, S* __restrict__ gdef) {
   constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0, X0+TX] x ...
@@ -511,9 +559,8 @@ __global__ void __launch_bounds__(NTHREADS) dmc_backward_kernel(Field<S> f, Geom
   int X0, Y0, Z0;
   ptile_coords<S>(blockIdx.x, g, X0, Y0, Z0);
   const int zc = Z0 / TZ;
-  const S zero3[3] = {S(0), S(0), S(0)};
-  if (!ptile_active(g, seg, X0, Y0, zc, false)) {
-    for (int ix = 0; ix < TX; ++ix) write_point_grads<S>(f, gsdf, gdef, X0 + 1 + ix, Y0 + 1 + warp, Z0 + 1 + lane, S(0), zero3);
+  if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
+    zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
     return;
   }
   win.load(f, X0, Y0, Z0);

@@ -20,8 +20,9 @@
  * per-row-segment counts into the caller's `seg` array and returns the output
  * sizes (one device-to-host copy, the only synchronisation of the forward);
  * the caller then allocates verts/faces and calls diso_forward_emit with the
- * same inputs and `seg`.  `seg` (diso_segment_slots() uint64 values) is all the
- * per-call state: keep it to run diso_backward later; the backward recomputes
+ * same inputs and `seg`.  `seg` (diso_segment_slots() uint64 values: the
+ * scanned per-segment counts, their total and one activity byte per tile) is all
+ * the per-call state: keep it to run diso_backward later; the backward recomputes
  * every crossing, case code and vertex index from the SDF.
  *
  * An extractor owns small scratch buffers (scan look-back state, the list of
