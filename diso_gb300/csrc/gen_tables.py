@@ -219,6 +219,13 @@ def render(mc_words):
     enc = [s[0] | (s[1] << 1) | (s[2] << 2) | (a << 3) for s, a in EDGES]
     p("#define DISO_EDGE_TABLE {" + ", ".join(str(v) for v in enc) + "}")
     p("")
+    p("// edge id of the cell-local edge starting at corner s (bit0 = dx, bit1 = dy, bit2 = dz)")
+    p("// along axis a, at index 3 * s + a; 15 where no edge of the cell starts there")
+    lut = [15] * 24
+    for e, (st, a) in enumerate(EDGES):
+        lut[3 * (st[0] | (st[1] << 1) | (st[2] << 2)) + a] = e
+    p("#define DISO_EDGE_LOOKUP {" + ", ".join(str(v) for v in lut) + "}")
+    p("")
     p("// MC: bits 0-3 triangle count, then 4-bit edge ids, three per triangle")
     p("#define DISO_MC_TRIANGLES {\\")
     for i in range(0, 256, 4):

@@ -1,14 +1,23 @@
 // Forward and backward kernels of DiffMC / DiffDMC.
 //
-//   count_kernel      all tiles: case codes, per-segment crossing / face (MC) or
-//                     crossing / patch (DMC) counts, the min/max of the SDF for the
-//                     empty-surface guard, and the list of tiles with crossings
+//   count_kernel      all tiles: per-segment crossing / face (MC) or crossing / patch
+//                     (DMC) counts, the min/max of the SDF for the empty-surface
+//                     guard, one activity byte per tile and the list of active tiles
 //   scan              scan.cuh
 //   mc_emit_kernel    active tiles: MC vertices and triangles
 //   dmc_emit_kernel   active tiles: DMC dual vertices and quads
 //   *_backward_kernel all point tiles: dL/dsdf and dL/ddeform, every element written
 //                     once (zeros away from the surface), crossings recomputed
 //   split_*           DMC quad -> triangle split (return_quads=False)
+//
+// Row masks.  Every kernel first turns the SDF rows its tile needs into bit masks:
+// a warp reads 32 (+3) consecutive points of a row (X, Y) along z, coalesced, and
+// one ballot gives bit k = (value >= iso) of padded point (X, Y, Z0 - 1 + k).
+// From the masks of the four rows around a row of 32 cells, the cells' crossing
+// edges, which cells are non-trivial, each cell's case code and each cell's
+// offset inside its segment all follow from a few 64-bit logic ops and popcounts
+// (the warp ballot / popc compaction), so a row segment without surface costs a
+// handful of instructions.
 #pragma once
 #include "common.cuh"
 
@@ -16,12 +25,18 @@ namespace diso {
 
 enum Method { MC = 0, DMC = 1 };
 
+constexpr int MASK_TOP = 34;  // highest valid mask bit: points Z0-1 .. Z0+33
+
+__device__ const uint8_t g_edge_of[24] = DISO_EDGE_LOOKUP;
+
+// ------------------------------------------------------------------ geometry helpers
+
 // lerp vertex of the edge from padded point (X,Y,Z) along axis a, in padded
 // coordinates with deform (computeMcVert, src/cumc.cu:343-368)
-template <class S, class Get>
-__device__ __forceinline__ void edge_vertex(const Field<S>& f, Get get, int X, int Y, int Z, int a, S out[3]) {
+template <class S>
+__device__ __forceinline__ void edge_vertex(const Field<S>& f, int X, int Y, int Z, int a, S out[3]) {
   const int ex = a == 0, ey = a == 1, ez = a == 2;
-  const S d0 = get(X, Y, Z), d1 = get(X + ex, Y + ey, Z + ez);
+  const S d0 = f.at(X, Y, Z), d1 = f.at(X + ex, Y + ey, Z + ez);
   S t = S(0.5);
   if (d1 != d0) {
     S r = (f.iso - d0) / (d1 - d0);
@@ -59,95 +74,204 @@ __device__ __forceinline__ void tile_coords(int64_t tile, const Geom& g, int& X0
   Z0 = tz * TZ;
 }
 
+// cells Z0 + j (j < 32) that exist
+__device__ __forceinline__ uint32_t zvalid(const Geom& g, int Z0) {
+  const int n = g.c[2] - Z0;
+  return n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+}
+
+// ------------------------------------------------------------------ row masks
+
+// Fill m[x][y] for point rows (WX0 + x, WY0 + y); bit k = point Z0 - 1 + k >= iso.
+// Tracks min / max of the caller's (interior) values when TRACK.
+template <class S, int WX, int WY, bool TRACK>
+__device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+                                           S& mn, S& mx, bool& seen) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int Z = Z0 - 1 + lane, Ze = Z0 + 31 + lane;
+  const bool zin = (unsigned)(Z - 1) < (unsigned)f.n2;
+  const bool ein = lane < 3 && (unsigned)(Ze - 1) < (unsigned)f.n2;
+  for (int r = warp; r < WX * WY; r += nw) {
+    const int x = r / WY, y = r % WY, X = WX0 + x, Y = WY0 + y;
+    const bool row = (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
+    const S* p = f.sdf + ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
+    const S v = (row && zin) ? __ldg(p + Z) : f.pad;
+    const S e = (row && ein) ? __ldg(p + Ze) : f.pad;
+    const uint32_t lo = __ballot_sync(0xffffffffu, v >= f.iso);
+    const uint32_t hi = __ballot_sync(0xffffffffu, lane < 3 && e >= f.iso);
+    if (lane == 0) m[x][y] = (uint64_t)lo | ((uint64_t)(hi & 7u) << 32);
+    if (TRACK && row && zin) {
+      mn = seen ? (v < mn ? v : mn) : v;
+      mx = seen ? (v > mx ? v : mx) : v;
+      seen = true;
+    }
+  }
+}
+
+// Morton code from the four row masks around a cell: a = (x,y), b = (x+1,y),
+// c = (x,y+1), d = (x+1,y+1); s = bit of the cell's corner 0
+__device__ __forceinline__ int code8(uint64_t a, uint64_t b, uint64_t c, uint64_t d, int s) {
+  const uint64_t lo = ((a >> s) & 1) | (((b >> s) & 1) << 1) | (((c >> s) & 1) << 2) | (((d >> s) & 1) << 3);
+  const int t = s + 1;
+  const uint64_t hi = ((a >> t) & 1) | (((b >> t) & 1) << 1) | (((c >> t) & 1) << 2) | (((d >> t) & 1) << 3);
+  return (int)(lo | (hi << 4));
+}
+
+// Morton code of cell (X, Y, Z) from the masks when its corners are in the
+// window, otherwise from global memory
+template <class S, int WX, int WY>
+__device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+                                         int X, int Y, int Z) {
+  const unsigned x = (unsigned)(X - WX0), y = (unsigned)(Y - WY0);
+  const int s = Z - Z0 + 1;
+  if (x + 1 < (unsigned)WX && y + 1 < (unsigned)WY && s >= 0 && s + 1 <= MASK_TOP)
+    return code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], s);
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c |= (f.at(X + (i & 1), Y + ((i >> 1) & 1), Z + ((i >> 2) & 1)) >= f.iso) << i;
+  return c;
+}
+
+// DMC code after the face-neighbour ambiguity test (src/cudualmc.cu:815-839):
+// a "problematic" code looks at the cell across its ambiguous face; when that
+// (raw) code is problematic too, the code is complemented.
+template <class S, int WX, int WY>
+__device__ __forceinline__ int dmc_resolve_m(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+                                             int code, int X, int Y, int Z, const Geom& g) {
+  const int dir = dmc_dir(dmc_case(code));
+  if (dir == 7) return code;
+  const int comp = dir >> 1, d = (dir & 1) ? 1 : -1;
+  const int NX = X + (comp == 0 ? d : 0), NY = Y + (comp == 1 ? d : 0), NZ = Z + (comp == 2 ? d : 0);
+  const int nc = comp == 0 ? NX : (comp == 1 ? NY : NZ);
+  if (nc < 0 || nc >= g.c[comp]) return code;
+  const int ncode = cell_code<S>(m, f, WX0, WY0, Z0, NX, NY, NZ);
+  return dmc_dir(dmc_case(ncode)) != 7 ? (code ^ 0xff) : code;
+}
+
+// per row of 32 cells: crossing +x / +y / +z edges owned by each cell and the
+// non-trivial cells (case code not 0 or 255), one bit per cell
+struct RowBits {
+  uint32_t xc, yc, zc, nt;
+};
+
+__device__ __forceinline__ RowBits row_bits(uint64_t a, uint64_t b, uint64_t c, uint64_t d, uint32_t valid) {
+  const uint64_t a1 = a >> 1, b1 = b >> 1, c1 = c >> 1, d1 = d >> 1;
+  const uint64_t a2 = a >> 2, b2 = b >> 2, c2 = c >> 2, d2 = d >> 2;
+  const uint64_t o = a1 | b1 | c1 | d1 | a2 | b2 | c2 | d2;
+  const uint64_t n = a1 & b1 & c1 & d1 & a2 & b2 & c2 & d2;
+  RowBits r;
+  r.xc = (uint32_t)(a1 ^ b1) & valid;
+  r.yc = (uint32_t)(a1 ^ c1) & valid;
+  r.zc = (uint32_t)(a1 ^ a2) & valid;
+  r.nt = (uint32_t)(o & ~n) & valid;
+  return r;
+}
+
+// crossing flags (bit a = edge along axis a) of the cell at mask bit s (a cell past the
+// 32 of a row, e.g. the first cell of the next segment)
+__device__ __forceinline__ int flags_at(uint64_t a, uint64_t b, uint64_t c, int s) {
+  const int p = (int)((a >> s) & 1);
+  return (p ^ (int)((b >> s) & 1)) | ((p ^ (int)((c >> s) & 1)) << 1) | ((p ^ (int)((a >> (s + 1)) & 1)) << 2);
+}
+
+__device__ __forceinline__ int row_flags(const RowBits& r, int j) {
+  return (int)(((r.xc >> j) & 1) | (((r.yc >> j) & 1) << 1) | (((r.zc >> j) & 1) << 2));
+}
+
+// crossings owned by cells 0..j-1 of the row
+__device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
+  const uint32_t lo = (1u << j) - 1u;
+  return __popc(r.xc & lo) + __popc(r.yc & lo) + __popc(r.zc & lo);
+}
+
 // ------------------------------------------------------------------ count
 
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                          uint8_t* __restrict__ tile_flag, Stats* stats,
                                                          int* __restrict__ active) {
-  __shared__ Window<S, TX + 1, TY + 1, TZ + 1> win;
+  // MC needs the rows of the cells' corners, DMC also those of the face neighbours
+  // used by the ambiguity test
+  constexpr int H = METHOD == DMC ? 1 : 0;
+  constexpr int WX = TX + 1 + 2 * H, WY = TY + 1 + 2 * H;
+  __shared__ uint64_t m[WX][WY];
   __shared__ S red_min[TY], red_max[TY];
-  __shared__ uint32_t red_nv[TY];
+  __shared__ uint32_t red_any[TY];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t tile = blockIdx.x;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
-  win.load(f, X0, Y0, Z0);
-  __syncthreads();
-  auto get = [&](int X, int Y, int Z) { return win.get(f, X0, Y0, Z0, X, Y, Z); };
-
-  uint32_t tile_nv = 0;
-  // min / max of the caller's grid (the guard of diso/__init__.py:49), in the grid's dtype
+  const int WX0 = X0 - H, WY0 = Y0 - H;
   S mn = f.pad, mx = f.pad;
-  bool any = false;
-  const int Y = Y0 + warp, Z = Z0 + lane;
+  bool seen = false;
+  load_masks<S, WX, WY, true>(m, f, WX0, WY0, Z0, mn, mx, seen);
+  __syncthreads();
+
+  const uint32_t valid = zvalid(g, Z0);
+  uint32_t any = 0;
 #pragma unroll 1
-  for (int ix = 0; ix < TX; ++ix) {
-    const int X = X0 + ix;
-    const bool row = X < g.c[0] && Y < g.c[1];
-    uint32_t nv = 0, nf = 0;
-    if (row && Z < g.c[2]) {
-      const int m = morton_code<S>(get, X, Y, Z, f.iso);
-      nv = __popc(cross_flags(m));
-      if (METHOD == MC) {
-        nf = (uint32_t)(mc_tri(mc_from_morton(m)) & 15);
-      } else if (m != 0 && m != 255) {
-        nf = dmc_npatch(dmc_case(dmc_resolve<S>(get, m, X, Y, Z, g.c, f.iso)));
+  for (int si = warp; si < TX * TY; si += TY) {
+    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
+    if (X >= g.c[0] || Y >= g.c[1]) continue;
+    const int x = ix + H, y = iy + H;
+    const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
+    const RowBits r = row_bits(a, b, c, d, valid);
+    const uint32_t nv = __popc(r.xc) + __popc(r.yc) + __popc(r.zc);
+    uint32_t nf = 0;
+    if (r.nt) {
+      uint32_t mine = 0;
+      if ((r.nt >> lane) & 1) {
+        const int code = code8(a, b, c, d, lane + 1);
+        if (METHOD == MC)
+          mine = (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+        else
+          mine = dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + lane, g)));
       }
-      if (X >= 1 && Y >= 1 && Z >= 1) {
-        const S v = get(X, Y, Z);
-        mn = any ? (v < mn ? v : mn) : v;
-        mx = any ? (v > mx ? v : mx) : v;
-        any = true;
-      }
+      nf = warp_sum(mine);
     }
-    const uint32_t snv = warp_sum(nv), snf = warp_sum(nf);
-    if (lane == 0 && row) seg[g.seg(X, Y, tz)] = Counts::pack(snv, snf);
+    if (lane == 0) seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
     // a cell can emit faces / patches without owning a crossing edge (its
     // crossings may all sit on edges owned by its +1 neighbours)
-    tile_nv += snv + snf;
+    any |= nv | nf;
   }
-  // lanes without an interior point hold the pad value, which never decides the guard
-  // because the guard only asks min >= iso or max <= iso of the interior values;
-  // replace them by a value already seen in the warp
-  const unsigned have = __ballot_sync(0xffffffffu, any);
+  // min / max of the caller's grid (the guard of diso/__init__.py:49)
+  const unsigned have = __ballot_sync(0xffffffffu, seen);
   if (have) {
     const int src = __ffs(have) - 1;
     const S m0 = __shfl_sync(0xffffffffu, mn, src), x0 = __shfl_sync(0xffffffffu, mx, src);
-    if (!any) {
+    if (!seen) {
       mn = m0;
       mx = x0;
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
-      const S a = __shfl_xor_sync(0xffffffffu, mn, o), b = __shfl_xor_sync(0xffffffffu, mx, o);
-      mn = a < mn ? a : mn;
-      mx = b > mx ? b : mx;
+      const S p = __shfl_xor_sync(0xffffffffu, mn, o), q = __shfl_xor_sync(0xffffffffu, mx, o);
+      mn = p < mn ? p : mn;
+      mx = q > mx ? q : mx;
     }
   }
   if (lane == 0) {
     red_min[warp] = mn;
     red_max[warp] = mx;
-    red_nv[warp] = tile_nv | (have ? 0x80000000u : 0u);
+    red_any[warp] = (any ? 1u : 0u) | (have ? 2u : 0u);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t t = 0;
-    bool seen = false;
+    bool act = false, got = false;
     for (int w = 0; w < TY; ++w) {
-      if (red_nv[w] & 0x80000000u) {
-        mn = seen ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
-        mx = seen ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
-        seen = true;
+      act |= (red_any[w] & 1u) != 0;
+      if (red_any[w] & 2u) {
+        mn = got ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
+        mx = got ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
+        got = true;
       }
-      t += red_nv[w] & 0x7fffffffu;
     }
-    if (seen) {
+    if (got) {
       atomicMin(&stats->min_key, ord_key((double)mn));
       atomicMax(&stats->max_key, ord_key((double)mx));
     }
-    tile_flag[tile] = t ? 1 : 0;
-    if (t) active[atomicAdd(&stats->n_active, 1ull)] = (int)tile;
+    tile_flag[tile] = act ? 1 : 0;
+    if (act) active[atomicAdd(&stats->n_active, 1ull)] = (int)tile;
   }
 }
 
@@ -157,75 +281,78 @@ template <class S>
 __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                            const int* __restrict__ active, S* __restrict__ verts,
                                                            int64_t* __restrict__ faces, int normalize) {
-  constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ]
-  __shared__ Window<S, TX + 2, TY + 2, TZ + 2> win;     // points [X0, X0+TX+1] ...
-  __shared__ uint8_t flg[CX][CY][CZ];
-  __shared__ uint8_t pre[CX][CY][CZ];
+  constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
+  __shared__ uint64_t m[WX][WY];
+  __shared__ RowBits rb[CX][CY];
+  __shared__ uint8_t f32[CX][CY];  // flags of cell Z0+32 (first of the next segment)
   __shared__ uint32_t vb[CX][CY][2];
   __shared__ uint32_t fb[TX][TY];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
-  win.load(f, X0, Y0, Z0);
+  S dmn, dmx;
+  bool dseen = false;
+  load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
   for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
     const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
     const int X = X0 + x, Y = Y0 + y, zc = tz + k;
-    uint64_t s = (X < g.c[0] && Y < g.c[1] && zc < g.nzc) ? seg[g.seg(X, Y, zc)] : 0ull;
+    const uint64_t s = (X < g.c[0] && Y < g.c[1] && zc < g.nzc) ? seg[g.seg(X, Y, zc)] : 0ull;
     vb[x][y][k] = Counts::lo(s);
     if (k == 0 && x < TX && y < TY) fb[x][y] = Counts::hi(s);
   }
   __syncthreads();
-  auto get = [&](int X, int Y, int Z) { return win.get(f, X0, Y0, Z0, X, Y, Z); };
-
-  // crossing flags and in-segment prefixes of the tile's cells and their +1 halo
-  for (int r = warp; r < CX * CY; r += TY) {
-    const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
-    const bool row = X < g.c[0] && Y < g.c[1];
-    int fl = (row && Z0 + lane < g.c[2]) ? cross_flags(morton_code<S>(get, X, Y, Z0 + lane, f.iso)) : 0;
-    const uint32_t c = __popc(fl);
-    const uint32_t inc = warp_incl(c);
-    flg[x][y][lane] = (uint8_t)fl;
-    pre[x][y][lane] = (uint8_t)(inc - c);
-    if (lane == 0) {
-      const int Zh = Z0 + TZ;
-      flg[x][y][TZ] = (uint8_t)((row && Zh < g.c[2]) ? cross_flags(morton_code<S>(get, X, Y, Zh, f.iso)) : 0);
-      pre[x][y][TZ] = 0;  // first cell of the next segment
+  const uint32_t valid = zvalid(g, Z0);
+  for (int i = threadIdx.x; i < CX * CY; i += blockDim.x) {
+    const int x = i / CY, y = i % CY;
+    RowBits r = {0u, 0u, 0u, 0u};
+    int fl = 0;
+    if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
+      r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+      if (Z0 + TZ < g.c[2]) fl = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
     }
+    rb[x][y] = r;
+    f32[x][y] = (uint8_t)fl;
   }
   __syncthreads();
-
-  const int Y = Y0 + warp, Z = Z0 + lane;
+  // index of the vertex on the edge along a owned by window cell (x, y, z index j in [0, 32])
+  auto vid = [&](int x, int y, int j, int a) -> int64_t {
+    if (j == TZ) return (int64_t)vb[x][y][1] + __popc(f32[x][y] & ((1 << a) - 1));
+    const RowBits r = rb[x][y];
+    return (int64_t)vb[x][y][0] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
+  };
 #pragma unroll 1
-  for (int ix = 0; ix < TX; ++ix) {
-    const int X = X0 + ix;
-    const bool valid = X < g.c[0] && Y < g.c[1] && Z < g.c[2];
+  for (int si = warp; si < TX * TY; si += TY) {
+    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
+    if (X >= g.c[0] || Y >= g.c[1]) continue;
+    const RowBits r = rb[ix][iy];
+    if (!(r.xc | r.yc | r.zc | r.nt)) continue;
+    const int j = lane, Z = Z0 + j;
     // vertices: one per crossing edge owned by the cell, in axis order (src/cumc.cu:370-410)
-    const int fl = flg[ix][warp][lane];
-    if (valid && fl) {
-      int64_t vid = (int64_t)vb[ix][warp][0] + pre[ix][warp][lane];
+    const int fl = row_flags(r, j);
+    if (fl) {
+      int64_t v = (int64_t)vb[ix][iy][0] + row_prefix(r, j);
 #pragma unroll
       for (int a = 0; a < 3; ++a)
         if (fl & (1 << a)) {
           S p[3];
-          edge_vertex<S>(f, get, X, Y, Z, a, p);
-          store_vertex<S>(verts, vid++, p, g, normalize);
+          edge_vertex<S>(f, X, Y, Z, a, p);
+          store_vertex<S>(verts, v++, p, g, normalize);
         }
     }
     // triangles (src/cumc.cu:564-649): each table edge -> owner cell (+0/+1) -> its vertex
-    const uint64_t w = valid ? mc_tri(mc_from_morton(morton_code<S>(get, X, Y, Z, f.iso))) : 0ull;
+    uint64_t w = 0;
+    if ((r.nt >> j) & 1) w = mc_tri(mc_from_morton(code8(m[ix][iy], m[ix + 1][iy], m[ix][iy + 1], m[ix + 1][iy + 1], j + 1)));
     const uint32_t nt = (uint32_t)(w & 15);
     const uint32_t tinc = warp_incl(nt);
     if (nt) {
-      const int64_t f0 = (int64_t)fb[ix][warp] + (tinc - nt);
+      const int64_t f0 = (int64_t)fb[ix][iy] + (tinc - nt);
       for (uint32_t t = 0; t < nt; ++t) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const int e = (int)((w >> (4 + 4 * (3 * t + k))) & 15);
           const int ge = g_edge[e];
-          const int ox = ix + (ge & 1), oy = warp + ((ge >> 1) & 1), oz = lane + ((ge >> 2) & 1), a = ge >> 3;
-          const int ofl = flg[ox][oy][oz];
-          const int64_t id = (int64_t)vb[ox][oy][oz == TZ ? 1 : 0] + pre[ox][oy][oz] + __popc(ofl & ((1 << a) - 1));
-          faces[3 * (f0 + t) + k] = id;
+          faces[3 * (f0 + t) + k] = vid(ix + (ge & 1), iy + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3);
         }
       }
     }
@@ -238,44 +365,46 @@ template <class S>
 __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                             const int* __restrict__ active, S* __restrict__ verts,
                                                             int64_t* __restrict__ quads, int normalize) {
-  constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0-1, X0+TX) x [Y0-1, Y0+TY) x [Z0-1, Z0+TZ)
-  __shared__ Window<S, TX + 2, TY + 2, TZ + 2> win;     // points [X0-1, X0+TX] ...
-  __shared__ uint8_t rc[CX][CY][CZ];
-  __shared__ int16_t pp[CX][CY][CZ];
+  constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
+  __shared__ uint64_t m[WX][WY];
+  __shared__ uint8_t rc[CX][CY][TZ + 1];  // resolved codes; z index j+1 for cell Z0+j, 0 for Z0-1
+  __shared__ int16_t pp[CX][CY][TZ + 1];  // first patch of the cell inside its segment
   __shared__ uint32_t pb[CX][CY];
   __shared__ uint32_t qb[TX][TY];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
-  win.load(f, X0 - 1, Y0 - 1, Z0 - 1);
+  const int WX0 = X0 - 1, WY0 = Y0 - 1;
+  S dmn, dmx;
+  bool dseen = false;
+  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
   for (int i = threadIdx.x; i < CX * CY; i += blockDim.x) {
-    const int y = i % CY, x = i / CY;
-    const int X = X0 - 1 + x, Y = Y0 - 1 + y;
-    uint64_t s = (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) ? seg[g.seg(X, Y, tz)] : 0ull;
+    const int y = i % CY, x = i / CY, X = X0 - 1 + x, Y = Y0 - 1 + y;
+    const uint64_t s = (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) ? seg[g.seg(X, Y, tz)] : 0ull;
     pb[x][y] = Counts::hi(s);
     if (x >= 1 && y >= 1) qb[x - 1][y - 1] = Counts::lo(s);
   }
   __syncthreads();
-  auto get = [&](int X, int Y, int Z) { return win.get(f, X0 - 1, Y0 - 1, Z0 - 1, X, Y, Z); };
-
-  // resolved codes and in-segment patch prefixes of the tile's cells and their -1 halo
+  const uint32_t valid = zvalid(g, Z0);
+  // resolved codes and in-segment patch prefixes of the tile's cells and their -1 halo;
+  // the mask row of cell (X0-1+x, Y0-1+y) is (x, y)
   for (int r = warp; r < CX * CY; r += TY) {
     const int x = r / CY, y = r % CY, X = X0 - 1 + x, Y = Y0 - 1 + y;
     const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+    const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
+    const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
     int code = 0;
-    if (row && Z0 + lane < g.c[2]) {
-      const int m = morton_code<S>(get, X, Y, Z0 + lane, f.iso);
-      code = (m == 0 || m == 255) ? m : dmc_resolve<S>(get, m, X, Y, Z0 + lane, g.c, f.iso);
-    }
+    if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
     const uint32_t np = dmc_npatch(dmc_case(code));
-    const uint32_t inc = warp_incl(np);
+    const uint32_t inc = nt ? warp_incl(np) : 0u;
     rc[x][y][lane + 1] = (uint8_t)code;
     pp[x][y][lane + 1] = (int16_t)(inc - np);
     if (lane == 0) {
       int c0 = 0;
       if (row && Z0 >= 1) {
-        const int m = morton_code<S>(get, X, Y, Z0 - 1, f.iso);
-        c0 = (m == 0 || m == 255) ? m : dmc_resolve<S>(get, m, X, Y, Z0 - 1, g.c, f.iso);
+        c0 = code8(a, b, c, d, 0);
+        if (c0 != 0 && c0 != 255) c0 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c0, X, Y, Z0 - 1, g);
       }
       rc[x][y][0] = (uint8_t)c0;
       pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
@@ -283,12 +412,15 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
   }
   __syncthreads();
 
-  const int Y = Y0 + warp, Z = Z0 + lane;
 #pragma unroll 1
-  for (int ix = 0; ix < TX; ++ix) {
-    const int X = X0 + ix;
-    const bool valid = X < g.c[0] && Y < g.c[1] && Z < g.c[2];
-    const int code = valid ? rc[ix + 1][warp + 1][lane + 1] : 0;
+  for (int si = warp; si < TX * TY; si += TY) {
+    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
+    if (X >= g.c[0] || Y >= g.c[1]) continue;
+    const int x = ix + 1, y = iy + 1;  // window cell / mask row of the own row
+    const RowBits r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+    if (!r.nt) continue;
+    const int j = lane, Z = Z0 + j;
+    const int code = rc[x][y][j + 1];
     const uint64_t w = dmc_case(code);
     const int np = dmc_npatch(w);
     // dual vertices: mean of the patch's edge vertices, edges in ascending id
@@ -304,7 +436,7 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
         if ((((code >> s) ^ (code >> (s | (1 << a)))) & 1) == 0) continue;
         const int p = dmc_patch_of(w, e);
         S v[3];
-        edge_vertex<S>(f, get, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), a, v);
+        edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), a, v);
 #pragma unroll
         for (int q = 0; q < 4; ++q)
           if (q == p) {
@@ -314,7 +446,7 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
             cnt[q] += 1;
           }
       }
-      const int64_t p0 = (int64_t)pb[ix + 1][warp + 1] + pp[ix + 1][warp + 1][lane + 1];
+      const int64_t p0 = (int64_t)pb[x][y] + pp[x][y][j + 1];
 #pragma unroll
       for (int q = 0; q < 4; ++q)
         if (q < np) {
@@ -323,25 +455,22 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
           store_vertex<S>(verts, p0 + q, v, g, normalize);
         }
     }
-    // quads: one per crossing edge owned by the cell (src/cudualmc.cu:753-794, 1019-1056)
-    const int fl = cross_flags(code);
-    const uint32_t c = __popc(fl);
-    const uint32_t inc = warp_incl(c);
+    // quads: one per crossing edge owned by the cell (src/cudualmc.cu:753-794, 1019-1056);
+    // the edge exits (value falls through iso) when its start point is >= iso
+    const int fl = row_flags(r, j);
     if (fl) {
-      int64_t qid = (int64_t)qb[ix][warp] + (inc - c);
-      const S d0 = get(X, Y, Z);
+      int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j);
+      const int exiting = (int)((m[x][y] >> (j + 1)) & 1);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         if (!(fl & (1 << a))) continue;
-        const S d1 = get(X + (a == 0), Y + (a == 1), Z + (a == 2));
-        const int type = a + ((d1 < f.iso && d0 >= f.iso) ? 3 : 0);
+        const int type = a + 3 * exiting;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = g_dmc_quad[4 * type + i];
-          const int nx = ix + 1 + (q & 3) - 1, ny = warp + 1 + ((q >> 2) & 3) - 1, nz = lane + 1 + ((q >> 4) & 3) - 1;
+          const int nx = x + (q & 3) - 1, ny = y + ((q >> 2) & 3) - 1, nz = j + 1 + ((q >> 4) & 3) - 1;
           const int eid = q >> 8;
-          const int64_t pid = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), eid);
-          quads[4 * qid + i] = pid;
+          quads[4 * qid + i] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), eid);
         }
         ++qid;
       }
@@ -353,22 +482,19 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
 
 // dL/dverts of vertex i in padded coordinates: the chain rule of "- 1" and "/ (dim - 1)"
 template <class S>
-__device__ __forceinline__ void load_grad(const S* __restrict__ gv, int64_t i, const Geom& g, int normalize, S out[3]) {
+__device__ __forceinline__ void load_grad(const S* __restrict__ gv, int64_t i, const S scale[3], S out[3]) {
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    S v = __ldg(gv + 3 * i + k);
-    out[k] = normalize ? v / S(g.n[k] - 1) : v;
-  }
+  for (int k = 0; k < 3; ++k) out[k] = __ldg(gv + 3 * i + k) * scale[k];
 }
 
 // adjoint of edge_vertex at one endpoint (adjComputeMcVert, src/cumc.cu:412-453):
 // the edge runs from padded point A along axis a; `end` = 0 when the point being
 // differentiated is A, 1 when it is A + e_a.  Adds into gs (dL/dsdf) and gd.
-template <class S, class Get>
-__device__ __forceinline__ void edge_adjoint(const Field<S>& f, Get get, int X, int Y, int Z, int a, int end,
-                                             const S gvec[3], S& gs, S gd[3]) {
+template <class S>
+__device__ __forceinline__ void edge_adjoint(const Field<S>& f, int X, int Y, int Z, int a, int end, const S gvec[3],
+                                             S& gs, S gd[3]) {
   const int ex = a == 0, ey = a == 1, ez = a == 2;
-  const S d0 = get(X, Y, Z), d1 = get(X + ex, Y + ey, Z + ez);
+  const S d0 = f.at(X, Y, Z), d1 = f.at(X + ex, Y + ey, Z + ez);
   S t = S(0.5);
   if (d1 != d0) {
     S r = (f.iso - d0) / (d1 - d0);
@@ -382,25 +508,18 @@ __device__ __forceinline__ void edge_adjoint(const Field<S>& f, Get get, int X, 
                    (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
   const S adj_t = dp[0] * gvec[0] + dp[1] * gvec[1] + dp[2] * gvec[2];
   const S den = (d1 - d0) * (d1 - d0);
-  if (end == 0) {
-    gs += (f.iso - d1) / den * adj_t;
-    const S w = S(1) - t;
-    gd[0] += w * gvec[0];
-    gd[1] += w * gvec[1];
-    gd[2] += w * gvec[2];
-  } else {
-    gs += (d0 - f.iso) / den * adj_t;
-    gd[0] += t * gvec[0];
-    gd[1] += t * gvec[1];
-    gd[2] += t * gvec[2];
-  }
+  const S w = end ? t : S(1) - t;
+  gs += (end ? (d0 - f.iso) : (f.iso - d1)) / den * adj_t;
+  gd[0] += w * gvec[0];
+  gd[1] += w * gvec[1];
+  gd[2] += w * gvec[2];
 }
 
-// Per point tile (unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ)), the
-// cells [x0, x0+TX] x ... (padded coordinates; cell x0+i owns point x0+i as corner 0)
-// own every edge that touches the tile's points.  They lie in the forward tiles
-// (x0/TX + {0,1}, y0/TY + {0,1}, z0/TZ + {0,1}); the tile is inactive when none of
-// them holds a crossing.
+// Point tiles: unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ); in padded
+// coordinates the points are (X0+1.., Y0+1.., Z0+1..) with (X0, Y0, Z0) = (x0, y0, z0),
+// and the cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ] own every edge that touches
+// them.  Those cells lie in the forward tiles (x0/TX + {0,1}, y0/TY + {0,1},
+// z0/TZ + {0,1}); the point tile is inactive when none of them holds a crossing.
 __device__ __forceinline__ bool ptile_active(const Geom& g, const uint8_t* __restrict__ tile_flag, int x0, int y0,
                                              int z0) {
   int a = 0;
@@ -445,7 +564,6 @@ __device__ __forceinline__ void zero_ptile(const Field<S>& f, S* __restrict__ gs
   }
 }
 
-template <class S>
 __device__ __forceinline__ void ptile_coords(int64_t tile, const Geom& g, int& x0, int& y0, int& z0) {
   const int tz = (int)(tile % g.ptiles_z());
   const int64_t r = tile / g.ptiles_z();
@@ -457,7 +575,6 @@ __device__ __forceinline__ void ptile_coords(int64_t tile, const Geom& g, int& x
 template <class S>
 __device__ __forceinline__ void write_point_grads(const Field<S>& f, S* __restrict__ gsdf, S* __restrict__ gdef,
                                                   int X, int Y, int Z, S gs, const S gd[3]) {
-  if (!f.inside(X, Y, Z)) return;
   const int64_t i = f.lin(X, Y, Z);
   gsdf[i] = gs;
   if (gdef) {
@@ -475,64 +592,71 @@ __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom 
                                                                const uint8_t* __restrict__ tile_flag,
                                                                const S* __restrict__ gv, int normalize,
                                                                S* __restrict__ gsdf, S* __restrict__ gdef) {
-  constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0, X0+TX] x ...
-  __shared__ Window<S, TX + 2, TY + 2, TZ + 2> win;     // points [X0, X0+TX+1] ...
-  __shared__ uint8_t flg[CX][CY][CZ];
-  __shared__ uint8_t pre[CX][CY][CZ];
+  constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
+  __shared__ uint64_t m[WX][WY];
+  __shared__ RowBits rb[CX][CY];
+  __shared__ uint8_t f32[CX][CY];
   __shared__ uint32_t vb[CX][CY][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int X0, Y0, Z0;  // padded cell origin = unpadded point origin
-  ptile_coords<S>(blockIdx.x, g, X0, Y0, Z0);
-  const int zc = Z0 / TZ;
+  int X0, Y0, Z0;
+  ptile_coords(blockIdx.x, g, X0, Y0, Z0);
   if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
     zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
     return;
   }
-  win.load(f, X0, Y0, Z0);
+  const int zc = Z0 / TZ;
+  S dmn, dmx;
+  bool dseen = false;
+  load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
   for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
     const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
     const int X = X0 + x, Y = Y0 + y, c = zc + k;
     vb[x][y][k] = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? Counts::lo(seg[g.seg(X, Y, c)]) : 0u;
   }
   __syncthreads();
-  auto get = [&](int X, int Y, int Z) { return win.get(f, X0, Y0, Z0, X, Y, Z); };
-  for (int r = warp; r < CX * CY; r += TY) {
-    const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
-    const bool row = X < g.c[0] && Y < g.c[1];
-    int fl = (row && Z0 + lane < g.c[2]) ? cross_flags(morton_code<S>(get, X, Y, Z0 + lane, f.iso)) : 0;
-    const uint32_t c = __popc(fl);
-    const uint32_t inc = warp_incl(c);
-    flg[x][y][lane] = (uint8_t)fl;
-    pre[x][y][lane] = (uint8_t)(inc - c);
-    if (lane == 0) {
-      const int Zh = Z0 + TZ;
-      flg[x][y][TZ] = (uint8_t)((row && Zh < g.c[2]) ? cross_flags(morton_code<S>(get, X, Y, Zh, f.iso)) : 0);
-      pre[x][y][TZ] = 0;
+  const uint32_t valid = zvalid(g, Z0);
+  for (int i = threadIdx.x; i < CX * CY; i += blockDim.x) {
+    const int x = i / CY, y = i % CY;
+    RowBits r = {0u, 0u, 0u, 0u};
+    int fl = 0;
+    if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
+      r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+      if (Z0 + TZ < g.c[2]) fl = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
     }
+    rb[x][y] = r;
+    f32[x][y] = (uint8_t)fl;
   }
   __syncthreads();
-  auto vid = [&](int x, int y, int z, int a) -> int64_t {
-    return (int64_t)vb[x][y][z == TZ ? 1 : 0] + pre[x][y][z] + __popc(flg[x][y][z] & ((1 << a) - 1));
+  S scale[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
+  auto flags = [&](int x, int y, int j) -> int { return j == TZ ? f32[x][y] : row_flags(rb[x][y], j); };
+  auto vid = [&](int x, int y, int j, int a) -> int64_t {
+    if (j == TZ) return (int64_t)vb[x][y][1] + __popc(f32[x][y] & ((1 << a) - 1));
+    const RowBits r = rb[x][y];
+    return (int64_t)vb[x][y][0] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
   };
+#pragma unroll 1
   for (int ix = 0; ix < TX; ++ix) {
-    // point (X, Y, Z) padded = cell index (ix+1, warp+1, lane+1) in the window
+    // point (X, Y, Z) is window cell (x, y, z)
     const int x = ix + 1, y = warp + 1, z = lane + 1;
     const int X = X0 + x, Y = Y0 + y, Z = Z0 + z;
+    if (!f.inside(X, Y, Z)) continue;
     S gs = S(0), gd[3] = {S(0), S(0), S(0)};
-    if (f.inside(X, Y, Z)) {
+    const int own = flags(x, y, z);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        if (flg[x][y][z] & (1 << a)) {
-          S gvec[3];
-          load_grad<S>(gv, vid(x, y, z, a), g, normalize, gvec);
-          edge_adjoint<S>(f, get, X, Y, Z, a, 0, gvec, gs, gd);
-        }
-        const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
-        if (flg[px][py][pz] & (1 << a)) {
-          S gvec[3];
-          load_grad<S>(gv, vid(px, py, pz, a), g, normalize, gvec);
-          edge_adjoint<S>(f, get, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
-        }
+    for (int a = 0; a < 3; ++a) {
+      if (own & (1 << a)) {
+        S gvec[3];
+        load_grad<S>(gv, vid(x, y, z, a), scale, gvec);
+        edge_adjoint<S>(f, X, Y, Z, a, 0, gvec, gs, gd);
+      }
+      const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
+      if (flags(px, py, pz) & (1 << a)) {
+        S gvec[3];
+        load_grad<S>(gv, vid(px, py, pz, a), scale, gvec);
+        edge_adjoint<S>(f, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
       }
     }
     write_point_grads<S>(f, gsdf, gdef, X, Y, Z, gs, gd);
@@ -550,90 +674,98 @@ __global__ void __launch_bounds__(NTHREADS) dmc_backward_kernel(Field<S> f, Geom
                                                                 const uint8_t* __restrict__ tile_flag,
                                                                 const S* __restrict__ gv, int normalize, int exact,
                                                                 S* __restrict__ gsdf, S* __restrict__ gdef) {
-  constexpr int CX = TX + 1, CY = TY + 1, CZ = TZ + 1;  // cells [X0, X0+TX] x ...
-  __shared__ Window<S, TX + 2, TY + 2, TZ + 2> win;     // points [X0, X0+TX+1] ...
-  __shared__ uint8_t rc[CX][CY][CZ];
-  __shared__ uint8_t pre[CX][CY][CZ];
+  constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]; mask row of cell (x, y) is (x+1, y+1)
+  __shared__ uint64_t m[WX][WY];
+  __shared__ uint8_t rc[CX][CY][TZ + 1];
+  __shared__ uint8_t pre[CX][CY][TZ + 1];
   __shared__ uint32_t pb[CX][CY][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
-  ptile_coords<S>(blockIdx.x, g, X0, Y0, Z0);
-  const int zc = Z0 / TZ;
+  ptile_coords(blockIdx.x, g, X0, Y0, Z0);
   if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
     zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
     return;
   }
-  win.load(f, X0, Y0, Z0);
+  const int zc = Z0 / TZ;
+  const int WX0 = X0 - 1, WY0 = Y0 - 1;
+  S dmn, dmx;
+  bool dseen = false;
+  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
   for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
     const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
     const int X = X0 + x, Y = Y0 + y, c = zc + k;
     pb[x][y][k] = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? Counts::hi(seg[g.seg(X, Y, c)]) : 0u;
   }
   __syncthreads();
-  auto get = [&](int X, int Y, int Z) { return win.get(f, X0, Y0, Z0, X, Y, Z); };
-  auto resolved = [&](int X, int Y, int Z) -> int {
-    const int m = morton_code<S>(get, X, Y, Z, f.iso);
-    return (m == 0 || m == 255) ? m : dmc_resolve<S>(get, m, X, Y, Z, g.c, f.iso);
-  };
+  const uint32_t valid = zvalid(g, Z0);
   for (int r = warp; r < CX * CY; r += TY) {
     const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
     const bool row = X < g.c[0] && Y < g.c[1];
-    const int code = (row && Z0 + lane < g.c[2]) ? resolved(X, Y, Z0 + lane) : 0;
+    const uint64_t a = m[x + 1][y + 1], b = m[x + 2][y + 1], c = m[x + 1][y + 2], d = m[x + 2][y + 2];
+    const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
+    int code = 0;
+    if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
     const uint32_t np = dmc_npatch(dmc_case(code));
-    const uint32_t inc = warp_incl(np);
+    const uint32_t inc = nt ? warp_incl(np) : 0u;
     rc[x][y][lane] = (uint8_t)code;
     pre[x][y][lane] = (uint8_t)(inc - np);
     if (lane == 0) {
-      const int Zh = Z0 + TZ;
-      rc[x][y][TZ] = (uint8_t)((row && Zh < g.c[2]) ? resolved(X, Y, Zh) : 0);
-      pre[x][y][TZ] = 0;
+      int c32 = 0;
+      if (row && Z0 + TZ < g.c[2]) {
+        c32 = code8(a, b, c, d, TZ + 1);
+        if (c32 != 0 && c32 != 255) c32 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c32, X, Y, Z0 + TZ, g);
+      }
+      rc[x][y][TZ] = (uint8_t)c32;
+      pre[x][y][TZ] = 0;  // first cell of the next segment
     }
   }
   __syncthreads();
+  S scale[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
   // dL/d(edge vertex) of the crossing edge owned by window cell (ox, oy, oz) along a
   auto edge_grad = [&](int ox, int oy, int oz, int a, S out[3]) {
     out[0] = out[1] = out[2] = S(0);
-    const int b = (a + 1) % 3, c = (a + 2) % 3;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int db = k & 1, dc = k >> 1;
-      int cell[3] = {ox, oy, oz};
-      cell[b] -= db;
-      cell[c] -= dc;
-      int st[3] = {0, 0, 0};
-      st[b] = db;
-      st[c] = dc;
-      const int code = rc[cell[0]][cell[1]][cell[2]];
+      // the cell one step back along the two other axes (b, c) = (a+1, a+2) mod 3
+      const int cx = ox - (a == 1 ? dc : (a == 2 ? db : 0));
+      const int cy = oy - (a == 0 ? db : (a == 2 ? dc : 0));
+      const int cz = oz - (a == 0 ? dc : (a == 1 ? db : 0));
+      const int start = (ox - cx) | ((oy - cy) << 1) | ((oz - cz) << 2);
+      const int code = rc[cx][cy][cz];
       const uint64_t w = dmc_case(code);
-      const int p = dmc_patch_of(w, edge_id(st[0], st[1], st[2], a));
+      const int p = dmc_patch_of(w, g_edge_of[3 * start + a]);
       const S inv = S(1) / S(dmc_patch_size(w, p));
-      const int64_t pid =
-          (int64_t)pb[cell[0]][cell[1]][cell[2] == TZ ? 1 : 0] + pre[cell[0]][cell[1]][cell[2]] + (exact ? p : 0);
+      const int64_t pid = (int64_t)pb[cx][cy][cz == TZ ? 1 : 0] + pre[cx][cy][cz] + (exact ? p : 0);
       S v[3];
-      load_grad<S>(gv, pid, g, normalize, v);
+      load_grad<S>(gv, pid, scale, v);
       out[0] += v[0] * inv;
       out[1] += v[1] * inv;
       out[2] += v[2] * inv;
     }
   };
+#pragma unroll 1
   for (int ix = 0; ix < TX; ++ix) {
     const int x = ix + 1, y = warp + 1, z = lane + 1;
     const int X = X0 + x, Y = Y0 + y, Z = Z0 + z;
+    if (!f.inside(X, Y, Z)) continue;
     S gs = S(0), gd[3] = {S(0), S(0), S(0)};
-    if (f.inside(X, Y, Z)) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        if (cross_flags(rc[x][y][z]) & (1 << a)) {
-          S gvec[3];
-          edge_grad(x, y, z, a, gvec);
-          edge_adjoint<S>(f, get, X, Y, Z, a, 0, gvec, gs, gd);
-        }
-        const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
-        if (cross_flags(rc[px][py][pz]) & (1 << a)) {
-          S gvec[3];
-          edge_grad(px, py, pz, a, gvec);
-          edge_adjoint<S>(f, get, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
-        }
+    const int own = cross_flags(rc[x][y][z]);
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+      if (own & (1 << a)) {
+        S gvec[3];
+        edge_grad(x, y, z, a, gvec);
+        edge_adjoint<S>(f, X, Y, Z, a, 0, gvec, gs, gd);
+      }
+      const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
+      if (cross_flags(rc[px][py][pz]) & (1 << a)) {
+        S gvec[3];
+        edge_grad(px, py, pz, a, gvec);
+        edge_adjoint<S>(f, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
       }
     }
     write_point_grads<S>(f, gsdf, gdef, X, Y, Z, gs, gd);
