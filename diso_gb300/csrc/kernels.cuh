@@ -83,26 +83,38 @@ __device__ __forceinline__ uint32_t zvalid(const Geom& g, int Z0) {
 // ------------------------------------------------------------------ row masks
 
 // Fill m[x][y] for point rows (WX0 + x, WY0 + y); bit k = point Z0 - 1 + k >= iso.
-// Tracks min / max of the caller's (interior) values when TRACK.
+// Each warp takes every (blockDim/32)-th row and issues all its loads before the
+// ballots, so a warp keeps up to PER row loads in flight.  Tracks min / max of the
+// caller's (interior) values when TRACK.  Needs blockDim.x == NTHREADS.
 template <class S, int WX, int WY, bool TRACK>
 __device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
                                            S& mn, S& mx, bool& seen) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  constexpr int NW = NTHREADS / 32, NR = WX * WY, PER = (NR + NW - 1) / NW;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z = Z0 - 1 + lane, Ze = Z0 + 31 + lane;
   const bool zin = (unsigned)(Z - 1) < (unsigned)f.n2;
   const bool ein = lane < 3 && (unsigned)(Ze - 1) < (unsigned)f.n2;
-  for (int r = warp; r < WX * WY; r += nw) {
+  S v[PER], e[PER];
+  bool in[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int r = warp + k * NW;
     const int x = r / WY, y = r % WY, X = WX0 + x, Y = WY0 + y;
-    const bool row = (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
-    const S* p = f.sdf + ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
-    const S v = (row && zin) ? __ldg(p + Z) : f.pad;
-    const S e = (row && ein) ? __ldg(p + Ze) : f.pad;
-    const uint32_t lo = __ballot_sync(0xffffffffu, v >= f.iso);
-    const uint32_t hi = __ballot_sync(0xffffffffu, lane < 3 && e >= f.iso);
-    if (lane == 0) m[x][y] = (uint64_t)lo | ((uint64_t)(hi & 7u) << 32);
-    if (TRACK && row && zin) {
-      mn = seen ? (v < mn ? v : mn) : v;
-      mx = seen ? (v > mx ? v : mx) : v;
+    const bool row = r < NR && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
+    const int64_t base = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
+    in[k] = row && zin;
+    v[k] = in[k] ? __ldg(f.sdf + base + Z) : f.pad;
+    e[k] = (row && ein) ? __ldg(f.sdf + base + Ze) : f.pad;
+  }
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int r = warp + k * NW;
+    const uint32_t lo = __ballot_sync(0xffffffffu, v[k] >= f.iso);
+    const uint32_t hi = __ballot_sync(0xffffffffu, lane < 3 && e[k] >= f.iso);
+    if (lane == 0 && r < NR) m[r / WY][r % WY] = (uint64_t)lo | ((uint64_t)(hi & 7u) << 32);
+    if (TRACK && in[k]) {
+      mn = seen ? (v[k] < mn ? v[k] : mn) : v[k];
+      mx = seen ? (v[k] > mx ? v[k] : mx) : v[k];
       seen = true;
     }
   }
@@ -122,9 +134,11 @@ __device__ __forceinline__ int code8(uint64_t a, uint64_t b, uint64_t c, uint64_
 template <class S, int WX, int WY>
 __device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
                                          int X, int Y, int Z) {
+  // rows x and x + 1 must both lie in the window (x is unsigned: a row below the
+  // window wraps to a huge value and fails the test)
   const unsigned x = (unsigned)(X - WX0), y = (unsigned)(Y - WY0);
   const int s = Z - Z0 + 1;
-  if (x + 1 < (unsigned)WX && y + 1 < (unsigned)WY && s >= 0 && s + 1 <= MASK_TOP)
+  if (x < (unsigned)(WX - 1) && y < (unsigned)(WY - 1) && s >= 0 && s + 1 <= MASK_TOP)
     return code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], s);
   int c = 0;
 #pragma unroll
