@@ -4,6 +4,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <new>
 
 #include "../../include/diso_gb300.h"
@@ -45,6 +46,7 @@ struct diso_extractor {
   uint64_t* split = nullptr;     // split counts (n_quads + 1)
   int64_t split_cap = 0;
   int64_t last_active = 0;       // from the last forward count
+  int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
 
   void release() {
     cudaFree(stats);
@@ -87,6 +89,15 @@ int bind_device(diso_extractor* ex) {
   if (!ex->stats) {
     CUDA_TRY(cudaMalloc((void**)&ex->stats, sizeof(Stats)));
     CUDA_TRY(cudaMallocHost((void**)&ex->stats_host, sizeof(Stats)));
+    int sms = 0, per_sm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (ex->dtype == DISO_F32)
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, ex->method == DISO_MC ? count_kernel<float, MC> : count_kernel<float, DMC>, NTHREADS, 0));
+    else
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, ex->method == DISO_MC ? count_kernel<double, MC> : count_kernel<double, DMC>, NTHREADS, 0));
+    ex->resident_ctas = sms * std::max(per_sm, 1);
   }
   return DISO_OK;
 }
@@ -156,12 +167,13 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
+  // persistent grid: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
+  const int64_t want = std::max<int64_t>(ex->resident_ctas, (g.ntiles() + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::min<int64_t>(want, g.ntiles());
   if (ex->method == DISO_MC)
-    count_kernel<S, MC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats,
-                                                                  ex->active);
+    count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
   else
-    count_kernel<S, DMC><<<(unsigned)g.ntiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats,
-                                                                   ex->active);
+    count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));

@@ -200,8 +200,15 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 
 // ------------------------------------------------------------------ count
 
+// Persistent: CTA b handles tiles b, b + gridDim.x, ...; it keeps the min / max
+// and the list of its active tiles in registers / shared memory and publishes
+// them with a handful of atomics at the end (per-tile atomics on one address
+// serialise in L2).  At most COUNT_LIST tiles per CTA: launch at least
+// ntiles / COUNT_LIST CTAs.
+constexpr int COUNT_LIST = 1024;
+
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
+__global__ void __launch_bounds__(NTHREADS, 4) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                          uint8_t* __restrict__ tile_flag, Stats* stats,
                                                          int* __restrict__ active) {
   // MC needs the rows of the cells' corners, DMC also those of the face neighbours
@@ -211,42 +218,53 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
   __shared__ uint64_t m[WX][WY];
   __shared__ S red_min[TY], red_max[TY];
   __shared__ uint32_t red_any[TY];
+  __shared__ int list[COUNT_LIST];
+  __shared__ int nlist, base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t tile = blockIdx.x;
-  int X0, Y0, Z0, tz;
-  tile_coords(tile, g, X0, Y0, Z0, tz);
-  const int WX0 = X0 - H, WY0 = Y0 - H;
+  if (threadIdx.x == 0) nlist = 0;
   S mn = f.pad, mx = f.pad;
   bool seen = false;
-  load_masks<S, WX, WY, true>(m, f, WX0, WY0, Z0, mn, mx, seen);
-  __syncthreads();
-
-  const uint32_t valid = zvalid(g, Z0);
-  uint32_t any = 0;
+  const int64_t ntiles = g.ntiles();
 #pragma unroll 1
-  for (int si = warp; si < TX * TY; si += TY) {
-    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
-    if (X >= g.c[0] || Y >= g.c[1]) continue;
-    const int x = ix + H, y = iy + H;
-    const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
-    const RowBits r = row_bits(a, b, c, d, valid);
-    const uint32_t nv = __popc(r.xc) + __popc(r.yc) + __popc(r.zc);
-    uint32_t nf = 0;
-    if (r.nt) {
-      uint32_t mine = 0;
-      if ((r.nt >> lane) & 1) {
-        const int code = code8(a, b, c, d, lane + 1);
-        if (METHOD == MC)
-          mine = (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-        else
-          mine = dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + lane, g)));
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int X0, Y0, Z0, tz;
+    tile_coords(tile, g, X0, Y0, Z0, tz);
+    const int WX0 = X0 - H, WY0 = Y0 - H;
+    load_masks<S, WX, WY, true>(m, f, WX0, WY0, Z0, mn, mx, seen);
+    __syncthreads();
+    const uint32_t valid = zvalid(g, Z0);
+    uint32_t any = 0;
+#pragma unroll 1
+    for (int si = warp; si < TX * TY; si += TY) {
+      const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
+      if (X >= g.c[0] || Y >= g.c[1]) continue;
+      const int x = ix + H, y = iy + H;
+      const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
+      const RowBits r = row_bits(a, b, c, d, valid);
+      const uint32_t nv = __popc(r.xc) + __popc(r.yc) + __popc(r.zc);
+      uint32_t nf = 0;
+      if (r.nt) {
+        uint32_t mine = 0;
+        if ((r.nt >> lane) & 1) {
+          const int code = code8(a, b, c, d, lane + 1);
+          if (METHOD == MC)
+            mine = (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+          else
+            mine = dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + lane, g)));
+        }
+        nf = warp_sum(mine);
       }
-      nf = warp_sum(mine);
+      if (lane == 0) seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
+      // a cell can emit faces / patches without owning a crossing edge (its
+      // crossings may all sit on edges owned by its +1 neighbours)
+      any |= nv | nf;
     }
-    if (lane == 0) seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-    // a cell can emit faces / patches without owning a crossing edge (its
-    // crossings may all sit on edges owned by its +1 neighbours)
-    any |= nv | nf;
+    // any crossing in the tile: ballot over the warps' results
+    const int act = __syncthreads_or(any != 0);
+    if (threadIdx.x == 0) {
+      tile_flag[tile] = act ? 1 : 0;
+      if (act) list[nlist++] = (int)tile;
+    }
   }
   // min / max of the caller's grid (the guard of diso/__init__.py:49)
   const unsigned have = __ballot_sync(0xffffffffu, seen);
@@ -267,14 +285,13 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
   if (lane == 0) {
     red_min[warp] = mn;
     red_max[warp] = mx;
-    red_any[warp] = (any ? 1u : 0u) | (have ? 2u : 0u);
+    red_any[warp] = have ? 1u : 0u;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    bool act = false, got = false;
+    bool got = false;
     for (int w = 0; w < TY; ++w) {
-      act |= (red_any[w] & 1u) != 0;
-      if (red_any[w] & 2u) {
+      if (red_any[w]) {
         mn = got ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
         mx = got ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
         got = true;
@@ -284,9 +301,10 @@ __global__ void __launch_bounds__(NTHREADS) count_kernel(Field<S> f, Geom g, uin
       atomicMin(&stats->min_key, ord_key((double)mn));
       atomicMax(&stats->max_key, ord_key((double)mx));
     }
-    tile_flag[tile] = act ? 1 : 0;
-    if (act) active[atomicAdd(&stats->n_active, 1ull)] = (int)tile;
+    base = nlist ? (int)atomicAdd(&stats->n_active, (unsigned long long)nlist) : 0;
   }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nlist; i += blockDim.x) active[base + i] = list[i];
 }
 
 // ------------------------------------------------------------------ MC emit
