@@ -5,7 +5,10 @@ Tolerances (the bar the benchmark spec states for this path):
 * case codes, face index lists and vertex counts: exact;
 * vertices: within 1e-6 of the grid extent in float32, 1e-12 in float64
   (extent = 1 with normalize, dim - 1 without);
-* gradients: max |a - b| <= 1e-5 * max |b| in float32 (1e-10 in float64);
+* gradients: max |a - b| <= 1e-5 * max |b| in float32 (1e-10 in float64) against
+  the reference's own outputs.  Against the float64 oracle a float32 result also
+  carries the reference's rounding of p = X + deform at magnitude X (up to
+  N * 2^-24 on p1 - p0), so that bound is scaled by max(1, N / 32);
 * DMC quad -> triangle split: the same choice for every quad except true
   near-ties, |max_cos1 - max_cos2| < 1e-5 (float32) / 1e-12 (float64) as
   evaluated in float64 on the reference's vertices.
@@ -81,7 +84,12 @@ def assert_verts_close(v, v_ref, case):
         assert err <= tol, f"vertex error {err:.3e} > {tol:.1e}"
 
 
-def assert_grads_close(g, g_ref, dtype, what="grad"):
+def oracle_grad_rtol(dtype, shape):
+    """Gradient tolerance of a float32 / float64 result against the float64 oracle."""
+    return GRAD_RTOL[dtype] * (max(1.0, max(shape) / 32.0) if dtype == "float32" else 1.0)
+
+
+def assert_grads_close(g, g_ref, dtype, what="grad", rtol=None):
     assert g.shape == g_ref.shape
     fa, fb = np.isfinite(g), np.isfinite(g_ref)
     assert np.array_equal(fa, fb), f"{what}: non-finite entries differ"
@@ -92,8 +100,9 @@ def assert_grads_close(g, g_ref, dtype, what="grad"):
     if scale == 0:
         assert np.abs(g).max() == 0, f"{what}: expected all zeros"
         return
+    rtol = GRAD_RTOL[dtype] if rtol is None else rtol
     err = np.abs(g.astype(np.float64) - g_ref.astype(np.float64)).max()
-    assert err <= GRAD_RTOL[dtype] * scale, f"{what}: max error {err:.3e} > {GRAD_RTOL[dtype]:.0e} * {scale:.3e}"
+    assert err <= rtol * scale, f"{what}: max error {err:.3e} > {rtol:.1e} * {scale:.3e}"
 
 
 def _tri_max_cos(V, a, b, c):

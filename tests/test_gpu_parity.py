@@ -1,10 +1,13 @@
 """Parity of the CUDA path (through the public DiffMC / DiffDMC API and the C ABI)
 with the reference's own outputs (golden fixtures) and with the CPU oracle."""
+import zlib
+
 import numpy as np
 import pytest
 import torch
 
-from helpers import (assert_faces_equal, assert_grads_close, assert_verts_close, fixture_names, load_fixture)
+from helpers import (assert_faces_equal, assert_grads_close, assert_verts_close, fixture_names, load_fixture,
+                     oracle_grad_rtol)
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -81,7 +84,7 @@ ORACLE_CASES = [
 
 @pytest.mark.parametrize("method,dtype,field,shape,deform,iso,normalize,rq", ORACLE_CASES)
 def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, normalize, rq):
-    rng = np.random.default_rng(abs(hash((method, dtype, field, shape))) % 2**32)
+    rng = np.random.default_rng(zlib.crc32(repr((method, dtype, field, shape)).encode()))
     sdf = _field(field, shape, rng).astype(dtype)
     dfm = rng.uniform(-deform, deform, shape + (3,)).astype(dtype) if deform else None
     case = dict(method=method, dtype=dtype, iso=iso, normalize=normalize, return_quads=rq, shape=shape)
@@ -95,9 +98,10 @@ def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, n
     assert_verts_close(out["verts"], v_ref, case)
     assert_faces_equal(out["faces"], f_ref, case, v_ref)
     gs, gd = O.backward(m, sdf, dfm, w, iso, normalize, dtype)
-    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf")
+    rtol = oracle_grad_rtol(dtype, shape)
+    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf", rtol)
     if dfm is not None:
-        assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform")
+        assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform", rtol)
 
 
 @pytest.mark.parametrize("dtype", ["float32", "float64"])
@@ -111,8 +115,9 @@ def test_dmc_exact_gradient_matches_oracle(cuda_device, dtype):
     w = rng.standard_normal(v_ref.shape).astype(dtype)
     out = run(case, sdf, dfm, w, exact_grad=True)
     gs, gd = O.backward(O.DMC, sdf, dfm, w, 0.0, True, dtype, exact=True)
-    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf")
-    assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform")
+    rtol = oracle_grad_rtol(dtype, shape)
+    assert_grads_close(out["grad_sdf"], gs, dtype, "grad_sdf", rtol)
+    assert_grads_close(out["grad_deform"], gd, dtype, "grad_deform", rtol)
 
 
 @pytest.mark.parametrize("method", ["mc", "dmc"])
