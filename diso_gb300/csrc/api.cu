@@ -168,8 +168,10 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grid: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
-  const int64_t want = std::max<int64_t>(ex->resident_ctas, (g.ntiles() + COUNT_LIST - 1) / COUNT_LIST);
-  const unsigned grid = (unsigned)std::min<int64_t>(want, g.ntiles());
+  const int64_t blocks = count_blocks(g);
+  const int64_t per_block = (CP / TX) * (CR / TY);
+  const int64_t want = std::max<int64_t>(ex->resident_ctas, (blocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::min<int64_t>(want, blocks);
   if (ex->method == DISO_MC)
     count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
   else

@@ -83,39 +83,42 @@ __device__ __forceinline__ uint32_t zvalid(const Geom& g, int Z0) {
 // ------------------------------------------------------------------ row masks
 
 // Fill m[x][y] for point rows (WX0 + x, WY0 + y); bit k = point Z0 - 1 + k >= iso.
-// Each warp takes every (blockDim/32)-th row and issues all its loads before the
-// ballots, so a warp keeps up to PER row loads in flight.  Tracks min / max of the
+// Warp w takes rows w, w + NW, ...; it issues the loads of BATCH rows before their
+// ballots, so each warp keeps BATCH row loads in flight.  Tracks min / max of the
 // caller's (interior) values when TRACK.  Needs blockDim.x == NTHREADS.
 template <class S, int WX, int WY, bool TRACK>
 __device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
                                            S& mn, S& mx, bool& seen) {
-  constexpr int NW = NTHREADS / 32, NR = WX * WY, PER = (NR + NW - 1) / NW;
+  constexpr int NW = NTHREADS / 32, NR = WX * WY, BATCH = 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z = Z0 - 1 + lane, Ze = Z0 + 31 + lane;
   const bool zin = (unsigned)(Z - 1) < (unsigned)f.n2;
   const bool ein = lane < 3 && (unsigned)(Ze - 1) < (unsigned)f.n2;
-  S v[PER], e[PER];
-  bool in[PER];
+#pragma unroll 1
+  for (int r0 = warp; r0 < NR; r0 += NW * BATCH) {
+    S v[BATCH], e[BATCH];
+    bool in[BATCH];
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int r = warp + k * NW;
-    const int x = r / WY, y = r % WY, X = WX0 + x, Y = WY0 + y;
-    const bool row = r < NR && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
-    const int64_t base = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
-    in[k] = row && zin;
-    v[k] = in[k] ? __ldg(f.sdf + base + Z) : f.pad;
-    e[k] = (row && ein) ? __ldg(f.sdf + base + Ze) : f.pad;
-  }
+    for (int k = 0; k < BATCH; ++k) {
+      const int r = r0 + k * NW;
+      const int x = r / WY, y = r % WY, X = WX0 + x, Y = WY0 + y;
+      const bool row = r < NR && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
+      const int64_t base = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
+      in[k] = row && zin;
+      v[k] = in[k] ? __ldg(f.sdf + base + Z) : f.pad;
+      e[k] = (row && ein) ? __ldg(f.sdf + base + Ze) : f.pad;
+    }
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int r = warp + k * NW;
-    const uint32_t lo = __ballot_sync(0xffffffffu, v[k] >= f.iso);
-    const uint32_t hi = __ballot_sync(0xffffffffu, lane < 3 && e[k] >= f.iso);
-    if (lane == 0 && r < NR) m[r / WY][r % WY] = (uint64_t)lo | ((uint64_t)(hi & 7u) << 32);
-    if (TRACK && in[k]) {
-      mn = seen ? (v[k] < mn ? v[k] : mn) : v[k];
-      mx = seen ? (v[k] > mx ? v[k] : mx) : v[k];
-      seen = true;
+    for (int k = 0; k < BATCH; ++k) {
+      const int r = r0 + k * NW;
+      const uint32_t lo = __ballot_sync(0xffffffffu, v[k] >= f.iso);
+      const uint32_t hi = __ballot_sync(0xffffffffu, lane < 3 && e[k] >= f.iso);
+      if (lane == 0 && r < NR) m[r / WY][r % WY] = (uint64_t)lo | ((uint64_t)(hi & 7u) << 32);
+      if (TRACK && in[k]) {
+        mn = seen ? (v[k] < mn ? v[k] : mn) : v[k];
+        mx = seen ? (v[k] > mx ? v[k] : mx) : v[k];
+        seen = true;
+      }
     }
   }
 }
@@ -200,70 +203,86 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 
 // ------------------------------------------------------------------ count
 
-// Persistent: CTA b handles tiles b, b + gridDim.x, ...; it keeps the min / max
-// and the list of its active tiles in registers / shared memory and publishes
-// them with a handful of atomics at the end (per-tile atomics on one address
-// serialise in L2).  At most COUNT_LIST tiles per CTA: launch at least
-// ntiles / COUNT_LIST CTAs.
-constexpr int COUNT_LIST = 1024;
+// The count pass works on blocks of CP planes x CR rows x 32 cells: one warp per
+// plane, one lane per row segment.  Each lane derives its segment's crossing count
+// from four row masks with popcounts and walks only the segment's non-trivial
+// cells for the case-table lookups.  A block covers (CP/TX) x (CR/TY) activity tiles.
+//
+// Persistent: CTA b handles blocks b, b + gridDim.x, ...; it keeps the min / max and
+// the list of its active tiles and publishes them with a few atomics at the end
+// (per-tile atomics on one address serialise in L2).  At most COUNT_LIST tiles per
+// CTA: launch at least ntiles / COUNT_LIST CTAs.
+constexpr int CP = 8, CR = 32;
+constexpr int COUNT_LIST = 2048;
+static_assert(CP * 32 == NTHREADS && CP % TX == 0 && CR % TY == 0, "count block shape");
+
+__host__ __device__ inline int64_t count_blocks(const Geom& g) {
+  return (int64_t)((g.c[0] + CP - 1) / CP) * ((g.c[1] + CR - 1) / CR) * g.nzc;
+}
 
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS, 4) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
-                                                         uint8_t* __restrict__ tile_flag, Stats* stats,
-                                                         int* __restrict__ active) {
+__global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
+                                                            uint8_t* __restrict__ tile_flag, Stats* stats,
+                                                            int* __restrict__ active) {
   // MC needs the rows of the cells' corners, DMC also those of the face neighbours
   // used by the ambiguity test
   constexpr int H = METHOD == DMC ? 1 : 0;
-  constexpr int WX = TX + 1 + 2 * H, WY = TY + 1 + 2 * H;
+  constexpr int WX = CP + 1 + 2 * H, WY = CR + 1 + 2 * H;
   __shared__ uint64_t m[WX][WY];
-  __shared__ S red_min[TY], red_max[TY];
-  __shared__ uint32_t red_any[TY];
+  __shared__ uint32_t act[CP];
+  __shared__ S red_min[CP], red_max[CP];
+  __shared__ uint32_t red_any[CP];
   __shared__ int list[COUNT_LIST];
   __shared__ int nlist, base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) nlist = 0;
   S mn = f.pad, mx = f.pad;
   bool seen = false;
-  const int64_t ntiles = g.ntiles();
+  const int nby = (g.c[1] + CR - 1) / CR;
+  const int64_t nblocks = count_blocks(g);
 #pragma unroll 1
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    int X0, Y0, Z0, tz;
-    tile_coords(tile, g, X0, Y0, Z0, tz);
+  for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    const int tz = (int)(blk % g.nzc);
+    const int r = (int)(blk / g.nzc);
+    const int X0 = (r / nby) * CP, Y0 = (r % nby) * CR, Z0 = tz * TZ;
     const int WX0 = X0 - H, WY0 = Y0 - H;
     load_masks<S, WX, WY, true>(m, f, WX0, WY0, Z0, mn, mx, seen);
     __syncthreads();
-    const uint32_t valid = zvalid(g, Z0);
-    uint32_t any = 0;
-#pragma unroll 1
-    for (int si = warp; si < TX * TY; si += TY) {
-      const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
-      if (X >= g.c[0] || Y >= g.c[1]) continue;
-      const int x = ix + H, y = iy + H;
+    const int X = X0 + warp, Y = Y0 + lane;
+    uint32_t nv = 0, nf = 0;
+    if (X < g.c[0] && Y < g.c[1]) {
+      const int x = warp + H, y = lane + H;
       const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
-      const RowBits r = row_bits(a, b, c, d, valid);
-      const uint32_t nv = __popc(r.xc) + __popc(r.yc) + __popc(r.zc);
-      uint32_t nf = 0;
-      if (r.nt) {
-        uint32_t mine = 0;
-        if ((r.nt >> lane) & 1) {
-          const int code = code8(a, b, c, d, lane + 1);
-          if (METHOD == MC)
-            mine = (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-          else
-            mine = dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + lane, g)));
-        }
-        nf = warp_sum(mine);
+      const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
+      nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
+      uint32_t nt = rw.nt;
+      while (nt) {
+        const int j = __ffs(nt) - 1;
+        nt &= nt - 1;
+        const int code = code8(a, b, c, d, j + 1);
+        if (METHOD == MC)
+          nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+        else
+          nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + j, g)));
       }
-      if (lane == 0) seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-      // a cell can emit faces / patches without owning a crossing edge (its
-      // crossings may all sit on edges owned by its +1 neighbours)
-      any |= nv | nf;
+      seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
     }
-    // any crossing in the tile: ballot over the warps' results
-    const int act = __syncthreads_or(any != 0);
-    if (threadIdx.x == 0) {
-      tile_flag[tile] = act ? 1 : 0;
-      if (act) list[nlist++] = (int)tile;
+    // a cell can emit faces / patches without owning a crossing edge (its
+    // crossings may all sit on edges owned by its +1 neighbours)
+    const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
+    if (lane == 0) act[warp] = busy;
+    __syncthreads();
+    if (threadIdx.x < (CP / TX) * (CR / TY)) {
+      const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
+      const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
+      if (tx < g.tiles_x() && ty < g.tiles_y()) {
+        uint32_t any = 0;
+#pragma unroll
+        for (int p = 0; p < TX; ++p) any |= (act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
+        const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
+        tile_flag[tile] = any ? 1 : 0;
+        if (any) list[atomicAdd(&nlist, 1)] = (int)tile;
+      }
     }
   }
   // min / max of the caller's grid (the guard of diso/__init__.py:49)
@@ -290,7 +309,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) count_kernel(Field<S> f, Geom g, 
   __syncthreads();
   if (threadIdx.x == 0) {
     bool got = false;
-    for (int w = 0; w < TY; ++w) {
+    for (int w = 0; w < CP; ++w) {
       if (red_any[w]) {
         mn = got ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
         mx = got ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
