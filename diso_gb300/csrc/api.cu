@@ -226,12 +226,17 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   g.init(nx, ny, nz);
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const unsigned grid = (unsigned)g.nptiles();
-  if (ex->method == DISO_MC)
-    mc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
-                                                    (S*)gsdf, (S*)gdef);
-  else
-    dmc_backward_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
-                                                     (flags & DISO_GRAD_EXACT) ? 1 : 0, (S*)gsdf, (S*)gdef);
+  const size_t smem = backward_dyn_smem<S>();
+  const int ex_flag = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  if (ex->method == DISO_MC) {
+    CUDA_TRY(cudaFuncSetAttribute(backward_kernel<S, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    backward_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize, 0,
+                                                       (S*)gsdf, (S*)gdef);
+  } else {
+    CUDA_TRY(cudaFuncSetAttribute(backward_kernel<S, DMC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    backward_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
+                                                        ex_flag, (S*)gsdf, (S*)gdef);
+  }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }

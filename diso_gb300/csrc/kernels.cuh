@@ -6,7 +6,7 @@
 //   scan              scan.cuh
 //   mc_emit_kernel    active tiles: MC vertices and triangles
 //   dmc_emit_kernel   active tiles: DMC dual vertices and quads
-//   *_backward_kernel all point tiles: dL/dsdf and dL/ddeform, every element written
+//   backward_kernel   all point tiles: dL/dsdf and dL/ddeform, every element written
 //                     once (zeros away from the surface), crossings recomputed
 //   split_*           DMC quad -> triangle split (return_quads=False)
 //
@@ -326,7 +326,54 @@ __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, 
   for (int i = threadIdx.x; i < nlist; i += blockDim.x) active[base + i] = list[i];
 }
 
+// ------------------------------------------------------------------ work lists
+
+// Exclusive scan of one value per thread over the block (blockDim.x == NTHREADS).
+// Returns the thread's offset; `total` receives the sum.  wsum: NW + 1 words of
+// shared memory, free again after the call returns.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* wsum, uint32_t& total) {
+  constexpr int NW = NTHREADS / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t inc = warp_incl(v);
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < NW ? wsum[lane] : 0u;
+    const uint32_t wi = warp_incl(w);
+    if (lane < NW) wsum[lane] = wi - w;
+    if (lane == NW - 1) wsum[NW] = wi;
+  }
+  __syncthreads();
+  total = wsum[NW];
+  const uint32_t off = wsum[warp] + inc - v;
+  __syncthreads();
+  return off;
+}
+
+// work item of a tile: cell-window coordinates and, for edge items, the axis
+__device__ __forceinline__ uint16_t item_code(int x, int y, int j, int a) {
+  return (uint16_t)(x | (y << 3) | (j << 7) | (a << 13));
+}
+__device__ __forceinline__ void item_decode(uint16_t c, int& x, int& y, int& j, int& a) {
+  x = c & 7;
+  y = (c >> 3) & 15;
+  j = (c >> 7) & 63;
+  a = c >> 13;
+}
+static_assert(TX + 1 <= 8 && TY + 1 <= 16 && TZ + 1 <= 64, "item code fields");
+
+// append the set bits of `bits` (bit j -> cell j) as items of cell row (x, y) and axis a
+__device__ __forceinline__ void put_items(uint16_t* list, uint32_t off, uint64_t bits, int x, int y, int a) {
+  while (bits) {
+    const int j = __ffsll((long long)bits) - 1;
+    bits &= bits - 1;
+    list[off++] = item_code(x, y, j, a);
+  }
+}
+
 // ------------------------------------------------------------------ MC emit
+
+constexpr int EMIT_ITEMS = 3 * TX * TY * TZ;  // every own edge crossing
 
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
@@ -339,7 +386,11 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
   __shared__ uint8_t f32[CX][CY];  // flags of cell Z0+32 (first of the next segment)
   __shared__ uint32_t vb[CX][CY][2];
   __shared__ uint32_t fb[TX][TY];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ uint8_t fpre[TX][TY][TZ];  // triangles before the cell inside its segment
+  __shared__ uint16_t vitems[EMIT_ITEMS];
+  __shared__ uint16_t citems[TX * TY * TZ];
+  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
+  __shared__ uint32_t nvi, nci;
   int X0, Y0, Z0, tz;
   tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
   S dmn, dmx;
@@ -366,45 +417,71 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
     f32[x][y] = (uint8_t)fl;
   }
   __syncthreads();
+  // one thread per own row: the row's vertex items and cell items, and the
+  // triangle prefix of its non-trivial cells
+  uint32_t cv = 0, cc = 0;
+  RowBits own = {0u, 0u, 0u, 0u};
+  const int ox = threadIdx.x / TY, oy = threadIdx.x % TY;
+  if (threadIdx.x < TX * TY) {
+    own = rb[ox][oy];
+    cv = __popc(own.xc) + __popc(own.yc) + __popc(own.zc);
+    cc = __popc(own.nt);
+    uint32_t nt = own.nt, run = 0;
+    while (nt) {
+      const int j = __ffs(nt) - 1;
+      nt &= nt - 1;
+      fpre[ox][oy][j] = (uint8_t)run;
+      run += (uint32_t)(mc_tri(mc_from_morton(code8(m[ox][oy], m[ox + 1][oy], m[ox][oy + 1], m[ox + 1][oy + 1], j + 1))) & 15);
+    }
+  }
+  uint32_t tot;
+  const uint32_t off = block_excl_scan(cv | (cc << 16), wsum, tot);
+  if (threadIdx.x == 0) {
+    nvi = tot & 0xffffu;
+    nci = tot >> 16;
+  }
+  if (threadIdx.x < TX * TY) {
+    uint32_t o = off & 0xffffu;
+    // vertices in (cell, axis) order: interleave the three axes per cell
+    uint32_t b = own.xc | own.yc | own.zc;
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      const int fl = row_flags(own, j);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        if (fl & (1 << a)) vitems[o++] = item_code(ox, oy, j, a);
+    }
+    put_items(citems, off >> 16, own.nt, ox, oy, 0);
+  }
+  __syncthreads();
   // index of the vertex on the edge along a owned by window cell (x, y, z index j in [0, 32])
   auto vid = [&](int x, int y, int j, int a) -> int64_t {
     if (j == TZ) return (int64_t)vb[x][y][1] + __popc(f32[x][y] & ((1 << a) - 1));
     const RowBits r = rb[x][y];
     return (int64_t)vb[x][y][0] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
   };
-#pragma unroll 1
-  for (int si = warp; si < TX * TY; si += TY) {
-    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
-    if (X >= g.c[0] || Y >= g.c[1]) continue;
-    const RowBits r = rb[ix][iy];
-    if (!(r.xc | r.yc | r.zc | r.nt)) continue;
-    const int j = lane, Z = Z0 + j;
-    // vertices: one per crossing edge owned by the cell, in axis order (src/cumc.cu:370-410)
-    const int fl = row_flags(r, j);
-    if (fl) {
-      int64_t v = (int64_t)vb[ix][iy][0] + row_prefix(r, j);
+  // vertices (src/cumc.cu:370-410)
+  for (uint32_t i = threadIdx.x; i < nvi; i += blockDim.x) {
+    int x, y, j, a;
+    item_decode(vitems[i], x, y, j, a);
+    S p[3];
+    edge_vertex<S>(f, X0 + x, Y0 + y, Z0 + j, a, p);
+    store_vertex<S>(verts, vid(x, y, j, a), p, g, normalize);
+  }
+  // triangles (src/cumc.cu:564-649): each table edge -> owner cell (+0/+1) -> its vertex
+  for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
+    int x, y, j, a;
+    item_decode(citems[i], x, y, j, a);
+    const uint64_t w = mc_tri(mc_from_morton(code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], j + 1)));
+    const int nt = (int)(w & 15);
+    const int64_t f0 = (int64_t)fb[x][y] + fpre[x][y][j];
+    for (int t = 0; t < nt; ++t) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a)
-        if (fl & (1 << a)) {
-          S p[3];
-          edge_vertex<S>(f, X, Y, Z, a, p);
-          store_vertex<S>(verts, v++, p, g, normalize);
-        }
-    }
-    // triangles (src/cumc.cu:564-649): each table edge -> owner cell (+0/+1) -> its vertex
-    uint64_t w = 0;
-    if ((r.nt >> j) & 1) w = mc_tri(mc_from_morton(code8(m[ix][iy], m[ix + 1][iy], m[ix][iy + 1], m[ix + 1][iy + 1], j + 1)));
-    const uint32_t nt = (uint32_t)(w & 15);
-    const uint32_t tinc = warp_incl(nt);
-    if (nt) {
-      const int64_t f0 = (int64_t)fb[ix][iy] + (tinc - nt);
-      for (uint32_t t = 0; t < nt; ++t) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int e = (int)((w >> (4 + 4 * (3 * t + k))) & 15);
-          const int ge = g_edge[e];
-          faces[3 * (f0 + t) + k] = vid(ix + (ge & 1), iy + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3);
-        }
+      for (int k = 0; k < 3; ++k) {
+        const int e = (int)((w >> (4 + 4 * (3 * t + k))) & 15);
+        const int ge = g_edge[e];
+        faces[3 * (f0 + t) + k] = vid(x + (ge & 1), y + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3);
       }
     }
   }
@@ -423,6 +500,10 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
   __shared__ int16_t pp[CX][CY][TZ + 1];  // first patch of the cell inside its segment
   __shared__ uint32_t pb[CX][CY];
   __shared__ uint32_t qb[TX][TY];
+  __shared__ uint16_t qitems[EMIT_ITEMS];
+  __shared__ uint16_t citems[TX * TY * TZ];
+  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
+  __shared__ uint32_t nqi, nci;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
@@ -461,71 +542,88 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
       pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
     }
   }
+  // work lists of the own rows: crossing edges (quads) and non-trivial cells (dual vertices)
+  uint32_t cq = 0, cc = 0;
+  RowBits own = {0u, 0u, 0u, 0u};
+  const int ox = threadIdx.x / TY, oy = threadIdx.x % TY;
+  if (threadIdx.x < TX * TY && X0 + ox < g.c[0] && Y0 + oy < g.c[1]) {
+    own = row_bits(m[ox + 1][oy + 1], m[ox + 2][oy + 1], m[ox + 1][oy + 2], m[ox + 2][oy + 2], valid);
+    cq = __popc(own.xc) + __popc(own.yc) + __popc(own.zc);
+    cc = __popc(own.nt);
+  }
+  uint32_t tot;
+  const uint32_t off = block_excl_scan(cq | (cc << 16), wsum, tot);
+  if (threadIdx.x == 0) {
+    nqi = tot & 0xffffu;
+    nci = tot >> 16;
+  }
+  if (threadIdx.x < TX * TY) {
+    uint32_t o = off & 0xffffu;
+    uint32_t b = own.xc | own.yc | own.zc;
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      const int fl = row_flags(own, j);
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        if (fl & (1 << a)) qitems[o++] = item_code(ox, oy, j, a);
+    }
+    put_items(citems, off >> 16, own.nt, ox, oy, 0);
+  }
   __syncthreads();
-
-#pragma unroll 1
-  for (int si = warp; si < TX * TY; si += TY) {
-    const int ix = si / TY, iy = si % TY, X = X0 + ix, Y = Y0 + iy;
-    if (X >= g.c[0] || Y >= g.c[1]) continue;
+  // quads: one per crossing edge owned by the cell (src/cudualmc.cu:753-794, 1019-1056);
+  // the edge exits (value falls through iso) when its start point is >= iso
+  for (uint32_t i = threadIdx.x; i < nqi; i += blockDim.x) {
+    int ix, iy, j, a;
+    item_decode(qitems[i], ix, iy, j, a);
     const int x = ix + 1, y = iy + 1;  // window cell / mask row of the own row
     const RowBits r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
-    if (!r.nt) continue;
-    const int j = lane, Z = Z0 + j;
+    const int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
+    const int type = a + 3 * (int)((m[x][y] >> (j + 1)) & 1);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int q = g_dmc_quad[4 * type + k];
+      const int nx = x + (q & 3) - 1, ny = y + ((q >> 2) & 3) - 1, nz = j + 1 + ((q >> 4) & 3) - 1;
+      quads[4 * qid + k] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8);
+    }
+  }
+  // dual vertices: mean of the patch's edge vertices, edges in ascending id
+  // (create_dmc_verts_kernel, src/cudualmc.cu:907-955)
+  for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
+    int ix, iy, j, a;
+    item_decode(citems[i], ix, iy, j, a);
+    const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
     const int code = rc[x][y][j + 1];
     const uint64_t w = dmc_case(code);
     const int np = dmc_npatch(w);
-    // dual vertices: mean of the patch's edge vertices, edges in ascending id
-    // (create_dmc_verts_kernel, src/cudualmc.cu:907-955)
-    if (np) {
-      S acc[4][3];
-      int cnt[4] = {0, 0, 0, 0};
+    S acc[4][3];
+    int cnt[4] = {0, 0, 0, 0};
 #pragma unroll
-      for (int p = 0; p < 4; ++p) acc[p][0] = acc[p][1] = acc[p][2] = S(0);
+    for (int p = 0; p < 4; ++p) acc[p][0] = acc[p][1] = acc[p][2] = S(0);
 #pragma unroll
-      for (int e = 0; e < 12; ++e) {
-        const int ge = g_edge[e], s = ge & 7, a = ge >> 3;
-        if ((((code >> s) ^ (code >> (s | (1 << a)))) & 1) == 0) continue;
-        const int p = dmc_patch_of(w, e);
-        S v[3];
-        edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), a, v);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (q == p) {
-            acc[q][0] += v[0];
-            acc[q][1] += v[1];
-            acc[q][2] += v[2];
-            cnt[q] += 1;
-          }
-      }
-      const int64_t p0 = (int64_t)pb[x][y] + pp[x][y][j + 1];
+    for (int e = 0; e < 12; ++e) {
+      const int ge = g_edge[e], s = ge & 7, ax = ge >> 3;
+      if ((((code >> s) ^ (code >> (s | (1 << ax)))) & 1) == 0) continue;
+      const int p = dmc_patch_of(w, e);
+      S v[3];
+      edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
 #pragma unroll
       for (int q = 0; q < 4; ++q)
-        if (q < np) {
-          const S inv = S(1) / S(cnt[q]);
-          const S v[3] = {acc[q][0] * inv, acc[q][1] * inv, acc[q][2] * inv};
-          store_vertex<S>(verts, p0 + q, v, g, normalize);
+        if (q == p) {
+          acc[q][0] += v[0];
+          acc[q][1] += v[1];
+          acc[q][2] += v[2];
+          cnt[q] += 1;
         }
     }
-    // quads: one per crossing edge owned by the cell (src/cudualmc.cu:753-794, 1019-1056);
-    // the edge exits (value falls through iso) when its start point is >= iso
-    const int fl = row_flags(r, j);
-    if (fl) {
-      int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j);
-      const int exiting = (int)((m[x][y] >> (j + 1)) & 1);
+    const int64_t p0 = (int64_t)pb[x][y] + pp[x][y][j + 1];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        if (!(fl & (1 << a))) continue;
-        const int type = a + 3 * exiting;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int q = g_dmc_quad[4 * type + i];
-          const int nx = x + (q & 3) - 1, ny = y + ((q >> 2) & 3) - 1, nz = j + 1 + ((q >> 4) & 3) - 1;
-          const int eid = q >> 8;
-          quads[4 * qid + i] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), eid);
-        }
-        ++qid;
+    for (int q = 0; q < 4; ++q)
+      if (q < np) {
+        const S inv = S(1) / S(cnt[q]);
+        const S v[3] = {acc[q][0] * inv, acc[q][1] * inv, acc[q][2] * inv};
+        store_vertex<S>(verts, p0 + q, v, g, normalize);
       }
-    }
   }
 }
 
@@ -538,12 +636,11 @@ __device__ __forceinline__ void load_grad(const S* __restrict__ gv, int64_t i, c
   for (int k = 0; k < 3; ++k) out[k] = __ldg(gv + 3 * i + k) * scale[k];
 }
 
-// adjoint of edge_vertex at one endpoint (adjComputeMcVert, src/cumc.cu:412-453):
-// the edge runs from padded point A along axis a; `end` = 0 when the point being
-// differentiated is A, 1 when it is A + e_a.  Adds into gs (dL/dsdf) and gd.
+// adjoint of edge_vertex (adjComputeMcVert, src/cumc.cu:412-453) for the edge from
+// padded point A along axis a: c0 = (dL/dsdf, dL/ddeform) at A, c1 at A + e_a
 template <class S>
-__device__ __forceinline__ void edge_adjoint(const Field<S>& f, int X, int Y, int Z, int a, int end, const S gvec[3],
-                                             S& gs, S gd[3]) {
+__device__ __forceinline__ void edge_adjoint2(const Field<S>& f, int X, int Y, int Z, int a, const S gvec[3], S c0[4],
+                                              S c1[4]) {
   const int ex = a == 0, ey = a == 1, ez = a == 2;
   const S d0 = f.at(X, Y, Z), d1 = f.at(X + ex, Y + ey, Z + ez);
   S t = S(0.5);
@@ -559,11 +656,14 @@ __device__ __forceinline__ void edge_adjoint(const Field<S>& f, int X, int Y, in
                    (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
   const S adj_t = dp[0] * gvec[0] + dp[1] * gvec[1] + dp[2] * gvec[2];
   const S den = (d1 - d0) * (d1 - d0);
-  const S w = end ? t : S(1) - t;
-  gs += (end ? (d0 - f.iso) : (f.iso - d1)) / den * adj_t;
-  gd[0] += w * gvec[0];
-  gd[1] += w * gvec[1];
-  gd[2] += w * gvec[2];
+  const S w0 = S(1) - t;
+  c0[0] = (f.iso - d1) / den * adj_t;
+  c1[0] = (d0 - f.iso) / den * adj_t;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    c0[k + 1] = w0 * gvec[k];
+    c1[k + 1] = t * gvec[k];
+  }
 }
 
 // Point tiles: unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ); in padded
@@ -623,32 +723,53 @@ __device__ __forceinline__ void ptile_coords(int64_t tile, const Geom& g, int& x
   z0 = tz * TZ;
 }
 
+// rows of cell-window coordinates whose edges along axis a touch the tile's points:
+// axis 0: x in [0, TX], y in [1, TY]; axis 1: x in [1, TX], y in [0, TY];
+// axis 2: x in [1, TX], y in [1, TY]
+constexpr int BW_ROWS0 = (TX + 1) * TY, BW_ROWS1 = TX * (TY + 1), BW_ROWS2 = TX * TY;
+constexpr int BW_ROWS = BW_ROWS0 + BW_ROWS1 + BW_ROWS2;
+constexpr int BW_ITEMS = BW_ROWS * (TZ + 1);
+static_assert(BW_ROWS <= NTHREADS, "one thread per backward item row");
+
 template <class S>
-__device__ __forceinline__ void write_point_grads(const Field<S>& f, S* __restrict__ gsdf, S* __restrict__ gdef,
-                                                  int X, int Y, int Z, S gs, const S gd[3]) {
-  const int64_t i = f.lin(X, Y, Z);
-  gsdf[i] = gs;
-  if (gdef) {
-    gdef[3 * i + 0] = gd[0];
-    gdef[3 * i + 1] = gd[1];
-    gdef[3 * i + 2] = gd[2];
-  }
+constexpr size_t backward_dyn_smem() {
+  return sizeof(S) * 2 * TX * TY * TZ * 4;
 }
 
-// MC: dL/dsdf and dL/ddeform of every point, gathered from its (at most six)
-// incident crossing edges.  Replaces adj_create_cell_mc_verts_kernel
-// (src/cumc.cu:474-512) plus the zero fills and the F.pad backward.
-template <class S>
-__global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                               const uint8_t* __restrict__ tile_flag,
-                                                               const S* __restrict__ gv, int normalize,
-                                                               S* __restrict__ gsdf, S* __restrict__ gdef) {
-  constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
-  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
+// dL/dsdf and dL/ddeform of every point of a tile.  Work list: the crossing edges
+// touching the tile, per axis.  Each edge's adjoint (adjComputeMcVert,
+// src/cumc.cu:412-453 / src/cudualmc.cu:710-751) is computed once and parked in the
+// slot of each endpoint inside the tile; each point then adds its (at most six)
+// slots in a fixed order, so the result is deterministic.  MC: the gradient
+// reaching an edge vertex is dL/dverts of that vertex (adj_create_cell_mc_verts_kernel,
+// src/cumc.cu:474-512).  DMC: it is the sum over the four cells around the edge of
+// dL/d(dual vertex) / (edges in that patch) (adj_create_dmc_verts_kernel,
+// src/cudualmc.cu:957-1005); the reference reads the gradient of the cell's first
+// patch for every patch of the cell (adj_verts[first] with first never advanced,
+// src/cudualmc.cu:990): exact = 0 reproduces that, exact = 1 uses each patch's own
+// gradient (the true derivative).  Replaces the forward re-run, the zero fills and
+// the F.pad backward of diso/__init__.py:30-44, 84-98.
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                            const uint8_t* __restrict__ tile_flag,
+                                                            const S* __restrict__ gv, int normalize, int exact,
+                                                            S* __restrict__ gsdf, S* __restrict__ gdef) {
+  constexpr int H = METHOD == DMC ? 1 : 0;  // DMC: one more mask row each side for the ambiguity test
+  constexpr int WX = TX + 2 + H, WY = TY + 2 + H;  // point rows [X0-H, X0+TX+1] x [Y0-H, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;          // cell rows [X0, X0+TX] x [Y0, Y0+TY]; mask row x + H
+  constexpr int RX = METHOD == DMC ? CX : 1, RY = METHOD == DMC ? CY : 1;
+  constexpr int NP = TX * TY * TZ;
   __shared__ uint64_t m[WX][WY];
   __shared__ RowBits rb[CX][CY];
   __shared__ uint8_t f32[CX][CY];
-  __shared__ uint32_t vb[CX][CY][2];
+  __shared__ uint32_t b0[CX][CY], b1[CX][CY];  // MC vertex / DMC patch bases of chunks zc and zc+1
+  __shared__ uint8_t rc[RX][RY][TZ + 1];
+  __shared__ uint8_t pre[RX][RY][TZ + 1];
+  __shared__ uint16_t items[BW_ITEMS];
+  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
+  __shared__ uint32_t aoff[4];
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  S* slot = reinterpret_cast<S*>(dyn_smem);  // [2][NP][4]: end 0 / end 1 adjoints of the current axis
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
   ptile_coords(blockIdx.x, g, X0, Y0, Z0);
@@ -657,13 +778,17 @@ __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom 
     return;
   }
   const int zc = Z0 / TZ;
+  const int WX0 = X0 - H, WY0 = Y0 - H;
   S dmn, dmx;
   bool dseen = false;
-  load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
+  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
   for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
     const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
     const int X = X0 + x, Y = Y0 + y, c = zc + k;
-    vb[x][y][k] = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? Counts::lo(seg[g.seg(X, Y, c)]) : 0u;
+    const uint64_t s = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? seg[g.seg(X, Y, c)] : 0ull;
+    const uint32_t v = METHOD == MC ? Counts::lo(s) : Counts::hi(s);
+    if (k) b1[x][y] = v;
+    else b0[x][y] = v;
   }
   __syncthreads();
   const uint32_t valid = zvalid(g, Z0);
@@ -672,154 +797,156 @@ __global__ void __launch_bounds__(NTHREADS) mc_backward_kernel(Field<S> f, Geom 
     RowBits r = {0u, 0u, 0u, 0u};
     int fl = 0;
     if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
-      r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
-      if (Z0 + TZ < g.c[2]) fl = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
+      const uint64_t a = m[x + H][y + H], b = m[x + H + 1][y + H], c = m[x + H][y + H + 1], d = m[x + H + 1][y + H + 1];
+      r = row_bits(a, b, c, d, valid);
+      if (Z0 + TZ < g.c[2]) fl = flags_at(a, b, c, TZ + 1);
     }
     rb[x][y] = r;
     f32[x][y] = (uint8_t)fl;
   }
-  __syncthreads();
-  S scale[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
-  auto flags = [&](int x, int y, int j) -> int { return j == TZ ? f32[x][y] : row_flags(rb[x][y], j); };
-  auto vid = [&](int x, int y, int j, int a) -> int64_t {
-    if (j == TZ) return (int64_t)vb[x][y][1] + __popc(f32[x][y] & ((1 << a) - 1));
-    const RowBits r = rb[x][y];
-    return (int64_t)vb[x][y][0] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
-  };
-#pragma unroll 1
-  for (int ix = 0; ix < TX; ++ix) {
-    // point (X, Y, Z) is window cell (x, y, z)
-    const int x = ix + 1, y = warp + 1, z = lane + 1;
-    const int X = X0 + x, Y = Y0 + y, Z = Z0 + z;
-    if (!f.inside(X, Y, Z)) continue;
-    S gs = S(0), gd[3] = {S(0), S(0), S(0)};
-    const int own = flags(x, y, z);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (own & (1 << a)) {
-        S gvec[3];
-        load_grad<S>(gv, vid(x, y, z, a), scale, gvec);
-        edge_adjoint<S>(f, X, Y, Z, a, 0, gvec, gs, gd);
-      }
-      const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
-      if (flags(px, py, pz) & (1 << a)) {
-        S gvec[3];
-        load_grad<S>(gv, vid(px, py, pz, a), scale, gvec);
-        edge_adjoint<S>(f, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
+  if constexpr (METHOD == DMC) {
+    // resolved codes and in-segment patch prefixes of the window cells
+    for (int r = warp; r < CX * CY; r += TY) {
+      const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
+      const bool row = X < g.c[0] && Y < g.c[1];
+      const uint64_t a = m[x + H][y + H], b = m[x + H + 1][y + H], c = m[x + H][y + H + 1], d = m[x + H + 1][y + H + 1];
+      const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
+      int code = 0;
+      if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
+      const uint32_t np = dmc_npatch(dmc_case(code));
+      const uint32_t inc = nt ? warp_incl(np) : 0u;
+      rc[x][y][lane] = (uint8_t)code;
+      pre[x][y][lane] = (uint8_t)(inc - np);
+      if (lane == 0) {
+        int c32 = 0;
+        if (row && Z0 + TZ < g.c[2]) {
+          c32 = code8(a, b, c, d, TZ + 1);
+          if (c32 != 0 && c32 != 255) c32 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c32, X, Y, Z0 + TZ, g);
+        }
+        rc[x][y][TZ] = (uint8_t)c32;
+        pre[x][y][TZ] = 0;  // first cell of the next segment
       }
     }
-    write_point_grads<S>(f, gsdf, gdef, X, Y, Z, gs, gd);
   }
-}
+  __syncthreads();
+  // work list: crossing edges touching the tile, grouped by axis
+  int ra = -1, rx = 0, ry = 0;
+  uint64_t bits = 0;
+  {
+    const int t = threadIdx.x;
+    if (t < BW_ROWS0) {
+      ra = 0;
+      rx = t / TY;
+      ry = 1 + t % TY;
+    } else if (t < BW_ROWS0 + BW_ROWS1) {
+      ra = 1;
+      rx = 1 + (t - BW_ROWS0) / (TY + 1);
+      ry = (t - BW_ROWS0) % (TY + 1);
+    } else if (t < BW_ROWS) {
+      ra = 2;
+      rx = 1 + (t - BW_ROWS0 - BW_ROWS1) / TY;
+      ry = 1 + (t - BW_ROWS0 - BW_ROWS1) % TY;
+    }
+    if (ra >= 0) {
+      const RowBits r = rb[rx][ry];
+      const uint32_t lo = ra == 0 ? r.xc : (ra == 1 ? r.yc : r.zc);
+      bits = (uint64_t)lo | ((uint64_t)((f32[rx][ry] >> ra) & 1) << TZ);
+      if (ra < 2) bits &= ~1ull;  // x / y edges of cell Z0 touch no point of the tile
+    }
+  }
+  uint32_t tot;
+  const uint32_t off = block_excl_scan((uint32_t)__popcll((long long)bits), wsum, tot);
+  if (threadIdx.x == 0) {
+    aoff[0] = 0;
+    aoff[3] = tot;
+  }
+  if (threadIdx.x == BW_ROWS0) aoff[1] = off;
+  if (threadIdx.x == BW_ROWS0 + BW_ROWS1) aoff[2] = off;
+  if (ra >= 0) put_items(items, off, bits, rx, ry, ra);
+  __syncthreads();
 
-// DMC: as above, but the gradient reaching an edge vertex is the sum over the
-// four cells around the edge of dL/d(dual vertex) / (edges in that patch)
-// (adj_create_dmc_verts_kernel, src/cudualmc.cu:957-1005).  The reference reads
-// the gradient of the cell's first patch for every patch of the cell
-// (adj_verts[first] with first never advanced, src/cudualmc.cu:990); exact = 0
-// reproduces that, exact = 1 uses each patch's own gradient (the true derivative).
-template <class S>
-__global__ void __launch_bounds__(NTHREADS) dmc_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                                const uint8_t* __restrict__ tile_flag,
-                                                                const S* __restrict__ gv, int normalize, int exact,
-                                                                S* __restrict__ gsdf, S* __restrict__ gdef) {
-  constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
-  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]; mask row of cell (x, y) is (x+1, y+1)
-  __shared__ uint64_t m[WX][WY];
-  __shared__ uint8_t rc[CX][CY][TZ + 1];
-  __shared__ uint8_t pre[CX][CY][TZ + 1];
-  __shared__ uint32_t pb[CX][CY][2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int X0, Y0, Z0;
-  ptile_coords(blockIdx.x, g, X0, Y0, Z0);
-  if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
-    zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
-    return;
-  }
-  const int zc = Z0 / TZ;
-  const int WX0 = X0 - 1, WY0 = Y0 - 1;
-  S dmn, dmx;
-  bool dseen = false;
-  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
-  for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
-    const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
-    const int X = X0 + x, Y = Y0 + y, c = zc + k;
-    pb[x][y][k] = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? Counts::hi(seg[g.seg(X, Y, c)]) : 0u;
-  }
-  __syncthreads();
-  const uint32_t valid = zvalid(g, Z0);
-  for (int r = warp; r < CX * CY; r += TY) {
-    const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
-    const bool row = X < g.c[0] && Y < g.c[1];
-    const uint64_t a = m[x + 1][y + 1], b = m[x + 2][y + 1], c = m[x + 1][y + 2], d = m[x + 2][y + 2];
-    const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
-    int code = 0;
-    if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
-    const uint32_t np = dmc_npatch(dmc_case(code));
-    const uint32_t inc = nt ? warp_incl(np) : 0u;
-    rc[x][y][lane] = (uint8_t)code;
-    pre[x][y][lane] = (uint8_t)(inc - np);
-    if (lane == 0) {
-      int c32 = 0;
-      if (row && Z0 + TZ < g.c[2]) {
-        c32 = code8(a, b, c, d, TZ + 1);
-        if (c32 != 0 && c32 != 255) c32 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c32, X, Y, Z0 + TZ, g);
-      }
-      rc[x][y][TZ] = (uint8_t)c32;
-      pre[x][y][TZ] = 0;  // first cell of the next segment
-    }
-  }
-  __syncthreads();
   S scale[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
-  // dL/d(edge vertex) of the crossing edge owned by window cell (ox, oy, oz) along a
-  auto edge_grad = [&](int ox, int oy, int oz, int a, S out[3]) {
-    out[0] = out[1] = out[2] = S(0);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int db = k & 1, dc = k >> 1;
-      // the cell one step back along the two other axes (b, c) = (a+1, a+2) mod 3
-      const int cx = ox - (a == 1 ? dc : (a == 2 ? db : 0));
-      const int cy = oy - (a == 0 ? db : (a == 2 ? dc : 0));
-      const int cz = oz - (a == 0 ? dc : (a == 1 ? db : 0));
-      const int start = (ox - cx) | ((oy - cy) << 1) | ((oz - cz) << 2);
-      const int code = rc[cx][cy][cz];
-      const uint64_t w = dmc_case(code);
-      const int p = dmc_patch_of(w, g_edge_of[3 * start + a]);
-      const S inv = S(1) / S(dmc_patch_size(w, p));
-      const int64_t pid = (int64_t)pb[cx][cy][cz == TZ ? 1 : 0] + pre[cx][cy][cz] + (exact ? p : 0);
-      S v[3];
-      load_grad<S>(gv, pid, scale, v);
-      out[0] += v[0] * inv;
-      out[1] += v[1] * inv;
-      out[2] += v[2] * inv;
-    }
+  auto crossing = [&](int x, int y, int j, int a) -> int {
+    return j == TZ ? (f32[x][y] >> a) & 1 : (row_flags(rb[x][y], j) >> a) & 1;
   };
+  S acc[TX][4];
+#pragma unroll
+  for (int ix = 0; ix < TX; ++ix) acc[ix][0] = acc[ix][1] = acc[ix][2] = acc[ix][3] = S(0);
 #pragma unroll 1
-  for (int ix = 0; ix < TX; ++ix) {
-    const int x = ix + 1, y = warp + 1, z = lane + 1;
-    const int X = X0 + x, Y = Y0 + y, Z = Z0 + z;
-    if (!f.inside(X, Y, Z)) continue;
-    S gs = S(0), gd[3] = {S(0), S(0), S(0)};
-    const int own = cross_flags(rc[x][y][z]);
-#pragma unroll 1
-    for (int a = 0; a < 3; ++a) {
-      if (own & (1 << a)) {
-        S gvec[3];
-        edge_grad(x, y, z, a, gvec);
-        edge_adjoint<S>(f, X, Y, Z, a, 0, gvec, gs, gd);
+  for (int a = 0; a < 3; ++a) {
+    for (uint32_t i = aoff[a] + threadIdx.x; i < aoff[a + 1]; i += blockDim.x) {
+      int x, y, j, ia;
+      item_decode(items[i], x, y, j, ia);
+      S gvec[3];
+      if constexpr (METHOD == MC) {
+        const int64_t v = j == TZ ? (int64_t)b1[x][y] + __popc(f32[x][y] & ((1 << a) - 1))
+                                  : (int64_t)b0[x][y] + row_prefix(rb[x][y], j) +
+                                        __popc(row_flags(rb[x][y], j) & ((1 << a) - 1));
+        load_grad<S>(gv, v, scale, gvec);
+      } else {
+        gvec[0] = gvec[1] = gvec[2] = S(0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int db = k & 1, dc = k >> 1;
+          // the cell one step back along the two other axes (b, c) = (a+1, a+2) mod 3
+          const int cx = x - (a == 1 ? dc : (a == 2 ? db : 0));
+          const int cy = y - (a == 0 ? db : (a == 2 ? dc : 0));
+          const int cz = j - (a == 0 ? dc : (a == 1 ? db : 0));
+          const int start = (x - cx) | ((y - cy) << 1) | ((j - cz) << 2);
+          const uint64_t w = dmc_case(rc[cx][cy][cz]);
+          const int p = dmc_patch_of(w, g_edge_of[3 * start + a]);
+          const S inv = S(1) / S(dmc_patch_size(w, p));
+          const int64_t pid = (int64_t)(cz == TZ ? b1[cx][cy] : b0[cx][cy]) + pre[cx][cy][cz] + (exact ? p : 0);
+          S v[3];
+          load_grad<S>(gv, pid, scale, v);
+          gvec[0] += v[0] * inv;
+          gvec[1] += v[1] * inv;
+          gvec[2] += v[2] * inv;
+        }
       }
-      const int px = x - (a == 0), py = y - (a == 1), pz = z - (a == 2);
-      if (cross_flags(rc[px][py][pz]) & (1 << a)) {
-        S gvec[3];
-        edge_grad(px, py, pz, a, gvec);
-        edge_adjoint<S>(f, X0 + px, Y0 + py, Z0 + pz, a, 1, gvec, gs, gd);
+      S c0[4], c1[4];
+      edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
+      if (x >= 1 && y >= 1 && j >= 1) {
+        S* s0 = slot + 4 * (((x - 1) * TY + (y - 1)) * TZ + (j - 1));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s0[k] = c0[k];
+      }
+      const int x1 = x + (a == 0), y1 = y + (a == 1), j1 = j + (a == 2);
+      if (x1 <= TX && y1 <= TY && j1 <= TZ) {
+        S* s1 = slot + 4 * (NP + ((x1 - 1) * TY + (y1 - 1)) * TZ + (j1 - 1));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s1[k] = c1[k];
       }
     }
-    write_point_grads<S>(f, gsdf, gdef, X, Y, Z, gs, gd);
+    __syncthreads();
+#pragma unroll
+    for (int ix = 0; ix < TX; ++ix) {
+      const int x = ix + 1, y = warp + 1, j = lane + 1;
+      const int p = (ix * TY + warp) * TZ + lane;
+      if (crossing(x, y, j, a)) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[ix][k] += slot[4 * p + k];
+      }
+      if (crossing(x - (a == 0), y - (a == 1), j - (a == 2), a)) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[ix][k] += slot[4 * (NP + p) + k];
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int ix = 0; ix < TX; ++ix) {
+    const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
+    if (!f.inside(X, Y, Z)) continue;
+    const int64_t i = f.lin(X, Y, Z);
+    gsdf[i] = acc[ix][0];
+    if (gdef) {
+      gdef[3 * i + 0] = acc[ix][1];
+      gdef[3 * i + 1] = acc[ix][2];
+      gdef[3 * i + 2] = acc[ix][3];
+    }
   }
 }
 
