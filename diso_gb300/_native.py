@@ -54,6 +54,9 @@ EXPORTS = {
                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p]),
+    "diso_forward_count_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
     "diso_last_error": (ctypes.c_char_p, []),
     "diso_version": (ctypes.c_char_p, []),
 }

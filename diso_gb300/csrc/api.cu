@@ -5,6 +5,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 
 #include "../../include/diso_gb300.h"
@@ -355,3 +356,127 @@ const char* diso_last_error(void) { return g_err; }
 const char* diso_version(void) { return "diso_gb300 0.1.0 (sm_103a)"; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// diso_forward_count_static: the forward count phase without any allocation.
+//
+// Its scratch (status words, the list of active tiles, the look-back state of
+// the scan) lives in one file-scope device array instead of buffers owned by an
+// extractor.  Host code cannot use the array's name as a device address, so at
+// the first call on each device (with that device current) the address is looked
+// up with cudaGetSymbolAddress and cached.
+namespace {
+
+constexpr int64_t kStaticMaxTiles = 65536;      // 4x8x32-cell tiles of one grid
+constexpr int64_t kStaticMaxScanTiles = 2048;   // look-back tiles of 2048 segments
+
+struct StaticScratch {
+  Stats stats;
+  uint32_t scan_flag[kStaticMaxScanTiles];
+  uint64_t scan_agg[kStaticMaxScanTiles];
+  uint64_t scan_incl[kStaticMaxScanTiles];
+  int active[kStaticMaxTiles];
+};
+
+__device__ __align__(256) unsigned char g_static_scratch[sizeof(StaticScratch)];
+
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+StaticScratch* g_static_ptr[kStaticMaxDevices] = {};
+int g_static_ctas[kStaticMaxDevices][4] = {};  // resident count-kernel CTAs per (method, dtype)
+
+int static_setup(int dev, StaticScratch** out, int method, int dtype, int* ctas) {
+  if (dev < 0 || dev >= kStaticMaxDevices) return fail(DISO_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+    int sms = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int per[4] = {0, 0, 0, 0};
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], count_kernel<float, MC>, NTHREADS, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], count_kernel<float, DMC>, NTHREADS, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], count_kernel<double, MC>, NTHREADS, 0));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], count_kernel<double, DMC>, NTHREADS, 0));
+    for (int k = 0; k < 4; ++k) g_static_ctas[dev][k] = sms * std::max(per[k], 1);
+    g_static_ptr[dev] = (StaticScratch*)p;
+  }
+  *out = g_static_ptr[dev];
+  *ctas = g_static_ctas[dev][2 * dtype + method];
+  return DISO_OK;
+}
+
+template <class S>
+int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sdf, int nx, int ny, int nz,
+                         double iso, double padval, uint64_t* seg, cudaStream_t s, diso_counts* out) {
+  Geom g;
+  g.init(nx, ny, nz);
+  // clear what must start at zero (the array keeps the previous call's contents)
+  CUDA_TRY(cudaMemsetAsync(&sc->stats, 0, sizeof(Stats), s));
+  CUDA_TRY(cudaMemsetAsync(&sc->stats.min_key, 0xff, sizeof(unsigned long long), s));
+  Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
+  const int64_t blocks = count_blocks(g);
+  const int64_t per_block = (CP / TX) * (CR / TY);
+  const int64_t want = std::max<int64_t>(ctas, (blocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::min<int64_t>(want, blocks);
+  if (method == DISO_MC)
+    count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), &sc->stats, sc->active);
+  else
+    count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), &sc->stats, sc->active);
+  CUDA_TRY(cudaGetLastError());
+  const int64_t tiles = (g.nseg + 1 + SCAN_TILE - 1) / SCAN_TILE;
+  CUDA_TRY(cudaMemsetAsync(sc->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
+  ScanState st{sc->scan_flag, sc->scan_agg, sc->scan_incl};
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(seg, g.nseg, st, &sc->stats);
+  CUDA_TRY(cudaGetLastError());
+  Stats h;
+  uint64_t total = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h, &sc->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(&total, seg + g.nseg, sizeof total, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
+  if (method == DISO_MC) {
+    out->n_verts = Counts::lo(total);
+    out->n_faces = Counts::hi(total);
+  } else {
+    out->n_verts = Counts::hi(total);
+    out->n_faces = Counts::lo(total);
+  }
+  out->sdf_min = key_to_double(h.min_key);
+  out->sdf_max = key_to_double(h.max_key);
+  const double isoS = (double)(S)iso;
+  out->empty = (out->sdf_min >= isoS || out->sdf_max <= isoS) ? 1 : 0;
+  out->pad_ = 0;
+  out->n_active_tiles = (int64_t)h.n_active;
+  return DISO_OK;
+}
+
+}  // namespace
+
+extern "C" int diso_forward_count_static(int method, int dtype, const void* sdf, int nx, int ny, int nz,
+                                         double isovalue, double padval, uint64_t* seg, void* stream,
+                                         diso_counts* out) {
+  if (method != DISO_MC && method != DISO_DMC) return fail(DISO_ERR_ARG, "unknown method %d", method);
+  if (dtype != DISO_F32 && dtype != DISO_F64) return fail(DISO_ERR_ARG, "unknown dtype %d", dtype);
+  if (!sdf || !seg || !out) return fail(DISO_ERR_ARG, "null sdf, seg or counts");
+  if (nx < 1 || ny < 1 || nz < 1) return fail(DISO_ERR_ARG, "grid dims must be >= 1 (got %d x %d x %d)", nx, ny, nz);
+  Geom g;
+  g.init(nx, ny, nz);
+  const int64_t scan_tiles = (g.nseg + 1 + SCAN_TILE - 1) / SCAN_TILE;
+  if (g.ntiles() > kStaticMaxTiles || scan_tiles > kStaticMaxScanTiles)
+    return fail(DISO_ERR_ARG,
+                "grid %d x %d x %d too large for diso_forward_count_static: %lld tiles (max %lld), %lld scan tiles "
+                "(max %lld); use diso_forward_count",
+                nx, ny, nz, (long long)g.ntiles(), (long long)kStaticMaxTiles, (long long)scan_tiles,
+                (long long)kStaticMaxScanTiles);
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  StaticScratch* sc = nullptr;
+  int ctas = 0;
+  int rc = static_setup(dev, &sc, method, dtype, &ctas);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  return dtype == DISO_F32
+             ? forward_count_static<float>(method, sc, ctas, sdf, nx, ny, nz, isovalue, padval, seg, s, out)
+             : forward_count_static<double>(method, sc, ctas, sdf, nx, ny, nz, isovalue, padval, seg, s, out);
+}

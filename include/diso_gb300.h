@@ -113,6 +113,26 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                   double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
                   void* grad_sdf, void* grad_deform, void* stream);
 
+/* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
+ * device memory: code running while a stream is being captured, where cudaMalloc
+ * is not allowed, and serving processes that fix their device memory at start-up
+ * and may not grow it per request.  No counterpart in the reference.
+ *
+ * It takes no extractor: its scratch (status words, active-tile list, scan state,
+ * about 300 KB) is one static device array of this library, which every GPU that
+ * loads the library holds until the process exits.  Nothing is allocated: no
+ * cudaMalloc / cudaFree / cudaMallocHost.  Grids of at most 65536 4x8x32-cell tiles
+ * (about 384^3; more precisely also at most 2048 x 2048 - 1 row segments) are
+ * accepted, larger ones fail with DISO_ERR_ARG and a message.  The first call on a
+ * device looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array: calls whose GPU work overlaps (other
+ * streams, other threads) race and must be serialised by the caller.  `seg` and
+ * the result have the meaning they have for diso_forward_count (diso_forward_emit
+ * then needs an extractor that ran diso_forward_count; diso_backward can use this
+ * `seg` directly). */
+int diso_forward_count_static(int method, int dtype, const void* sdf, int nx, int ny, int nz, double isovalue,
+                              double padval, uint64_t* seg, void* stream, diso_counts* out);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* diso_last_error(void);
 
