@@ -9,7 +9,8 @@ Drop-in for the reference package's public API (diso/__init__.py):
 The compute path is hand-written sm_103a CUDA behind the C ABI of
 include/diso_gb300.h; there is no CPU path.
 """
+from .batch import BatchPlan, DiffDMCBatch, DiffMCBatch, extract_batch  # noqa: F401
 from .extraction import DiffDMC, DiffMC, extract  # noqa: F401
 
-__all__ = ["DiffMC", "DiffDMC", "extract"]
+__all__ = ["DiffMC", "DiffDMC", "extract", "DiffMCBatch", "DiffDMCBatch", "extract_batch", "BatchPlan"]
 __version__ = "0.1.0"

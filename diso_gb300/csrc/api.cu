@@ -48,8 +48,32 @@ struct diso_extractor {
   int64_t split_cap = 0;
   int64_t last_active = 0;       // from the last forward count
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
+  int sms = 0;
+
+  // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
+  void* bdesc = nullptr;         // device BatchGrid<S>[MAX_BATCH]
+  void* bdesc_host = nullptr;    // pinned staging
+  Stats* bstats = nullptr;       // device Stats[MAX_BATCH]
+  Stats* bstats_host = nullptr;
+  uint64_t* bbound = nullptr;    // device: scanned value at each grid's first segment, + total
+  uint64_t* bbound_host = nullptr;
+  uint64_t* brecord = nullptr;   // the caller's batch record
+  int bn = 0;                    // grids in the prepared batch
+  int64_t bseg_total = 0, bblocks = 0, bptiles = 0, btiles = 0;
+  int64_t bseg_off[MAX_BATCH + 1] = {};
+  int bcount_ctas = 0, bwork_ctas = 0;
 
   void release() {
+    cudaFree(bdesc);
+    cudaFreeHost(bdesc_host);
+    cudaFree(bstats);
+    cudaFreeHost(bstats_host);
+    cudaFree(bbound);
+    cudaFreeHost(bbound_host);
+    bdesc = bdesc_host = nullptr;
+    bstats = bstats_host = nullptr;
+    bbound = bbound_host = nullptr;
+    bn = 0;
     cudaFree(stats);
     cudaFreeHost(stats_host);
     cudaFree(scan_flag);
@@ -99,6 +123,7 @@ int bind_device(diso_extractor* ex) {
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per_sm, ex->method == DISO_MC ? count_kernel<double, MC> : count_kernel<double, DMC>, NTHREADS, 0));
     ex->resident_ctas = sms * std::max(per_sm, 1);
+    ex->sms = sms;
   }
   return DISO_OK;
 }
@@ -264,6 +289,199 @@ int split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int
   return DISO_OK;
 }
 
+// ------------------------------------------------------------------ batches
+
+// zero the per-grid status words, min keys to the top
+__global__ void init_stats_kernel(Stats* st, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    Stats z = {};
+    z.min_key = ~0ull;
+    st[i] = z;
+  }
+}
+
+// scanned value at the first segment of every grid, and the total
+__global__ void gather_bounds_kernel(const uint64_t* seg, const int64_t* off, int n, uint64_t* out) {
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) out[i] = seg[off[i]];
+}
+
+int64_t batch_record_slots(const diso_grid* grids, int n, int64_t* seg_total, int64_t* tiles_total) {
+  int64_t segs = 0, tiles = 0;
+  for (int i = 0; i < n; ++i) {
+    Geom g;
+    g.init(grids[i].nx, grids[i].ny, grids[i].nz);
+    segs += g.nseg;
+    tiles += g.ntiles();
+  }
+  if (seg_total) *seg_total = segs;
+  if (tiles_total) *tiles_total = tiles;
+  // segments of every grid, the total slot, then one activity byte per tile of every grid
+  return segs + 1 + (tiles + 7) / 8;
+}
+
+template <class S>
+int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* record, cudaStream_t s) {
+  if (!ex->bdesc) {
+    CUDA_TRY(cudaMalloc(&ex->bdesc, sizeof(BatchGrid<double>) * MAX_BATCH));
+    CUDA_TRY(cudaMallocHost(&ex->bdesc_host, sizeof(BatchGrid<double>) * MAX_BATCH + sizeof(int64_t) * (MAX_BATCH + 1)));
+    CUDA_TRY(cudaMalloc((void**)&ex->bstats, sizeof(Stats) * MAX_BATCH));
+    CUDA_TRY(cudaMallocHost((void**)&ex->bstats_host, sizeof(Stats) * MAX_BATCH));
+    CUDA_TRY(cudaMalloc((void**)&ex->bbound, sizeof(uint64_t) * (MAX_BATCH + 1) + sizeof(int64_t) * (MAX_BATCH + 1)));
+    CUDA_TRY(cudaMallocHost((void**)&ex->bbound_host, sizeof(uint64_t) * (MAX_BATCH + 1)));
+    int per = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per, ex->method == DISO_MC ? batch_count_kernel<S, MC> : batch_count_kernel<S, DMC>, NTHREADS, 0));
+    ex->bcount_ctas = ex->sms * std::max(per, 1);
+    ex->bwork_ctas = ex->sms * 4;
+    const size_t smem = backward_dyn_smem<S>();
+    CUDA_TRY(cudaFuncSetAttribute(batch_backward_kernel<S, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUDA_TRY(cudaFuncSetAttribute(batch_backward_kernel<S, DMC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  // the previous prepare's upload must have left the staging buffer
+  CUDA_TRY(cudaStreamSynchronize(s));
+  BatchGrid<S>* d = (BatchGrid<S>*)ex->bdesc_host;
+  int64_t* offs = (int64_t*)((char*)ex->bdesc_host + sizeof(BatchGrid<double>) * MAX_BATCH);
+  int64_t seg_off = 0, tile_off = 0, cblk = 0, ptile = 0;
+  int64_t seg_total = 0, tiles_total = 0;
+  batch_record_slots(grids, n, &seg_total, &tiles_total);
+  uint8_t* flags = (uint8_t*)(record + seg_total + 1);
+  for (int i = 0; i < n; ++i) {
+    const diso_grid& q = grids[i];
+    BatchGrid<S> b;
+    b.f = make_field<S>(q.sdf, q.deform, q.nx, q.ny, q.nz, q.isovalue, q.padval);
+    b.g.init(q.nx, q.ny, q.nz);
+    b.seg = record + seg_off;
+    b.seg_end = record + seg_off + b.g.nseg;
+    b.tile_flag = flags + tile_off;
+    b.cblk0 = cblk;
+    b.ptile0 = ptile;
+    b.gsdf = (S*)q.grad_sdf;
+    b.gdef = q.deform ? (S*)q.grad_deform : nullptr;
+    d[i] = b;
+    offs[i] = seg_off;
+    ex->bseg_off[i] = seg_off;
+    seg_off += b.g.nseg;
+    tile_off += b.g.ntiles();
+    cblk += count_blocks(b.g);
+    ptile += b.g.nptiles();
+  }
+  offs[n] = seg_off;
+  ex->bseg_off[n] = seg_off;
+  ex->bn = n;
+  ex->brecord = record;
+  ex->bseg_total = seg_total;
+  ex->btiles = tiles_total;
+  ex->bblocks = cblk;
+  ex->bptiles = ptile;
+  int rc;
+  if ((rc = grow(ex->active, ex->active_cap, tiles_total)) != DISO_OK) return rc;
+  // grow the scan state now so that count allocates nothing
+  const int64_t scan_tiles = (seg_total + 1 + SCAN_TILE - 1) / SCAN_TILE;
+  if (scan_tiles > ex->scan_cap) {
+    cudaFree(ex->scan_flag);
+    cudaFree(ex->scan_agg);
+    cudaFree(ex->scan_incl);
+    ex->scan_flag = nullptr;
+    ex->scan_agg = ex->scan_incl = nullptr;
+    ex->scan_cap = 0;
+    const int64_t cap = scan_tiles + scan_tiles / 4 + 64;
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_flag, (size_t)cap * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_agg, (size_t)cap * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc((void**)&ex->scan_incl, (size_t)cap * sizeof(uint64_t)));
+    ex->scan_cap = cap;
+  }
+  CUDA_TRY(cudaMemcpyAsync(ex->bdesc, d, sizeof(BatchGrid<S>) * n, cudaMemcpyHostToDevice, s));
+  int64_t* doffs = (int64_t*)((char*)ex->bbound + sizeof(uint64_t) * (MAX_BATCH + 1));
+  CUDA_TRY(cudaMemcpyAsync(doffs, offs, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return DISO_OK;
+}
+
+template <class S>
+int batch_count(diso_extractor* ex, cudaStream_t s) {
+  const int n = ex->bn;
+  init_stats_kernel<<<1, 256, 0, s>>>(ex->bstats, n);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemsetAsync(ex->stats, 0, sizeof(Stats), s));
+  const int64_t per_block = (CP / TX) * (CR / TY);
+  const int64_t want = std::max<int64_t>(ex->bcount_ctas, (ex->bblocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, ex->bblocks));
+  const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
+  if (ex->method == DISO_MC)
+    batch_count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, n, ex->bblocks, ex->bstats, &ex->bstats->n_active,
+                                                         ex->active);
+  else
+    batch_count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(d, n, ex->bblocks, ex->bstats, &ex->bstats->n_active,
+                                                          ex->active);
+  CUDA_TRY(cudaGetLastError());
+  const int64_t tiles = (ex->bseg_total + 1 + SCAN_TILE - 1) / SCAN_TILE;
+  CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
+  ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(ex->brecord, ex->bseg_total, st, ex->stats);
+  CUDA_TRY(cudaGetLastError());
+  const int64_t* doffs = (const int64_t*)((char*)ex->bbound + sizeof(uint64_t) * (MAX_BATCH + 1));
+  gather_bounds_kernel<<<1, 256, 0, s>>>(ex->brecord, doffs, n, ex->bbound);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+template <class S>
+int batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+               cudaStream_t s) {
+  const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
+  const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
+  if (ex->method == DISO_MC)
+    batch_emit_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, ex->active, &ex->bstats->n_active, (S*)verts, faces, vcap,
+                                                        fcap, normalize, ex->bstats);
+  else
+    batch_emit_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(d, ex->active, &ex->bstats->n_active, (S*)verts, faces,
+                                                         vcap, fcap, normalize, ex->bstats);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+template <class S>
+int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv, cudaStream_t s) {
+  const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
+  const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
+  const size_t smem = backward_dyn_smem<S>();
+  const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  if (ex->method == DISO_MC)
+    batch_backward_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(d, ex->bn, ex->bptiles, (const S*)gv, normalize, 0);
+  else
+    batch_backward_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(d, ex->bn, ex->bptiles, (const S*)gv, normalize, exact);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+int batch_results(diso_extractor* ex, diso_counts* out, int64_t* voff, int64_t* foff, int* overflow,
+                  cudaStream_t s) {
+  const int n = ex->bn;
+  CUDA_TRY(cudaMemcpyAsync(ex->bstats_host, ex->bstats, sizeof(Stats) * n, cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(ex->bbound_host, ex->bbound, sizeof(uint64_t) * (n + 1), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (ex->stats_host->error & 1ull) return fail(DISO_ERR_SCAN, "batch segment scan: look-back wait gave up");
+  const bool mc = ex->method == DISO_MC;
+  for (int i = 0; i < n; ++i) {
+    const uint64_t a = ex->bbound_host[i], b = ex->bbound_host[i + 1];
+    const int64_t va = mc ? Counts::lo(a) : Counts::hi(a), vb = mc ? Counts::lo(b) : Counts::hi(b);
+    const int64_t fa = mc ? Counts::hi(a) : Counts::lo(a), fb = mc ? Counts::hi(b) : Counts::lo(b);
+    const Stats& h = ex->bstats_host[i];
+    out[i].n_verts = vb - va;
+    out[i].n_faces = fb - fa;
+    out[i].sdf_min = key_to_double(h.min_key);
+    out[i].sdf_max = key_to_double(h.max_key);
+    out[i].empty = 0;  // the caller applies the guard with its own isovalue (see diso_batch_results)
+    out[i].pad_ = 0;
+    out[i].n_active_tiles = 0;
+    if (voff) voff[i] = va;
+    if (foff) foff[i] = fa;
+  }
+  if (overflow) *overflow = (ex->bstats_host[0].error & 2ull) ? 1 : 0;
+  return DISO_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -349,6 +567,65 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                                                  grad_verts, grad_sdf, deform ? grad_deform : nullptr, s)
                                : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
                                                   flags, grad_verts, grad_sdf, deform ? grad_deform : nullptr, s);
+}
+
+int64_t diso_batch_record_slots(const diso_grid* grids, int ngrids) {
+  if (!grids || ngrids < 1 || ngrids > MAX_BATCH) return 0;
+  return batch_record_slots(grids, ngrids, nullptr, nullptr);
+}
+
+int diso_batch_prepare(diso_extractor* ex, const diso_grid* grids, int ngrids, uint64_t* record, void* stream) {
+  if (!ex || !grids || !record) return fail(DISO_ERR_ARG, "null extractor, grids or record");
+  if (ngrids < 1 || ngrids > MAX_BATCH) return fail(DISO_ERR_ARG, "batch of %d grids (1..%d)", ngrids, MAX_BATCH);
+  int64_t tiles = 0;
+  for (int i = 0; i < ngrids; ++i) {
+    int rc = check_common(ex, grids[i].sdf, grids[i].nx, grids[i].ny, grids[i].nz);
+    if (rc) return rc;
+    Geom g;
+    g.init(grids[i].nx, grids[i].ny, grids[i].nz);
+    if (g.ntiles() >= (1ll << BATCH_TILE_BITS)) return fail(DISO_ERR_ARG, "grid %d too large for a batch", i);
+    tiles += g.ntiles();
+  }
+  int64_t segs = 0;
+  batch_record_slots(grids, ngrids, &segs, &tiles);
+  if (3.0 * (double)segs * TZ >= 2147483647.0) return fail(DISO_ERR_ARG, "batch too large for 32-bit counts");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? batch_prepare<float>(ex, grids, ngrids, record, s)
+                               : batch_prepare<double>(ex, grids, ngrids, record, s);
+}
+
+int diso_batch_count(diso_extractor* ex, void* stream) {
+  if (!ex || ex->bn < 1) return fail(DISO_ERR_ARG, "no prepared batch");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? batch_count<float>(ex, s) : batch_count<double>(ex, s);
+}
+
+int diso_batch_results(diso_extractor* ex, diso_counts* per_grid, int64_t* vert_offset, int64_t* face_offset,
+                       int* overflow, void* stream) {
+  if (!ex || ex->bn < 1 || !per_grid) return fail(DISO_ERR_ARG, "no prepared batch or null output");
+  return batch_results(ex, per_grid, vert_offset, face_offset, overflow, (cudaStream_t)stream);
+}
+
+int diso_batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                    void* stream) {
+  if (!ex || ex->bn < 1) return fail(DISO_ERR_ARG, "no prepared batch");
+  if ((!verts && vcap) || (!faces && fcap) || vcap < 0 || fcap < 0) return fail(DISO_ERR_ARG, "bad output buffers");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? batch_emit<float>(ex, normalize, verts, vcap, faces, fcap, s)
+                               : batch_emit<double>(ex, normalize, verts, vcap, faces, fcap, s);
+}
+
+int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, void* stream) {
+  if (!ex || ex->bn < 1) return fail(DISO_ERR_ARG, "no prepared batch");
+  if (!grad_verts) return fail(DISO_ERR_ARG, "null grad_verts");
+  for (int i = 0; i < ex->bn; ++i) {
+    const bool missing = ex->dtype == DISO_F32 ? ((const BatchGrid<float>*)ex->bdesc_host)[i].gsdf == nullptr
+                                               : ((const BatchGrid<double>*)ex->bdesc_host)[i].gsdf == nullptr;
+    if (missing) return fail(DISO_ERR_ARG, "grid %d of the batch has no grad_sdf", i);
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? batch_backward<float>(ex, normalize, flags, grad_verts, s)
+                               : batch_backward<double>(ex, normalize, flags, grad_verts, s);
 }
 
 const char* diso_last_error(void) { return g_err; }

@@ -221,109 +221,175 @@ __host__ __device__ inline int64_t count_blocks(const Geom& g) {
 }
 
 template <class S, int METHOD>
+struct CountShared {
+  // MC needs the rows of the cells' corners, DMC also those of the face neighbours
+  // used by the ambiguity test
+  static constexpr int H = METHOD == DMC ? 1 : 0;
+  static constexpr int WX = CP + 1 + 2 * H, WY = CR + 1 + 2 * H;
+  uint64_t m[WX][WY];
+  uint32_t act[CP];
+  int list[COUNT_LIST];
+  int nlist, base;
+};
+
+// lower the grid's min / max keys (one warp's values); reads first so that most
+// warps need no atomic
+template <class S>
+__device__ __forceinline__ void publish_minmax(Stats* stats, S mn, S mx, bool seen) {
+  const int lane = threadIdx.x & 31;
+  const unsigned have = __ballot_sync(0xffffffffu, seen);
+  if (!have) return;
+  const int src = __ffs(have) - 1;
+  const S m0 = __shfl_sync(0xffffffffu, mn, src), x0 = __shfl_sync(0xffffffffu, mx, src);
+  if (!seen) {
+    mn = m0;
+    mx = x0;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const S p = __shfl_xor_sync(0xffffffffu, mn, o), q = __shfl_xor_sync(0xffffffffu, mx, o);
+    mn = p < mn ? p : mn;
+    mx = q > mx ? q : mx;
+  }
+  if (lane == 0) {
+    const unsigned long long kmn = ord_key((double)mn), kmx = ord_key((double)mx);
+    if (kmn < *(volatile unsigned long long*)&stats->min_key) atomicMin(&stats->min_key, kmn);
+    if (kmx > *(volatile unsigned long long*)&stats->max_key) atomicMax(&stats->max_key, kmx);
+  }
+}
+
+// One count block: the per-segment counts, the activity bytes of the block's
+// tiles, the grid's min / max; active tiles are appended (as tile | tag) to sh.list.
+template <class S, int METHOD>
+__device__ __forceinline__ void count_block(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
+                                            Stats* stats, int blk, int tag) {
+  constexpr int H = CountShared<S, METHOD>::H, WX = CountShared<S, METHOD>::WX, WY = CountShared<S, METHOD>::WY;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nby = (g.c[1] + CR - 1) / CR;
+  const int tz = blk % g.nzc;
+  const int r = blk / g.nzc;
+  const int X0 = (r / nby) * CP, Y0 = (r % nby) * CR, Z0 = tz * TZ;
+  const int WX0 = X0 - H, WY0 = Y0 - H;
+  S mn = f.pad, mx = f.pad;
+  bool seen = false;
+  load_masks<S, WX, WY, true>(sh.m, f, WX0, WY0, Z0, mn, mx, seen);
+  __syncthreads();
+  publish_minmax<S>(stats, mn, mx, seen);
+  const int X = X0 + warp, Y = Y0 + lane;
+  uint32_t nv = 0, nf = 0;
+  if (X < g.c[0] && Y < g.c[1]) {
+    const int x = warp + H, y = lane + H;
+    const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
+    const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
+    nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
+    uint32_t nt = rw.nt;
+    while (nt) {
+      const int j = __ffs(nt) - 1;
+      nt &= nt - 1;
+      const int code = code8(a, b, c, d, j + 1);
+      if (METHOD == MC)
+        nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+      else
+        nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, WX0, WY0, Z0, code, X, Y, Z0 + j, g)));
+    }
+    seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
+  }
+  // a cell can emit faces / patches without owning a crossing edge (its
+  // crossings may all sit on edges owned by its +1 neighbours)
+  const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
+  if (lane == 0) sh.act[warp] = busy;
+  __syncthreads();
+  if (threadIdx.x < (CP / TX) * (CR / TY)) {
+    const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
+    const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
+    if (tx < g.tiles_x() && ty < g.tiles_y()) {
+      uint32_t any = 0;
+#pragma unroll
+      for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
+      const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
+      tile_flag[tile] = any ? 1 : 0;
+      if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
+    }
+  }
+}
+
+// append the CTA's active tiles to the global list
+template <class S, int METHOD>
+__device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned long long* n_active,
+                                            int* __restrict__ active) {
+  __syncthreads();
+  if (threadIdx.x == 0) sh.base = sh.nlist ? (int)atomicAdd(n_active, (unsigned long long)sh.nlist) : 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < sh.nlist; i += blockDim.x) active[sh.base + i] = sh.list[i];
+}
+
+// Persistent: CTA b handles blocks b, b + gridDim.x, ...; the active tiles of a CTA
+// are kept in shared memory and published with one atomic at the end (per-tile
+// atomics on one address serialise in L2).  At most COUNT_LIST tiles per CTA:
+// launch at least ntiles / COUNT_LIST CTAs.
+template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                             uint8_t* __restrict__ tile_flag, Stats* stats,
                                                             int* __restrict__ active) {
-  // MC needs the rows of the cells' corners, DMC also those of the face neighbours
-  // used by the ambiguity test
-  constexpr int H = METHOD == DMC ? 1 : 0;
-  constexpr int WX = CP + 1 + 2 * H, WY = CR + 1 + 2 * H;
-  __shared__ uint64_t m[WX][WY];
-  __shared__ uint32_t act[CP];
-  __shared__ S red_min[CP], red_max[CP];
-  __shared__ uint32_t red_any[CP];
-  __shared__ int list[COUNT_LIST];
-  __shared__ int nlist, base;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) nlist = 0;
-  S mn = f.pad, mx = f.pad;
-  bool seen = false;
-  const int nby = (g.c[1] + CR - 1) / CR;
-  const int64_t nblocks = count_blocks(g);
+  __shared__ CountShared<S, METHOD> sh;
+  if (threadIdx.x == 0) sh.nlist = 0;
+  const int nblocks = (int)count_blocks(g);
 #pragma unroll 1
-  for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
-    const int tz = (int)(blk % g.nzc);
-    const int r = (int)(blk / g.nzc);
-    const int X0 = (r / nby) * CP, Y0 = (r % nby) * CR, Z0 = tz * TZ;
-    const int WX0 = X0 - H, WY0 = Y0 - H;
-    load_masks<S, WX, WY, true>(m, f, WX0, WY0, Z0, mn, mx, seen);
-    __syncthreads();
-    const int X = X0 + warp, Y = Y0 + lane;
-    uint32_t nv = 0, nf = 0;
-    if (X < g.c[0] && Y < g.c[1]) {
-      const int x = warp + H, y = lane + H;
-      const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
-      const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
-      nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
-      uint32_t nt = rw.nt;
-      while (nt) {
-        const int j = __ffs(nt) - 1;
-        nt &= nt - 1;
-        const int code = code8(a, b, c, d, j + 1);
-        if (METHOD == MC)
-          nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-        else
-          nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code, X, Y, Z0 + j, g)));
-      }
-      seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-    }
-    // a cell can emit faces / patches without owning a crossing edge (its
-    // crossings may all sit on edges owned by its +1 neighbours)
-    const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
-    if (lane == 0) act[warp] = busy;
-    __syncthreads();
-    if (threadIdx.x < (CP / TX) * (CR / TY)) {
-      const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
-      const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
-      if (tx < g.tiles_x() && ty < g.tiles_y()) {
-        uint32_t any = 0;
-#pragma unroll
-        for (int p = 0; p < TX; ++p) any |= (act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
-        const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
-        tile_flag[tile] = any ? 1 : 0;
-        if (any) list[atomicAdd(&nlist, 1)] = (int)tile;
-      }
-    }
+  for (int blk = blockIdx.x; blk < nblocks; blk += gridDim.x) count_block<S, METHOD>(sh, f, g, seg, tile_flag, stats, blk, 0);
+  count_flush<S, METHOD>(sh, &stats->n_active, active);
+}
+
+// ------------------------------------------------------------------ batches
+
+// One grid of a batch: its field, geometry, its slices of the concatenated
+// per-call record (segments and tile bytes), its first flattened count block,
+// active-tile and point tile, and its gradient outputs.
+template <class S>
+struct BatchGrid {
+  Field<S> f;
+  Geom g;
+  uint64_t* seg;        // this grid's first segment in the concatenated, globally scanned array
+  uint64_t* seg_end;    // the next grid's first segment (or the total slot)
+  uint8_t* tile_flag;   // this grid's tile bytes
+  int64_t cblk0;        // first count block of the grid in the flattened queue
+  int64_t ptile0;       // first point tile (backward)
+  S* gsdf;              // backward outputs
+  S* gdef;
+};
+constexpr int MAX_BATCH = 256;  // grids per batch (the grid index is stored in 8 bits of a tile id)
+constexpr int BATCH_TILE_BITS = 24;
+
+// index of the grid whose range [start[i], start[i+1]) holds item b
+__device__ __forceinline__ int batch_find(const int64_t* start, int n, int64_t b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid - 1;
   }
-  // min / max of the caller's grid (the guard of diso/__init__.py:49)
-  const unsigned have = __ballot_sync(0xffffffffu, seen);
-  if (have) {
-    const int src = __ffs(have) - 1;
-    const S m0 = __shfl_sync(0xffffffffu, mn, src), x0 = __shfl_sync(0xffffffffu, mx, src);
-    if (!seen) {
-      mn = m0;
-      mx = x0;
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const S p = __shfl_xor_sync(0xffffffffu, mn, o), q = __shfl_xor_sync(0xffffffffu, mx, o);
-      mn = p < mn ? p : mn;
-      mx = q > mx ? q : mx;
-    }
-  }
-  if (lane == 0) {
-    red_min[warp] = mn;
-    red_max[warp] = mx;
-    red_any[warp] = have ? 1u : 0u;
-  }
+  return lo;
+}
+
+// every grid of a batch in one persistent launch over the flattened queue of count
+// blocks; per-grid status words in stats[grid]
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                                  int64_t nblocks, Stats* stats,
+                                                                  unsigned long long* n_active,
+                                                                  int* __restrict__ active) {
+  __shared__ CountShared<S, METHOD> sh;
+  __shared__ int64_t start[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].cblk0;
+  if (threadIdx.x == 0) sh.nlist = 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    bool got = false;
-    for (int w = 0; w < CP; ++w) {
-      if (red_any[w]) {
-        mn = got ? (red_min[w] < mn ? red_min[w] : mn) : red_min[w];
-        mx = got ? (red_max[w] > mx ? red_max[w] : mx) : red_max[w];
-        got = true;
-      }
-    }
-    if (got) {
-      atomicMin(&stats->min_key, ord_key((double)mn));
-      atomicMax(&stats->max_key, ord_key((double)mx));
-    }
-    base = nlist ? (int)atomicAdd(&stats->n_active, (unsigned long long)nlist) : 0;
+#pragma unroll 1
+  for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    const int i = batch_find(start, ngrids, b);
+    const BatchGrid<S>& G = grids[i];
+    count_block<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, stats + i, (int)(b - start[i]), i << BATCH_TILE_BITS);
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nlist; i += blockDim.x) active[base + i] = list[i];
+  count_flush<S, METHOD>(sh, n_active, active);
 }
 
 // ------------------------------------------------------------------ work lists
@@ -375,10 +441,12 @@ __device__ __forceinline__ void put_items(uint16_t* list, uint32_t off, uint64_t
 
 constexpr int EMIT_ITEMS = 3 * TX * TY * TZ;  // every own edge crossing
 
+// One active tile: its vertices and triangles.  Vertex ids written into faces are
+// reduced by vsub (the grid's first vertex, for batches whose vertices are concatenated).
 template <class S>
-__global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                           const int* __restrict__ active, S* __restrict__ verts,
-                                                           int64_t* __restrict__ faces, int normalize) {
+__device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+                                             int tile, S* __restrict__ verts, int64_t* __restrict__ faces,
+                                             int normalize, int64_t vsub) {
   constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint64_t m[WX][WY];
@@ -392,7 +460,7 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
   __shared__ uint32_t nvi, nci;
   int X0, Y0, Z0, tz;
-  tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
+  tile_coords(tile, g, X0, Y0, Z0, tz);
   S dmn, dmx;
   bool dseen = false;
   load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
@@ -481,18 +549,28 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
       for (int k = 0; k < 3; ++k) {
         const int e = (int)((w >> (4 + 4 * (3 * t + k))) & 15);
         const int ge = g_edge[e];
-        faces[3 * (f0 + t) + k] = vid(x + (ge & 1), y + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3);
+        faces[3 * (f0 + t) + k] = vid(x + (ge & 1), y + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3) - vsub;
       }
     }
   }
+  __syncthreads();  // the shared arrays are reused by the CTA's next tile
+}
+
+template <class S>
+__global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                           const int* __restrict__ active, S* __restrict__ verts,
+                                                           int64_t* __restrict__ faces, int normalize) {
+  mc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, faces, normalize, 0);
 }
 
 // ------------------------------------------------------------------ DMC emit
 
+// One active tile: its dual vertices and quads; patch ids written into quads are
+// reduced by vsub (as in mc_emit_tile).
 template <class S>
-__global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                            const int* __restrict__ active, S* __restrict__ verts,
-                                                            int64_t* __restrict__ quads, int normalize) {
+__device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+                                              int tile, S* __restrict__ verts, int64_t* __restrict__ quads,
+                                              int normalize, int64_t vsub) {
   constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
   __shared__ uint64_t m[WX][WY];
@@ -506,7 +584,7 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
   __shared__ uint32_t nqi, nci;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
-  tile_coords(active[blockIdx.x], g, X0, Y0, Z0, tz);
+  tile_coords(tile, g, X0, Y0, Z0, tz);
   const int WX0 = X0 - 1, WY0 = Y0 - 1;
   S dmn, dmx;
   bool dseen = false;
@@ -584,7 +662,7 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
     for (int k = 0; k < 4; ++k) {
       const int q = g_dmc_quad[4 * type + k];
       const int nx = x + (q & 3) - 1, ny = y + ((q >> 2) & 3) - 1, nz = j + 1 + ((q >> 4) & 3) - 1;
-      quads[4 * qid + k] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8);
+      quads[4 * qid + k] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8) - vsub;
     }
   }
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
@@ -625,6 +703,14 @@ __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, 
         store_vertex<S>(verts, p0 + q, v, g, normalize);
       }
   }
+  __syncthreads();  // the shared arrays are reused by the CTA's next tile
+}
+
+template <class S>
+__global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                            const int* __restrict__ active, S* __restrict__ verts,
+                                                            int64_t* __restrict__ quads, int normalize) {
+  dmc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, quads, normalize, 0);
 }
 
 // ------------------------------------------------------------------ backward
@@ -750,10 +836,10 @@ constexpr size_t backward_dyn_smem() {
 // gradient (the true derivative).  Replaces the forward re-run, the zero fills and
 // the F.pad backward of diso/__init__.py:30-44, 84-98.
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                            const uint8_t* __restrict__ tile_flag,
-                                                            const S* __restrict__ gv, int normalize, int exact,
-                                                            S* __restrict__ gsdf, S* __restrict__ gdef) {
+__device__ __forceinline__ void backward_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+                                              const uint8_t* __restrict__ tile_flag, int64_t ptile,
+                                              const S* __restrict__ gv, int normalize, int exact,
+                                              S* __restrict__ gsdf, S* __restrict__ gdef) {
   constexpr int H = METHOD == DMC ? 1 : 0;  // DMC: one more mask row each side for the ambiguity test
   constexpr int WX = TX + 2 + H, WY = TY + 2 + H;  // point rows [X0-H, X0+TX+1] x [Y0-H, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;          // cell rows [X0, X0+TX] x [Y0, Y0+TY]; mask row x + H
@@ -772,7 +858,7 @@ __global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, 
   S* slot = reinterpret_cast<S*>(dyn_smem);  // [2][NP][4]: end 0 / end 1 adjoints of the current axis
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
-  ptile_coords(blockIdx.x, g, X0, Y0, Z0);
+  ptile_coords(ptile, g, X0, Y0, Z0);
   if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
     zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
     return;
@@ -947,6 +1033,67 @@ __global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, 
       gdef[3 * i + 1] = acc[ix][2];
       gdef[3 * i + 2] = acc[ix][3];
     }
+  }
+  __syncthreads();  // the shared arrays are reused by the CTA's next tile
+}
+
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                            const uint8_t* __restrict__ tile_flag,
+                                                            const S* __restrict__ gv, int normalize, int exact,
+                                                            S* __restrict__ gsdf, S* __restrict__ gdef) {
+  backward_tile<S, METHOD>(f, g, seg, tile_flag, blockIdx.x, gv, normalize, exact, gsdf, gdef);
+}
+
+// ------------------------------------------------------------------ batch emit / backward
+
+// Emit every active tile of a batch (persistent).  Outputs are concatenated in grid
+// order; faces hold grid-local vertex ids.  When a grid's outputs would pass the
+// capacities (vcap vertices, fcap faces) the grid is skipped and bit 1 of
+// stats[0].error is set; the host then retries with larger buffers.
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS) batch_emit_kernel(const BatchGrid<S>* __restrict__ grids,
+                                                              const int* __restrict__ active,
+                                                              const unsigned long long* __restrict__ n_active,
+                                                              S* __restrict__ verts, int64_t* __restrict__ faces,
+                                                              int64_t vcap, int64_t fcap, int normalize,
+                                                              Stats* stats) {
+  const int64_t n = (int64_t)*n_active;
+#pragma unroll 1
+  for (int64_t t = blockIdx.x; t < n; t += gridDim.x) {
+    const int code = active[t];
+    const int i = (int)((unsigned)code >> BATCH_TILE_BITS), tile = code & ((1 << BATCH_TILE_BITS) - 1);
+    const BatchGrid<S>& G = grids[i];
+    const uint64_t b0 = *G.seg, b1 = *G.seg_end;
+    // MC: low half = vertices, high half = triangles; DMC: low = quads, high = patches
+    const int64_t v0 = METHOD == MC ? Counts::lo(b0) : Counts::hi(b0);
+    const int64_t v1 = METHOD == MC ? Counts::lo(b1) : Counts::hi(b1);
+    const int64_t f1 = METHOD == MC ? Counts::hi(b1) : Counts::lo(b1);
+    if (v1 > vcap || f1 > fcap) {
+      if (threadIdx.x == 0) atomicOr(&stats->error, 2ull);
+      continue;
+    }
+    if (METHOD == MC)
+      mc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0);
+    else
+      dmc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0);
+  }
+}
+
+// dL/dsdf and dL/ddeform of every grid of a batch (persistent over the flattened
+// point tiles); dL/dverts is the concatenated [total vertices, 3] array.
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS) batch_backward_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                                  int64_t ntiles, const S* __restrict__ gv,
+                                                                  int normalize, int exact) {
+  __shared__ int64_t start[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].ptile0;
+  __syncthreads();
+#pragma unroll 1
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i = batch_find(start, ngrids, t);
+    const BatchGrid<S>& G = grids[i];
+    backward_tile<S, METHOD>(G.f, G.g, G.seg, G.tile_flag, t - start[i], gv, normalize, exact, G.gsdf, G.gdef);
   }
 }
 

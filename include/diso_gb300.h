@@ -133,6 +133,51 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
 int diso_forward_count_static(int method, int dtype, const void* sdf, int nx, int ny, int nz, double isovalue,
                               double padval, uint64_t* seg, void* stream, diso_counts* out);
 
+/* ---------------------------------------------------------------- batches
+ *
+ * Many grids of uneven size in one launch per phase (count, scan, emit,
+ * backward) over a flattened queue of their tiles; the reference has no batched
+ * call (its README runs a Python loop over one extractor, README.md:61-70), so
+ * these replace that loop.  diso_batch_prepare uploads the grid descriptors and
+ * grows the scratch; after it, diso_batch_count / _emit / _backward allocate
+ * nothing and do not synchronise with the host, so the sequence can be captured
+ * in a CUDA graph and replayed while the grids' contents change in place. */
+typedef struct {
+  const void* sdf;    /* [nx][ny][nz] */
+  const void* deform; /* [nx][ny][nz][3] or NULL */
+  void* grad_sdf;     /* backward output [nx][ny][nz] (needed by diso_batch_backward) */
+  void* grad_deform;  /* backward output [nx][ny][nz][3] when deform is given */
+  int nx, ny, nz;
+  int pad_;
+  double isovalue, padval; /* per grid, as in diso_forward_count */
+} diso_grid;
+
+/* uint64 slots of the batch record (segments of every grid, their total, tile bytes); 0 on bad input */
+int64_t diso_batch_record_slots(const diso_grid* grids, int ngrids);
+
+/* Lay out the record, upload the descriptors (1 <= ngrids <= 256), grow the scratch.  Synchronises. */
+int diso_batch_prepare(diso_extractor* ex, const diso_grid* grids, int ngrids, uint64_t* record, void* stream);
+
+/* Count and scan every grid of the prepared batch: one launch each, no host synchronisation. */
+int diso_batch_count(diso_extractor* ex, void* stream);
+
+/* Results of the last count (and emit): per-grid sizes, the grids' first vertex / face in the
+ * concatenated outputs, and *overflow = 1 when an emit skipped grids past its capacities.
+ * sdf_min / sdf_max are filled; `empty` is left 0: the caller applies the guard of
+ * diso/__init__.py:49, 103 with each grid's isovalue.  Synchronises the stream. */
+int diso_batch_results(diso_extractor* ex, diso_counts* per_grid, int64_t* vert_offset, int64_t* face_offset,
+                       int* overflow, void* stream);
+
+/* Emit every grid into concatenated verts [vcap][3] and faces [fcap][3] (MC) or [fcap][4]
+ * (DMC quads); faces hold grid-local vertex ids.  A grid whose outputs would pass the
+ * capacities is skipped and reported through diso_batch_results. */
+int diso_batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                    void* stream);
+
+/* Backward of every grid from the concatenated dL/dverts; writes each grid's grad_sdf and
+ * grad_deform (flags as for diso_backward). */
+int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* diso_last_error(void);
 
