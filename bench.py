@@ -68,6 +68,145 @@ def loss_weights(nv, device, dtype):
     return torch.randn(nv, 3, device=device, dtype=dtype, generator=g)
 
 
+# ----------------------------------------------------------------------------- uneven grids
+def object_field(shape, kind, rng, device, dtype=torch.float32, noise=0.02):
+    """Sphere (radius U(0.3, 0.7)) or rounded box (half-extent U(0.3, 0.6), radius 0.1)
+    on linspace(-1, 1) axes, plus N(0, noise) noise; `rng` is a numpy Generator."""
+    axes = [torch.linspace(-1, 1, n, device=device, dtype=dtype) for n in shape]
+    X, Y, Z = axes[0].view(-1, 1, 1), axes[1].view(1, -1, 1), axes[2].view(1, 1, -1)
+    if kind == "sphere":
+        s = torch.sqrt(X * X + Y * Y + Z * Z) - float(rng.uniform(0.3, 0.7))
+    else:
+        h = float(rng.uniform(0.3, 0.6))
+        q = torch.stack(torch.broadcast_tensors((X.abs() - h).clamp_min(0), (Y.abs() - h).clamp_min(0),
+                                                (Z.abs() - h).clamp_min(0)), -1)
+        s = q.norm(dim=-1) - 0.1
+    g = torch.Generator(device=device).manual_seed(int(rng.integers(1 << 31)))
+    return (s + noise * torch.randn(shape, device=device, dtype=dtype, generator=g)).contiguous()
+
+
+def uneven_batch(ngrids=64, seed=1, device="cuda", dtype=torch.float32, deform=0.3):
+    """The batched workload: N log-uniform in [32, 256], sphere or rounded box + noise, deform U(-0.3, 0.3)."""
+    rng = np.random.default_rng(seed)
+    sdfs, defs = [], []
+    for _ in range(ngrids):
+        n = int(round(float(np.exp(rng.uniform(np.log(32), np.log(256))))))
+        kind = "sphere" if rng.random() < 0.5 else "box"
+        sdfs.append(object_field((n, n, n), kind, rng, device, dtype))
+        g = torch.Generator(device=device).manual_seed(int(rng.integers(1 << 31)))
+        defs.append((torch.rand((n, n, n, 3), device=device, dtype=dtype, generator=g) * 2 * deform - deform).contiguous())
+    return sdfs, defs
+
+
+def request_inputs(seed, shape, kind, deform=0.3, dtype=torch.float32):
+    """Device inputs of one served request, rebuilt identically from its seed:
+    (sdf, deform, dL/dverts generator)."""
+
+    def make(device):
+        rng = np.random.default_rng(seed)
+        if kind == "random":
+            g = torch.Generator(device=device).manual_seed(seed)
+            sdf = torch.rand(shape, device=device, dtype=dtype, generator=g) * 2 - 1
+        else:
+            sdf = object_field(shape, kind, rng, device, dtype)
+        g = torch.Generator(device=device).manual_seed(seed + 1)
+        dfm = (torch.rand(shape + (3,), device=device, dtype=dtype, generator=g) * 2 * deform - deform).contiguous()
+
+        def grad(nv):
+            gg = torch.Generator(device=device).manual_seed(seed + 2)
+            return torch.randn((nv, 3), device=device, dtype=dtype, generator=gg)
+
+        return sdf, dfm, grad
+
+    return make
+
+
+def served_trace(nreq=2000, rate=2000.0, seed=3):
+    """Poisson arrivals; N in {64,128,256,384} at {.4,.3,.2,.1}; MC / DMC 50/50;
+    U(-1,1) random fields 30%, sphere / rounded box 70%; deform U(-0.3, 0.3)."""
+    from diso_gb300.serve import Request, estimate_bytes
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(nreq):
+        t += float(rng.exponential(1.0 / rate))
+        n = int(rng.choice([64, 128, 256, 384], p=[0.4, 0.3, 0.2, 0.1]))
+        method = int(rng.integers(2))
+        u = rng.random()
+        kind = "random" if u < 0.3 else ("sphere" if u < 0.65 else "box")
+        shape = (n, n, n)
+        out.append(Request(rid=i, method=method, shape=shape, arrival=t,
+                           make_inputs=request_inputs(int(rng.integers(1 << 30)), shape, kind),
+                           est_bytes=estimate_bytes(shape, dense=kind == "random")))
+    return out
+
+
+def run_batched(device, method, steps=10, warmup=3, ngrids=64):
+    """grids/s of a plain per-grid loop against one batched launch per phase (eager and
+    CUDA-graph replay), forward + backward, on the uneven batch."""
+    from diso_gb300 import BatchPlan, DiffDMC, DiffMC
+
+    sdfs, defs = uneven_batch(ngrids, device=device)
+    ext = DiffMC(torch.float32) if method == 0 else DiffDMC(torch.float32)
+    ins = [(s.clone().requires_grad_(True), d.clone().requires_grad_(True)) for s, d in zip(sdfs, defs)]
+    kw = {} if method == 0 else {"return_quads": True}
+    ws = [loss_weights(ext(s, d, **kw)[0].shape[0], device, torch.float32) for s, d in ins]
+
+    def loop():
+        for (s, d), w in zip(ins, ws):
+            s.grad = None
+            d.grad = None
+            v, _ = ext(s, d, **kw)
+            torch.autograd.backward(v, w)
+
+    def timed(fn, k):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(k):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    ms_loop = timed(loop, steps)
+    plan = BatchPlan(method, torch.float32, [tuple(s.shape) for s in sdfs], deform=True)
+    for i, (s, d) in enumerate(zip(sdfs, defs)):
+        plan.sdf[i].copy_(s)
+        plan.deform[i].copy_(d)
+    nv, _ = plan.size_outputs()
+    plan.grad_verts[:nv].copy_(torch.cat(ws))
+    ms_eager = timed(plan.run, steps)
+    plan.capture()
+    ms_graph = timed(plan.replay, steps)
+    plan.results()
+    return {"grids": ngrids, "loop_grids_s": ngrids / (ms_loop * 1e-3), "batched_grids_s": ngrids / (ms_eager * 1e-3),
+            "graph_grids_s": ngrids / (ms_graph * 1e-3), "speedup_vs_loop": ms_loop / ms_graph,
+            "ms_loop": ms_loop, "ms_graph": ms_graph}
+
+
+def run_served(device, nreq=2000, rate=2000.0):
+    """p50 / p99 latency and grids/s of the continuous-batching server against the
+    plain per-request call on the same arrival trace."""
+    from diso_gb300.serve import Server, serve_plain, summarize
+
+    srv = Server(device, hbm_budget=60e9, max_batch=32, workers=2)
+    srv.serve(served_trace(64, rate, seed=11), realtime=False)  # warm-up
+    trace = served_trace(nreq, rate)
+    srv.serve(trace)
+    peak = srv.peak
+    srv.close()
+    ours = summarize(trace)
+    plain_trace = served_trace(nreq, rate)
+    serve_plain(plain_trace, device)
+    plain = summarize(plain_trace)
+    return {"requests": nreq, "rate_per_s": rate, "server": ours, "plain_per_request": plain,
+            "grids_s_speedup": ours["grids_per_s"] / plain["grids_per_s"], "peak_budget_gb": peak / 1e9}
+
+
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons while running."""
@@ -348,6 +487,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
+    ap.add_argument("--requests", type=int, default=2000, help="served-trace length (20000 for the full trace)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -378,6 +519,13 @@ def main():
         torch.distributed.init_process_group("nccl")
     device = torch.device("cuda", torch.cuda.current_device())
     res = run_ours(args, rank, world, device)
+    if rank == 0 and world == 1 and not args.no_batched:
+        for name, fn in (("batched_mc", lambda: run_batched(device, 0)), ("batched_dmc", lambda: run_batched(device, 1)),
+                         ("served", lambda: run_served(device, args.requests))):
+            try:
+                res[name] = fn()
+            except Exception as e:  # report, but keep the headline line
+                res[name] = {"error": repr(e)[:300]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         value, planes, cores, sec = run_cpu(args, 1, 0, args.cpu_budget)
         res["cpu_baseline"] = {"value": value, "unit": "grids/s", "cores": cores, "kind": "port",
