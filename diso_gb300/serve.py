@@ -199,8 +199,11 @@ class Server:
         waiting = deque()
         total = len(trace)
         while True:
+            # cleared before looking, so a completion signalled while we look is not lost
+            self.poke.clear()
             now = self.now()
             # admission: arrival order, while the budget allows
+            blocked = False
             while pending and (pending[0].arrival <= now or not realtime):
                 r = pending[0]
                 with self.lock:
@@ -209,11 +212,12 @@ class Server:
                         self.in_use += r.est_bytes
                         self.peak = max(self.peak, self.in_use)
                 if not fits:
+                    blocked = True
                     break
                 pending.popleft()
                 r.admitted = now
                 waiting.append(r)
-            # dispatch: the oldest waiting request's method, up to max_batch of that method
+            # dispatch: the oldest waiting request's kind, up to max_batch of that kind
             for w in self.workers:
                 if not waiting:
                     break
@@ -232,9 +236,13 @@ class Server:
                 finished = self.completed == total
             if finished:
                 break
-            nxt = pending[0].arrival - self.now() if pending else 0.01
-            self.poke.wait(max(0.0, min(0.002, nxt)))
-            self.poke.clear()
+            # sleep until the next arrival, or until a worker finishes (which frees memory
+            # and a worker); never spin, the workers need the interpreter
+            if pending and not blocked and realtime:
+                timeout = max(0.0, pending[0].arrival - self.now())
+            else:
+                timeout = 0.05
+            self.poke.wait(timeout)
         return trace
 
 
