@@ -47,13 +47,14 @@ EXPORTS = {
     "diso_forward_emit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-                                         ctypes.c_void_p]),
+                                         ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_edge_record_slots": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64]),
     "diso_split_quads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "diso_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
-                                     ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
-                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                     ctypes.c_void_p]),
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]),
     "diso_forward_count_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
@@ -142,9 +143,15 @@ class Extractor:
                                        stream_of(sdf.device), ctypes.byref(c)), "forward count")
         return c
 
-    def emit(self, sdf, deform, iso, pad, seg, normalize, verts, faces):
+    def record_slots(self, counts) -> int:
+        """int64 slots of the edge record of a forward with these counts."""
+        return int(lib().diso_edge_record_slots(self.method, dtype_tag(self.dtype), int(counts.n_verts),
+                                                int(counts.n_faces)))
+
+    def emit(self, sdf, deform, iso, pad, seg, normalize, verts, faces, record=None):
         check(lib().diso_forward_emit(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),
-                                      int(bool(normalize)), ptr(verts), ptr(faces), stream_of(sdf.device)),
+                                      int(bool(normalize)), ptr(verts), ptr(faces), ptr(record),
+                                      stream_of(sdf.device)),
               "forward emit")
 
     def split(self, verts, quads, tris) -> int:
@@ -153,7 +160,8 @@ class Extractor:
                                      stream_of(verts.device)), "quad split")
         return int(n.value)
 
-    def backward(self, sdf, deform, iso, pad, seg, normalize, grad_verts, grad_sdf, grad_deform, exact=False):
-        check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),
+    def backward(self, sdf, deform, iso, pad, seg, record, normalize, grad_verts, grad_sdf, grad_deform,
+                 exact=False):
+        check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg), ptr(record),
                                   int(bool(normalize)), GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_sdf),
                                   ptr(grad_deform), stream_of(sdf.device)), "backward")

@@ -48,9 +48,9 @@ _BATCH_EXPORTS = {
                                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
                                           ctypes.c_void_p]),
     "diso_batch_emit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
-                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_batch_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
-                                           ctypes.c_void_p]),
+                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
 }
 N.EXPORTS.update(_BATCH_EXPORTS)
 
@@ -110,13 +110,20 @@ class _Batch:
                                           N.stream_of(device)), "batch results")
         return r
 
-    def emit(self, normalize, verts, faces, device):
-        N.check(_lib().diso_batch_emit(self.ex._h, int(bool(normalize)), N.ptr(verts), verts.shape[0],
-                                       N.ptr(faces), faces.shape[0], N.stream_of(device)), "batch emit")
+    def edge_record(self, vcap, fcap, device):
+        """A batch edge record for outputs of these capacities (int64, at least one slot)."""
+        n = int(N.lib().diso_edge_record_slots(self.method, N.dtype_tag(self.dtype), int(vcap), int(fcap)))
+        return torch.empty(max(1, n), dtype=torch.int64, device=device)
 
-    def backward(self, normalize, exact, gv, device):
+    def emit(self, normalize, verts, faces, device, record=None):
+        N.check(_lib().diso_batch_emit(self.ex._h, int(bool(normalize)), N.ptr(verts), verts.shape[0],
+                                       N.ptr(faces), faces.shape[0], N.ptr(record), N.stream_of(device)),
+                "batch emit")
+
+    def backward(self, normalize, exact, gv, record, vcap, fcap, device):
         N.check(_lib().diso_batch_backward(self.ex._h, int(bool(normalize)), N.GRAD_EXACT if exact else 0,
-                                           N.ptr(gv), N.stream_of(device)), "batch backward")
+                                           N.ptr(gv), N.ptr(record), int(vcap), int(fcap), N.stream_of(device)),
+                "batch backward")
 
 
 def record_slots(grids):
@@ -145,9 +152,11 @@ class _BatchFunction(Function):
         width = 3 if bx.method == N.MC else 4
         verts = torch.empty((nv, 3), dtype=bx.dtype, device=dev)
         faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
-        bx.emit(normalize, verts, faces, dev)
+        wants_grad = any(ctx.needs_input_grad[7:])
+        edges = bx.edge_record(nv, nf, dev) if wants_grad else None
+        bx.emit(normalize, verts, faces, dev, edges)
         ctx.bx, ctx.n, ctx.has_def, ctx.isos, ctx.normalize, ctx.exact = bx, n, has_def, isos, normalize, exact_grad
-        ctx.record = record
+        ctx.record, ctx.edges, ctx.caps = record, edges, (nv, nf)
         ctx.save_for_backward(*inputs)
         meta = [(int(res.voff[i]), int(res.counts[i].n_verts), int(res.foff[i]), int(res.counts[i].n_faces),
                  _guard(res, i, isos[i], bx.dtype)) for i in range(n)]
@@ -179,11 +188,11 @@ class _BatchFunction(Function):
         gd = [torch.empty_like(d) for d in defs] if defs is not None else None
         grids = _grids(sdfs, defs, ctx.isos, ctx.bx.dtype, gs, gd)
         bx = ctx.bx
-        # the forward's record (scanned segment counts and tile bytes) is all the state kept;
-        # every crossing is re-derived from the grids
+        # the forward's records (scanned segment counts and tile bytes; the edge record)
+        # are all the state kept
         bx.prepare(grids, ctx.record, dev)
         gv = gverts.contiguous() if gverts is not None else torch.zeros(0, 3, dtype=bx.dtype, device=dev)
-        bx.backward(ctx.normalize, ctx.exact, gv, dev)
+        bx.backward(ctx.normalize, ctx.exact, gv, ctx.edges, *ctx.caps, dev)
         return (None,) * 7 + tuple(gs) + (tuple(gd) if gd is not None else ())
 
 
@@ -290,14 +299,16 @@ class BatchPlan:
             self.verts = torch.empty((vcap, 3), dtype=self.dtype, device=self.device)
             self.faces = torch.empty((fcap, width), dtype=torch.int64, device=self.device)
             self.grad_verts = torch.zeros((vcap, 3), dtype=self.dtype, device=self.device)
+            self.edges = self.bx.edge_record(vcap, fcap, self.device)
         self.graph = None
         return nv, nf
 
     def run(self):
         """Count, emit and backward of every grid: device work only, no host synchronisation."""
         self.bx.count(self.device)
-        self.bx.emit(self.normalize, self.verts, self.faces, self.device)
-        self.bx.backward(self.normalize, self.exact, self.grad_verts, self.device)
+        self.bx.emit(self.normalize, self.verts, self.faces, self.device, self.edges)
+        self.bx.backward(self.normalize, self.exact, self.grad_verts, self.edges, self.verts.shape[0],
+                         self.faces.shape[0], self.device)
 
     def capture(self):
         if self.verts is None:

@@ -194,10 +194,10 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grid: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
-  const int64_t blocks = count_blocks(g);
-  const int64_t per_block = (CP / TX) * (CR / TY);
-  const int64_t want = std::max<int64_t>(ex->resident_ctas, (blocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
-  const unsigned grid = (unsigned)std::min<int64_t>(want, blocks);
+  const int64_t units = count_units(g);
+  const int64_t want =
+      std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::min<int64_t>(want, units);
   if (ex->method == DISO_MC)
     count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
   else
@@ -230,39 +230,39 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
 
 template <class S>
 int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
-                 double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, cudaStream_t s) {
+                 double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, void* record,
+                 cudaStream_t s) {
   Geom g;
   g.init(nx, ny, nz);
   if (ex->last_active <= 0) return DISO_OK;
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const unsigned grid = (unsigned)ex->last_active;
   if (ex->method == DISO_MC)
-    mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize);
+    mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
   else
-    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize);
+    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
 
+// CTAs of the persistent edge pass
+inline unsigned edge_ctas(const diso_extractor* ex) { return (unsigned)std::max(1, ex->sms * 8); }
+
 template <class S>
 int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
-             double padval, const uint64_t* seg, int normalize, int flags, const void* gv, void* gsdf, void* gdef,
-             cudaStream_t s) {
+             double padval, const uint64_t* seg, void* record, int normalize, int flags, const void* gv, void* gsdf,
+             void* gdef, cudaStream_t s) {
   Geom g;
   g.init(nx, ny, nz);
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
-  const unsigned grid = (unsigned)g.nptiles();
-  const size_t smem = backward_dyn_smem<S>();
-  const int ex_flag = (flags & DISO_GRAD_EXACT) ? 1 : 0;
-  if (ex->method == DISO_MC) {
-    CUDA_TRY(cudaFuncSetAttribute(backward_kernel<S, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    backward_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize, 0,
-                                                       (S*)gsdf, (S*)gdef);
-  } else {
-    CUDA_TRY(cudaFuncSetAttribute(backward_kernel<S, DMC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    backward_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(f, g, seg, tile_flags(seg, g), (const S*)gv, normalize,
-                                                        ex_flag, (S*)gsdf, (S*)gdef);
-  }
+  const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  if (ex->method == DISO_MC)
+    edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, 0);
+  else
+    edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, exact);
+  CUDA_TRY(cudaGetLastError());
+  gather_kernel<S><<<(unsigned)g.nptiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), record, (S*)gsdf,
+                                                               (S*)gdef);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
@@ -333,9 +333,6 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
         &per, ex->method == DISO_MC ? batch_count_kernel<S, MC> : batch_count_kernel<S, DMC>, NTHREADS, 0));
     ex->bcount_ctas = ex->sms * std::max(per, 1);
     ex->bwork_ctas = ex->sms * 4;
-    const size_t smem = backward_dyn_smem<S>();
-    CUDA_TRY(cudaFuncSetAttribute(batch_backward_kernel<S, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CUDA_TRY(cudaFuncSetAttribute(batch_backward_kernel<S, DMC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   // the previous prepare's upload must have left the staging buffer
   CUDA_TRY(cudaStreamSynchronize(s));
@@ -362,7 +359,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     ex->bseg_off[i] = seg_off;
     seg_off += b.g.nseg;
     tile_off += b.g.ntiles();
-    cblk += count_blocks(b.g);
+    cblk += count_units(b.g);
     ptile += b.g.nptiles();
   }
   offs[n] = seg_off;
@@ -403,8 +400,8 @@ int batch_count(diso_extractor* ex, cudaStream_t s) {
   init_stats_kernel<<<1, 256, 0, s>>>(ex->bstats, n);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemsetAsync(ex->stats, 0, sizeof(Stats), s));
-  const int64_t per_block = (CP / TX) * (CR / TY);
-  const int64_t want = std::max<int64_t>(ex->bcount_ctas, (ex->bblocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
+  const int64_t want =
+      std::max<int64_t>(ex->bcount_ctas, (ex->bblocks * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, ex->bblocks));
   const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
   if (ex->method == DISO_MC)
@@ -425,31 +422,47 @@ int batch_count(diso_extractor* ex, cudaStream_t s) {
   return DISO_OK;
 }
 
+// the batch record is laid out for the capacities: E = faces (DMC quads) or vertices (MC)
+template <class S>
+EdgeRecord<S> batch_record(const diso_extractor* ex, void* record, int64_t vcap, int64_t fcap) {
+  if (!record) return EdgeRecord<S>{nullptr, nullptr, nullptr, nullptr};
+  return edge_record<S>(record, ex->method, vcap, ex->method == DISO_MC ? vcap : fcap);
+}
+
 template <class S>
 int batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
-               cudaStream_t s) {
+               void* record, cudaStream_t s) {
   const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
   const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
+  const EdgeRecord<S> rec = batch_record<S>(ex, record, vcap, fcap);
   if (ex->method == DISO_MC)
     batch_emit_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, ex->active, &ex->bstats->n_active, (S*)verts, faces, vcap,
-                                                        fcap, normalize, ex->bstats);
+                                                        fcap, normalize, ex->bstats, rec);
   else
     batch_emit_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(d, ex->active, &ex->bstats->n_active, (S*)verts, faces,
-                                                         vcap, fcap, normalize, ex->bstats);
+                                                         vcap, fcap, normalize, ex->bstats, rec);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
 
 template <class S>
-int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv, cudaStream_t s) {
+int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv, void* record, int64_t vcap,
+                   int64_t fcap, cudaStream_t s) {
   const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
   const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
-  const size_t smem = backward_dyn_smem<S>();
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
-  if (ex->method == DISO_MC)
-    batch_backward_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(d, ex->bn, ex->bptiles, (const S*)gv, normalize, 0);
-  else
-    batch_backward_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(d, ex->bn, ex->bptiles, (const S*)gv, normalize, exact);
+  const EdgeRecord<S> rec = batch_record<S>(ex, record, vcap, fcap);
+  if (ex->method == DISO_MC) {
+    batch_edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(d, ex->bn, rec, vcap, fcap, (const S*)gv,
+                                                                   normalize, 0);
+    CUDA_TRY(cudaGetLastError());
+    batch_gather_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, ex->bn, ex->bptiles, record, vcap, fcap);
+  } else {
+    batch_edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(d, ex->bn, rec, vcap, fcap, (const S*)gv,
+                                                                    normalize, exact);
+    CUDA_TRY(cudaGetLastError());
+    batch_gather_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(d, ex->bn, ex->bptiles, record, vcap, fcap);
+  }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
@@ -529,14 +542,23 @@ int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int 
 
 int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
                       double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
-                      int64_t* faces, void* stream) {
+                      int64_t* faces, uint64_t* edge_record, void* stream) {
   int rc = check_common(ex, sdf, nx, ny, nz);
   if (rc) return rc;
   if (!seg || !verts || !faces) return fail(DISO_ERR_ARG, "null seg, verts or faces");
+  if (((uintptr_t)edge_record & 31u) != 0) return fail(DISO_ERR_ARG, "edge record must be 32-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
-  return ex->dtype == DISO_F32
-             ? forward_emit<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, verts, faces, s)
-             : forward_emit<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, verts, faces, s);
+  return ex->dtype == DISO_F32 ? forward_emit<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
+                                                     verts, faces, edge_record, s)
+                               : forward_emit<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
+                                                      verts, faces, edge_record, s);
+}
+
+int64_t diso_edge_record_slots(int method, int dtype, int64_t n_verts, int64_t n_faces) {
+  if ((method != DISO_MC && method != DISO_DMC) || (dtype != DISO_F32 && dtype != DISO_F64)) return 0;
+  if (n_verts < 0 || n_faces < 0) return 0;
+  const int64_t E = method == DISO_MC ? n_verts : n_faces;
+  return edge_record_slots(method, dtype == DISO_F32 ? 4 : 8, n_verts, E);
 }
 
 int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int64_t n_quads, int64_t* tris,
@@ -555,18 +577,22 @@ int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads
 }
 
 int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
-                  double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
-                  void* grad_sdf, void* grad_deform, void* stream) {
-  int rc = check_common(ex, sdf, nx, ny, nz);
-  if (rc) return rc;
+                  double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
+                  const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream) {
   if (!seg || !grad_sdf) return fail(DISO_ERR_ARG, "null seg or grad_sdf");
+  if (!edge_record) return fail(DISO_ERR_ARG, "null edge record (the forward emit must record the edges)");
+  if (((uintptr_t)edge_record & 31u) != 0) return fail(DISO_ERR_ARG, "edge record must be 32-byte aligned");
   if (deform && !grad_deform) return fail(DISO_ERR_ARG, "deform given without grad_deform");
   if (!grad_verts) return fail(DISO_ERR_ARG, "null grad_verts");
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
-  return ex->dtype == DISO_F32 ? backward<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize, flags,
-                                                 grad_verts, grad_sdf, deform ? grad_deform : nullptr, s)
-                               : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
-                                                  flags, grad_verts, grad_sdf, deform ? grad_deform : nullptr, s);
+  return ex->dtype == DISO_F32 ? backward<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, edge_record,
+                                                 normalize, flags, grad_verts, grad_sdf,
+                                                 deform ? grad_deform : nullptr, s)
+                               : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, edge_record,
+                                                  normalize, flags, grad_verts, grad_sdf,
+                                                  deform ? grad_deform : nullptr, s);
 }
 
 int64_t diso_batch_record_slots(const diso_grid* grids, int ngrids) {
@@ -607,25 +633,30 @@ int diso_batch_results(diso_extractor* ex, diso_counts* per_grid, int64_t* vert_
 }
 
 int diso_batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
-                    void* stream) {
+                    uint64_t* edge_record, void* stream) {
   if (!ex || ex->bn < 1) return fail(DISO_ERR_ARG, "no prepared batch");
   if ((!verts && vcap) || (!faces && fcap) || vcap < 0 || fcap < 0) return fail(DISO_ERR_ARG, "bad output buffers");
+  if (((uintptr_t)edge_record & 31u) != 0) return fail(DISO_ERR_ARG, "edge record must be 32-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
-  return ex->dtype == DISO_F32 ? batch_emit<float>(ex, normalize, verts, vcap, faces, fcap, s)
-                               : batch_emit<double>(ex, normalize, verts, vcap, faces, fcap, s);
+  return ex->dtype == DISO_F32 ? batch_emit<float>(ex, normalize, verts, vcap, faces, fcap, edge_record, s)
+                               : batch_emit<double>(ex, normalize, verts, vcap, faces, fcap, edge_record, s);
 }
 
-int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, void* stream) {
+int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, uint64_t* edge_record,
+                        int64_t vcap, int64_t fcap, void* stream) {
   if (!ex || ex->bn < 1) return fail(DISO_ERR_ARG, "no prepared batch");
   if (!grad_verts) return fail(DISO_ERR_ARG, "null grad_verts");
+  if (!edge_record) return fail(DISO_ERR_ARG, "null edge record (the batch emit must record the edges)");
+  if (((uintptr_t)edge_record & 31u) != 0) return fail(DISO_ERR_ARG, "edge record must be 32-byte aligned");
+  if (vcap < 0 || fcap < 0) return fail(DISO_ERR_ARG, "bad capacities");
   for (int i = 0; i < ex->bn; ++i) {
     const bool missing = ex->dtype == DISO_F32 ? ((const BatchGrid<float>*)ex->bdesc_host)[i].gsdf == nullptr
                                                : ((const BatchGrid<double>*)ex->bdesc_host)[i].gsdf == nullptr;
     if (missing) return fail(DISO_ERR_ARG, "grid %d of the batch has no grad_sdf", i);
   }
   cudaStream_t s = (cudaStream_t)stream;
-  return ex->dtype == DISO_F32 ? batch_backward<float>(ex, normalize, flags, grad_verts, s)
-                               : batch_backward<double>(ex, normalize, flags, grad_verts, s);
+  return ex->dtype == DISO_F32 ? batch_backward<float>(ex, normalize, flags, grad_verts, edge_record, vcap, fcap, s)
+                               : batch_backward<double>(ex, normalize, flags, grad_verts, edge_record, vcap, fcap, s);
 }
 
 const char* diso_last_error(void) { return g_err; }
@@ -692,10 +723,9 @@ int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sd
   CUDA_TRY(cudaMemsetAsync(&sc->stats, 0, sizeof(Stats), s));
   CUDA_TRY(cudaMemsetAsync(&sc->stats.min_key, 0xff, sizeof(unsigned long long), s));
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
-  const int64_t blocks = count_blocks(g);
-  const int64_t per_block = (CP / TX) * (CR / TY);
-  const int64_t want = std::max<int64_t>(ctas, (blocks * per_block + COUNT_LIST - 1) / COUNT_LIST);
-  const unsigned grid = (unsigned)std::min<int64_t>(want, blocks);
+  const int64_t units = count_units(g);
+  const int64_t want = std::max<int64_t>(ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+  const unsigned grid = (unsigned)std::min<int64_t>(want, units);
   if (method == DISO_MC)
     count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), &sc->stats, sc->active);
   else

@@ -80,6 +80,58 @@ __device__ __forceinline__ uint32_t zvalid(const Geom& g, int Z0) {
   return n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
 }
 
+// ------------------------------------------------------------------ edge record
+
+// Per-call edge record, written by the forward emit when gradients will be wanted
+// and read by the backward.  E = crossing edges (the MC vertices / the DMC quads, in
+// output order), V = vertices.  Layout in 8-byte slots, ordered so that adj and ids
+// are 32- and 16-byte aligned when the record is 32-byte aligned:
+//   adj [E][8] S      the backward's per-edge adjoints: (dL/dsdf, dL/ddeform) at the
+//                     edge's first point, then at its second point
+//   ids [E][4] int32  DMC: the patch (grid-local vertex id) of each of the four cells
+//                     around the edge, the cell one step back by db along axis a+1
+//                     and dc along axis a+2 (mod 3) at index db + 2 dc
+//   loc [E] int64     the edge's owner cell (X, Y, Z) and axis, packed by pack_loc
+//   aux [V] uint8     DMC: edges of the vertex's patch | index of the patch in its cell << 4
+template <class S>
+struct EdgeRecord {
+  S* adj;
+  int64_t* loc;
+  int32_t* ids;
+  uint8_t* aux;
+};
+
+__host__ __device__ inline int64_t edge_record_slots(int method, int dsize, int64_t V, int64_t E) {
+  return E * dsize + E + (method == 1 ? 2 * E + (V + 7) / 8 : 0);
+}
+
+template <class S>
+__host__ __device__ inline EdgeRecord<S> edge_record(void* base, int method, int64_t V, int64_t E) {
+  EdgeRecord<S> r;
+  int64_t* p = (int64_t*)base;
+  r.adj = (S*)p;
+  p += E * (int64_t)sizeof(S);
+  r.ids = method == 1 ? (int32_t*)p : nullptr;
+  if (method == 1) p += 2 * E;
+  r.loc = p;
+  p += E;
+  r.aux = method == 1 ? (uint8_t*)p : nullptr;
+  (void)V;
+  return r;
+}
+
+// cells per axis are below 2^21 (x, y) and 2^20 (z)
+constexpr int LOC_MAX_XY = 1 << 21, LOC_MAX_Z = 1 << 20;
+__device__ __forceinline__ int64_t pack_loc(int X, int Y, int Z, int a) {
+  return ((int64_t)X << 43) | ((int64_t)Y << 22) | ((int64_t)Z << 2) | (int64_t)a;
+}
+__device__ __forceinline__ void unpack_loc(int64_t l, int& X, int& Y, int& Z, int& a) {
+  X = (int)(l >> 43);
+  Y = (int)((l >> 22) & (LOC_MAX_XY - 1));
+  Z = (int)((l >> 2) & (LOC_MAX_Z - 1));
+  a = (int)(l & 3);
+}
+
 // ------------------------------------------------------------------ row masks
 
 // Fill m[x][y] for point rows (WX0 + x, WY0 + y); bit k = point Z0 - 1 + k >= iso.
@@ -203,115 +255,182 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 
 // ------------------------------------------------------------------ count
 
-// The count pass works on blocks of CP planes x CR rows x 32 cells: one warp per
-// plane, one lane per row segment.  Each lane derives its segment's crossing count
-// from four row masks with popcounts and walks only the segment's non-trivial
-// cells for the case-table lookups.  A block covers (CP/TX) x (CR/TY) activity tiles.
+// The count pass works on units of CP planes x CR rows of cells and KZ chunks of 32
+// cells along z, walked in z order: one warp per plane, one lane per row segment.
+// For every chunk, each point row of the unit ((CP+1) x (CR+1) rows) is read once,
+// 32 points by one coalesced load, and turned into one ballot; a row's 35-bit mask
+// is spliced from the ballots of three consecutive chunks (two bits of the chunk
+// below, all of the chunk, one bit of the chunk above), so every point is read once
+// per unit and the per-row cost is a load, a compare, a ballot and a store.  Each
+// lane derives its segment's crossing count from four row masks with popcounts and
+// walks only the segment's non-trivial cells for the case-table lookups (the DMC
+// ambiguity test reads a neighbour outside the unit's rows from global memory).
 //
-// Persistent: CTA b handles blocks b, b + gridDim.x, ...; it keeps the min / max and
-// the list of its active tiles and publishes them with a few atomics at the end
-// (per-tile atomics on one address serialise in L2).  At most COUNT_LIST tiles per
-// CTA: launch at least ntiles / COUNT_LIST CTAs.
-constexpr int CP = 8, CR = 32;
+// Persistent: CTA b handles units b, b + gridDim.x, ...; it keeps the list of its
+// active tiles and publishes it with one atomic at the end (per-tile atomics on one
+// address serialise in L2).  At most COUNT_LIST tiles per CTA: launch at least
+// ntiles / COUNT_LIST CTAs.
+constexpr int CP = 8, CR = 32, KZ = 4;
+constexpr int CROWS = (CP + 1) * (CR + 1);  // point rows of a unit
+constexpr int CRPW = (CROWS + 7) / 8;       // point rows per warp
 constexpr int COUNT_LIST = 2048;
-static_assert(CP * 32 == NTHREADS && CP % TX == 0 && CR % TY == 0, "count block shape");
+constexpr int COUNT_TILES_PER_UNIT = (CP / TX) * (CR / TY) * KZ;
+static_assert(CP * 32 == NTHREADS && CP % TX == 0 && CR % TY == 0 && CRPW <= 64, "count unit shape");
 
-__host__ __device__ inline int64_t count_blocks(const Geom& g) {
-  return (int64_t)((g.c[0] + CP - 1) / CP) * ((g.c[1] + CR - 1) / CR) * g.nzc;
+__host__ __device__ inline int64_t count_units(const Geom& g) {
+  return (int64_t)((g.c[0] + CP - 1) / CP) * ((g.c[1] + CR - 1) / CR) * ((g.nzc + KZ - 1) / KZ);
 }
 
 template <class S, int METHOD>
 struct CountShared {
-  // MC needs the rows of the cells' corners, DMC also those of the face neighbours
-  // used by the ambiguity test
-  static constexpr int H = METHOD == DMC ? 1 : 0;
-  static constexpr int WX = CP + 1 + 2 * H, WY = CR + 1 + 2 * H;
-  uint64_t m[WX][WY];
+  uint64_t m[CP + 1][CR + 1];  // masks of the current chunk, point row r = x * (CR + 1) + y
+  int64_t rowoff[CROWS];       // offset of point row r in the SDF, -1 outside the grid
+  uint32_t bal[CROWS];         // ballots of the chunk just read (each row read and used by one warp)
   uint32_t act[CP];
   int list[COUNT_LIST];
   int nlist, base;
 };
 
-// lower the grid's min / max keys (one warp's values); reads first so that most
-// warps need no atomic
+__device__ __forceinline__ float smin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float smax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double smin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ double smax(double a, double b) { return fmax(a, b); }
+
+// lower the grid's min / max keys by one warp's values (+inf / -inf: none seen);
+// reads first so that most warps need no atomic
 template <class S>
-__device__ __forceinline__ void publish_minmax(Stats* stats, S mn, S mx, bool seen) {
+__device__ __forceinline__ void publish_minmax(Stats* stats, S mn, S mx) {
   const int lane = threadIdx.x & 31;
-  const unsigned have = __ballot_sync(0xffffffffu, seen);
-  if (!have) return;
-  const int src = __ffs(have) - 1;
-  const S m0 = __shfl_sync(0xffffffffu, mn, src), x0 = __shfl_sync(0xffffffffu, mx, src);
-  if (!seen) {
-    mn = m0;
-    mx = x0;
-  }
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
-    const S p = __shfl_xor_sync(0xffffffffu, mn, o), q = __shfl_xor_sync(0xffffffffu, mx, o);
-    mn = p < mn ? p : mn;
-    mx = q > mx ? q : mx;
+    mn = smin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = smax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   }
-  if (lane == 0) {
+  if (lane == 0 && mn <= mx) {
     const unsigned long long kmn = ord_key((double)mn), kmx = ord_key((double)mx);
     if (kmn < *(volatile unsigned long long*)&stats->min_key) atomicMin(&stats->min_key, kmn);
     if (kmx > *(volatile unsigned long long*)&stats->max_key) atomicMax(&stats->max_key, kmx);
   }
 }
 
-// One count block: the per-segment counts, the activity bytes of the block's
-// tiles, the grid's min / max; active tiles are appended (as tile | tag) to sh.list.
+// ballots of chunk t (unpadded z in [32t, 32t + 32)) of the warp's point rows into
+// sh.bal; min / max of the values read.  Only the lanes in `lanes` read (the chunks
+// below and above a unit contribute two bits and one bit to its masks).
 template <class S, int METHOD>
-__device__ __forceinline__ void count_block(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
-                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
-                                            Stats* stats, int blk, int tag) {
-  constexpr int H = CountShared<S, METHOD>::H, WX = CountShared<S, METHOD>::WX, WY = CountShared<S, METHOD>::WY;
+__device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const Field<S>& f, int t, uint32_t lanes,
+                                              S& mn, S& mx) {
+  constexpr int NB = 4, HALF = (CRPW + NB - 1) / NB;  // NB batches of HALF row loads in flight
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nby = (g.c[1] + CR - 1) / CR;
-  const int tz = blk % g.nzc;
-  const int r = blk / g.nzc;
-  const int X0 = (r / nby) * CP, Y0 = (r % nby) * CR, Z0 = tz * TZ;
-  const int WX0 = X0 - H, WY0 = Y0 - H;
-  S mn = f.pad, mx = f.pad;
-  bool seen = false;
-  load_masks<S, WX, WY, true>(sh.m, f, WX0, WY0, Z0, mn, mx, seen);
-  __syncthreads();
-  publish_minmax<S>(stats, mn, mx, seen);
-  const int X = X0 + warp, Y = Y0 + lane;
-  uint32_t nv = 0, nf = 0;
-  if (X < g.c[0] && Y < g.c[1]) {
-    const int x = warp + H, y = lane + H;
-    const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
-    const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
-    nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
-    uint32_t nt = rw.nt;
-    while (nt) {
-      const int j = __ffs(nt) - 1;
-      nt &= nt - 1;
-      const int code = code8(a, b, c, d, j + 1);
-      if (METHOD == MC)
-        nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-      else
-        nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, WX0, WY0, Z0, code, X, Y, Z0 + j, g)));
-    }
-    seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-  }
-  // a cell can emit faces / patches without owning a crossing edge (its
-  // crossings may all sit on edges owned by its +1 neighbours)
-  const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
-  if (lane == 0) sh.act[warp] = busy;
-  __syncthreads();
-  if (threadIdx.x < (CP / TX) * (CR / TY)) {
-    const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
-    const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
-    if (tx < g.tiles_x() && ty < g.tiles_y()) {
-      uint32_t any = 0;
+  const int z = 32 * t + lane;
+  const bool zin = (unsigned)z < (unsigned)f.n2 && ((lanes >> lane) & 1u);
 #pragma unroll
-      for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
-      const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
-      tile_flag[tile] = any ? 1 : 0;
-      if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
+  for (int h = 0; h < NB; ++h) {
+    S v[HALF];
+    bool in[HALF];
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      const int r = warp + 8 * (h * HALF + k);
+      const int64_t off = r < CROWS ? sh.rowoff[r] : -1;
+      in[k] = zin && off >= 0;
+      v[k] = in[k] ? __ldg(f.sdf + off + z) : f.pad;
+    }
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      const int r = warp + 8 * (h * HALF + k);
+      if (h * HALF + k < CRPW && r < CROWS) {
+        const uint32_t b = __ballot_sync(0xffffffffu, v[k] >= f.iso);
+        if (lane == 0) sh.bal[r] = b;
+      }
+      if (in[k]) {
+        mn = smin(mn, v[k]);
+        mx = smax(mx, v[k]);
+      }
     }
   }
+  __syncwarp();
+}
+
+// One unit: per-segment counts, activity bytes of its tiles, the grid's min / max;
+// active tiles are appended (as tile | tag) to sh.list.
+template <class S, int METHOD>
+__device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+                                           uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
+                                           Stats* stats, int64_t unit, int tag) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // a row of nzc chunks is cut into nbz near-equal runs of at most KZ chunks
+  const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
+  const int tz0 = (int)(unit % nbz) * kz;
+  const int64_t col = unit / nbz;
+  const int X0 = (int)(col / nby) * CP, Y0 = (int)(col % nby) * CR;
+  const int tz1 = min(tz0 + kz, g.nzc);
+  // point row r = (X0 + r / (CR+1), Y0 + r % (CR+1)) in padded coordinates
+  for (int r = threadIdx.x; r < CROWS; r += NTHREADS) {
+    const int X = X0 + r / (CR + 1), Y = Y0 + r % (CR + 1);
+    const bool in = (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
+    sh.rowoff[r] = in ? ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 : -1;
+  }
+  __syncthreads();  // also: the previous unit's last readers of sh.m / sh.act are done
+  S mn = S(INFINITY), mx = S(-INFINITY);
+  // ballot history of the lane's rows i = lane and lane + 32 of this warp:
+  // chunks tz - 1 (p2) and tz (p1)
+  uint32_t p1[2] = {0u, 0u}, p2[2] = {0u, 0u};
+  // interior z of chunk t: [32t, 32t + 32); the padded mask of chunk tz spans
+  // unpadded z in [32tz - 2, 32tz + 33)
+#pragma unroll 1
+  for (int t = tz0 - 1; t <= tz1; ++t) {
+    count_ballots<S, METHOD>(sh, f, t, t < tz0 ? 0xc0000000u : (t == tz1 ? 1u : 0xffffffffu), mn, mx);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int i = lane + 32 * k, r = warp + 8 * i;
+      if (i < CRPW && r < CROWS) {
+        const uint32_t cur = sh.bal[r];
+        if (t >= tz0 + 1)
+          (&sh.m[0][0])[r] = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
+        p2[k] = p1[k];
+        p1[k] = cur;
+      }
+    }
+    if (t < tz0 + 1) continue;
+    const int tz = t - 1, Z0 = tz * TZ;
+    __syncthreads();
+    const int X = X0 + warp, Y = Y0 + lane;
+    uint32_t nv = 0, nf = 0;
+    if (X < g.c[0] && Y < g.c[1]) {
+      const int x = warp, y = lane;
+      const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
+      const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
+      nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
+      uint32_t nt = rw.nt;
+      while (nt) {
+        const int j = __ffs(nt) - 1;
+        nt &= nt - 1;
+        const int code = code8(a, b, c, d, j + 1);
+        if (METHOD == MC)
+          nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+        else
+          nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g)));
+      }
+      seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
+    }
+    // a cell can emit faces / patches without owning a crossing edge (its
+    // crossings may all sit on edges owned by its +1 neighbours)
+    const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
+    if (lane == 0) sh.act[warp] = busy;
+    __syncthreads();
+    if (threadIdx.x < (CP / TX) * (CR / TY)) {
+      const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
+      const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
+      if (tx < g.tiles_x() && ty < g.tiles_y()) {
+        uint32_t any = 0;
+#pragma unroll
+        for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
+        const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
+        tile_flag[tile] = any ? 1 : 0;
+        if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
+      }
+    }
+  }
+  publish_minmax<S>(stats, mn, mx);
 }
 
 // append the CTA's active tiles to the global list
@@ -324,19 +443,15 @@ __device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned
   for (int i = threadIdx.x; i < sh.nlist; i += blockDim.x) active[sh.base + i] = sh.list[i];
 }
 
-// Persistent: CTA b handles blocks b, b + gridDim.x, ...; the active tiles of a CTA
-// are kept in shared memory and published with one atomic at the end (per-tile
-// atomics on one address serialise in L2).  At most COUNT_LIST tiles per CTA:
-// launch at least ntiles / COUNT_LIST CTAs.
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                             uint8_t* __restrict__ tile_flag, Stats* stats,
                                                             int* __restrict__ active) {
   __shared__ CountShared<S, METHOD> sh;
   if (threadIdx.x == 0) sh.nlist = 0;
-  const int nblocks = (int)count_blocks(g);
+  const int64_t nunits = count_units(g);
 #pragma unroll 1
-  for (int blk = blockIdx.x; blk < nblocks; blk += gridDim.x) count_block<S, METHOD>(sh, f, g, seg, tile_flag, stats, blk, 0);
+  for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x) count_unit<S, METHOD>(sh, f, g, seg, tile_flag, stats, u, 0);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
 
@@ -352,7 +467,7 @@ struct BatchGrid {
   uint64_t* seg;        // this grid's first segment in the concatenated, globally scanned array
   uint64_t* seg_end;    // the next grid's first segment (or the total slot)
   uint8_t* tile_flag;   // this grid's tile bytes
-  int64_t cblk0;        // first count block of the grid in the flattened queue
+  int64_t cblk0;        // first count unit of the grid in the flattened queue
   int64_t ptile0;       // first point tile (backward)
   S* gsdf;              // backward outputs
   S* gdef;
@@ -372,7 +487,7 @@ __device__ __forceinline__ int batch_find(const int64_t* start, int n, int64_t b
 }
 
 // every grid of a batch in one persistent launch over the flattened queue of count
-// blocks; per-grid status words in stats[grid]
+// units; per-grid status words in stats[grid]
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
                                                                   int64_t nblocks, Stats* stats,
@@ -387,7 +502,7 @@ __global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGri
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
     const int i = batch_find(start, ngrids, b);
     const BatchGrid<S>& G = grids[i];
-    count_block<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, stats + i, (int)(b - start[i]), i << BATCH_TILE_BITS);
+    count_unit<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, stats + i, b - start[i], i << BATCH_TILE_BITS);
   }
   count_flush<S, METHOD>(sh, n_active, active);
 }
@@ -446,7 +561,7 @@ constexpr int EMIT_ITEMS = 3 * TX * TY * TZ;  // every own edge crossing
 template <class S>
 __device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
                                              int tile, S* __restrict__ verts, int64_t* __restrict__ faces,
-                                             int normalize, int64_t vsub) {
+                                             int normalize, int64_t vsub, const EdgeRecord<S>& rec) {
   constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint64_t m[WX][WY];
@@ -535,7 +650,9 @@ __device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, c
     item_decode(vitems[i], x, y, j, a);
     S p[3];
     edge_vertex<S>(f, X0 + x, Y0 + y, Z0 + j, a, p);
-    store_vertex<S>(verts, vid(x, y, j, a), p, g, normalize);
+    const int64_t v = vid(x, y, j, a);
+    store_vertex<S>(verts, v, p, g, normalize);
+    if (rec.loc) rec.loc[v] = pack_loc(X0 + x, Y0 + y, Z0 + j, a);
   }
   // triangles (src/cumc.cu:564-649): each table edge -> owner cell (+0/+1) -> its vertex
   for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
@@ -556,11 +673,21 @@ __device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, c
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
+// the record of one grid (null: none), laid out for the grid's scanned totals
+template <class S, int METHOD>
+__device__ __forceinline__ EdgeRecord<S> grid_record(void* record, const Geom& g, const uint64_t* __restrict__ seg) {
+  if (!record) return EdgeRecord<S>{nullptr, nullptr, nullptr, nullptr};
+  const uint64_t tot = seg[g.nseg];
+  return edge_record<S>(record, METHOD, METHOD == MC ? Counts::lo(tot) : Counts::hi(tot), Counts::lo(tot));
+}
+
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                            const int* __restrict__ active, S* __restrict__ verts,
-                                                           int64_t* __restrict__ faces, int normalize) {
-  mc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, faces, normalize, 0);
+                                                           int64_t* __restrict__ faces, int normalize,
+                                                           void* record) {
+  const EdgeRecord<S> rec = grid_record<S, MC>(record, g, seg);
+  mc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, faces, normalize, 0, rec);
 }
 
 // ------------------------------------------------------------------ DMC emit
@@ -570,7 +697,7 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
 template <class S>
 __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
                                               int tile, S* __restrict__ verts, int64_t* __restrict__ quads,
-                                              int normalize, int64_t vsub) {
+                                              int normalize, int64_t vsub, const EdgeRecord<S>& rec) {
   constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
   __shared__ uint64_t m[WX][WY];
@@ -658,11 +785,21 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const RowBits r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
     const int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
     const int type = a + 3 * (int)((m[x][y] >> (j + 1)) & 1);
+    int rid[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int q = g_dmc_quad[4 * type + k];
-      const int nx = x + (q & 3) - 1, ny = y + ((q >> 2) & 3) - 1, nz = j + 1 + ((q >> 4) & 3) - 1;
-      quads[4 * qid + k] = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8) - vsub;
+      const int ox = (q & 3) - 1, oy = ((q >> 2) & 3) - 1, oz = ((q >> 4) & 3) - 1;
+      const int nx = x + ox, ny = y + oy, nz = j + 1 + oz;
+      const int64_t id = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8) - vsub;
+      quads[4 * qid + k] = id;
+      // the record orders the cells by their steps back (db, dc) along axes a+1, a+2
+      const int db = -(a == 0 ? oy : (a == 1 ? oz : ox)), dc = -(a == 0 ? oz : (a == 1 ? ox : oy));
+      rid[db + 2 * dc] = (int)id;
+    }
+    if (rec.loc) {
+      rec.loc[qid] = pack_loc(X0 + ix, Y0 + iy, Z0 + j, a);
+      reinterpret_cast<int4*>(rec.ids)[qid] = make_int4(rid[0], rid[1], rid[2], rid[3]);
     }
   }
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
@@ -701,6 +838,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
         const S inv = S(1) / S(cnt[q]);
         const S v[3] = {acc[q][0] * inv, acc[q][1] * inv, acc[q][2] * inv};
         store_vertex<S>(verts, p0 + q, v, g, normalize);
+        if (rec.aux) rec.aux[p0 + q] = (uint8_t)(cnt[q] | (q << 4));
       }
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
@@ -709,8 +847,10 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                             const int* __restrict__ active, S* __restrict__ verts,
-                                                            int64_t* __restrict__ quads, int normalize) {
-  dmc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, quads, normalize, 0);
+                                                            int64_t* __restrict__ quads, int normalize,
+                                                            void* record) {
+  const EdgeRecord<S> rec = grid_record<S, DMC>(record, g, seg);
+  dmc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, quads, normalize, 0, rec);
 }
 
 // ------------------------------------------------------------------ backward
@@ -809,53 +949,135 @@ __device__ __forceinline__ void ptile_coords(int64_t tile, const Geom& g, int& x
   z0 = tz * TZ;
 }
 
-// rows of cell-window coordinates whose edges along axis a touch the tile's points:
-// axis 0: x in [0, TX], y in [1, TY]; axis 1: x in [1, TX], y in [0, TY];
-// axis 2: x in [1, TX], y in [1, TY]
-constexpr int BW_ROWS0 = (TX + 1) * TY, BW_ROWS1 = TX * (TY + 1), BW_ROWS2 = TX * TY;
-constexpr int BW_ROWS = BW_ROWS0 + BW_ROWS1 + BW_ROWS2;
-constexpr int BW_ITEMS = BW_ROWS * (TZ + 1);
-static_assert(BW_ROWS <= NTHREADS, "one thread per backward item row");
+__device__ const float g_recip_f[16] = {0.f,      1.f / 1,  1.f / 2,  1.f / 3,  1.f / 4,  1.f / 5,
+                                        1.f / 6,  1.f / 7,  1.f / 8,  1.f / 9,  1.f / 10, 1.f / 11,
+                                        1.f / 12, 1.f / 13, 1.f / 14, 1.f / 15};
+__device__ const double g_recip_d[16] = {0.,      1. / 1,  1. / 2,  1. / 3,  1. / 4,  1. / 5,  1. / 6,  1. / 7,
+                                         1. / 8,  1. / 9,  1. / 10, 1. / 11, 1. / 12, 1. / 13, 1. / 14, 1. / 15};
+// 1 / n, correctly rounded (what S(1) / S(n) gives)
+template <class S>
+__device__ __forceinline__ S recip(int n);
+template <>
+__device__ __forceinline__ float recip<float>(int n) { return __ldg(g_recip_f + n); }
+template <>
+__device__ __forceinline__ double recip<double>(int n) { return __ldg(g_recip_d + n); }
+
+// The backward runs in two passes.
+//
+// Edge pass: one thread per crossing edge of the record.  The gradient reaching the
+// edge's lerp vertex: MC, dL/dverts of that vertex (adj_create_cell_mc_verts_kernel,
+// src/cumc.cu:474-512); DMC, the sum over the four cells around the edge of
+// dL/d(dual vertex) / (edges in that patch) (adj_create_dmc_verts_kernel,
+// src/cudualmc.cu:957-1005), where the reference reads the gradient of the cell's
+// first patch for every patch of the cell (adj_verts[first] with first never
+// advanced, src/cudualmc.cu:990): exact = 0 reproduces that, exact = 1 uses each
+// patch's own gradient (the true derivative).  Its adjoint at both end points
+// (adjComputeMcVert, src/cumc.cu:412-453) goes to the record's adj slots.
+//
+// Point pass: every point tile; each point adds the adjoints of its (at most six)
+// crossing edges in a fixed order, so the result is deterministic without atomics,
+// and every gradient element is written once (zeros away from the surface).  This
+// replaces the forward re-run, the zero fills and the F.pad backward of
+// diso/__init__.py:30-44, 84-98.
 
 template <class S>
-constexpr size_t backward_dyn_smem() {
-  return sizeof(S) * 2 * TX * TY * TZ * 4;
+__device__ __forceinline__ void store_adj(S* __restrict__ adj, int64_t q, const S c0[4], const S c1[4]) {
+  S* o = adj + 8 * q;
+  if constexpr (sizeof(S) == 4) {
+    reinterpret_cast<float4*>(o)[0] = make_float4(c0[0], c0[1], c0[2], c0[3]);
+    reinterpret_cast<float4*>(o)[1] = make_float4(c1[0], c1[1], c1[2], c1[3]);
+  } else {
+    reinterpret_cast<double2*>(o)[0] = make_double2(c0[0], c0[1]);
+    reinterpret_cast<double2*>(o)[1] = make_double2(c0[2], c0[3]);
+    reinterpret_cast<double2*>(o)[2] = make_double2(c1[0], c1[1]);
+    reinterpret_cast<double2*>(o)[3] = make_double2(c1[2], c1[3]);
+  }
 }
 
-// dL/dsdf and dL/ddeform of every point of a tile.  Work list: the crossing edges
-// touching the tile, per axis.  Each edge's adjoint (adjComputeMcVert,
-// src/cumc.cu:412-453 / src/cudualmc.cu:710-751) is computed once and parked in the
-// slot of each endpoint inside the tile; each point then adds its (at most six)
-// slots in a fixed order, so the result is deterministic.  MC: the gradient
-// reaching an edge vertex is dL/dverts of that vertex (adj_create_cell_mc_verts_kernel,
-// src/cumc.cu:474-512).  DMC: it is the sum over the four cells around the edge of
-// dL/d(dual vertex) / (edges in that patch) (adj_create_dmc_verts_kernel,
-// src/cudualmc.cu:957-1005); the reference reads the gradient of the cell's first
-// patch for every patch of the cell (adj_verts[first] with first never advanced,
-// src/cudualmc.cu:990): exact = 0 reproduces that, exact = 1 uses each patch's own
-// gradient (the true derivative).  Replaces the forward re-run, the zero fills and
-// the F.pad backward of diso/__init__.py:30-44, 84-98.
+// adds adjoint slot k (0: the edge's first point, 1: its second) of edge q to acc
+template <class S>
+__device__ __forceinline__ void add_adj(const S* __restrict__ adj, int64_t q, int k, S acc[4]) {
+  const S* o = adj + 8 * q + 4 * k;
+  if constexpr (sizeof(S) == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(o));
+    acc[0] += v.x;
+    acc[1] += v.y;
+    acc[2] += v.z;
+    acc[3] += v.w;
+  } else {
+    const double2 u = __ldg(reinterpret_cast<const double2*>(o)), w = __ldg(reinterpret_cast<const double2*>(o) + 1);
+    acc[0] += u.x;
+    acc[1] += u.y;
+    acc[2] += w.x;
+    acc[3] += w.y;
+  }
+}
+
+// edge pass for edge q of the record; vbase = the grid's first vertex (batches)
 template <class S, int METHOD>
-__device__ __forceinline__ void backward_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
-                                              const uint8_t* __restrict__ tile_flag, int64_t ptile,
-                                              const S* __restrict__ gv, int normalize, int exact,
-                                              S* __restrict__ gsdf, S* __restrict__ gdef) {
-  constexpr int H = METHOD == DMC ? 1 : 0;  // DMC: one more mask row each side for the ambiguity test
-  constexpr int WX = TX + 2 + H, WY = TY + 2 + H;  // point rows [X0-H, X0+TX+1] x [Y0-H, Y0+TY+1]
-  constexpr int CX = TX + 1, CY = TY + 1;          // cell rows [X0, X0+TX] x [Y0, Y0+TY]; mask row x + H
-  constexpr int RX = METHOD == DMC ? CX : 1, RY = METHOD == DMC ? CY : 1;
-  constexpr int NP = TX * TY * TZ;
+__device__ __forceinline__ void edge_adjoint_at(const Field<S>& f, const EdgeRecord<S>& r, int64_t q, int64_t vbase,
+                                                const S* __restrict__ gv, const S scale[3], int exact) {
+  int X, Y, Z, a;
+  unpack_loc(__ldg(r.loc + q), X, Y, Z, a);
+  S gvec[3];
+  if constexpr (METHOD == MC) {
+    load_grad<S>(gv, q, scale, gvec);  // the edge's vertex has the edge's index
+  } else {
+    const int4 id4 = __ldg(reinterpret_cast<const int4*>(r.ids) + q);
+    const int id[4] = {id4.x, id4.y, id4.z, id4.w};
+    gvec[0] = gvec[1] = gvec[2] = S(0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t p = vbase + id[k];
+      const unsigned x = __ldg(r.aux + p);
+      const S inv = recip<S>((int)(x & 15u));
+      S v[3];
+      load_grad<S>(gv, exact ? p : p - (int64_t)(x >> 4), scale, v);
+      gvec[0] += v[0] * inv;
+      gvec[1] += v[1] * inv;
+      gvec[2] += v[2] * inv;
+    }
+  }
+  S c0[4], c1[4];
+  edge_adjoint2<S>(f, X, Y, Z, a, gvec, c0, c1);
+  store_adj<S>(r.adj, q, c0, c1);
+}
+
+template <class S>
+__device__ __forceinline__ void grad_scale(const Geom& g, int normalize, S scale[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
+}
+
+// edge pass of one grid: E and V from the scanned total of the per-call record
+template <class S, int METHOD>
+__global__ void __launch_bounds__(256) edge_adjoint_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                           void* record, const S* __restrict__ gv, int normalize,
+                                                           int exact) {
+  const int64_t E = Counts::lo(seg[g.nseg]);
+  const EdgeRecord<S> r = grid_record<S, METHOD>(record, g, seg);
+  S scale[3];
+  grad_scale<S>(g, normalize, scale);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < E; q += (int64_t)gridDim.x * blockDim.x)
+    edge_adjoint_at<S, METHOD>(f, r, q, 0, gv, scale, exact);
+}
+
+// Point tiles: unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ); in padded
+// coordinates the points are (X0+1.., Y0+1.., Z0+1..) with (X0, Y0, Z0) = (x0, y0, z0),
+// and the cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ] own every edge that touches
+// them.  Those cells lie in the forward tiles (x0/TX + {0,1}, y0/TY + {0,1},
+// z0/TZ + {0,1}); the point tile is inactive when none of them holds a crossing.
+// adj: the record's adjoints, indexed by the scanned crossing counts of seg.
+template <class S>
+__device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+                                            const uint8_t* __restrict__ tile_flag, int64_t ptile,
+                                            const S* __restrict__ adj, S* __restrict__ gsdf, S* __restrict__ gdef) {
+  constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
+  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint64_t m[WX][WY];
   __shared__ RowBits rb[CX][CY];
-  __shared__ uint8_t f32[CX][CY];
-  __shared__ uint32_t b0[CX][CY], b1[CX][CY];  // MC vertex / DMC patch bases of chunks zc and zc+1
-  __shared__ uint8_t rc[RX][RY][TZ + 1];
-  __shared__ uint8_t pre[RX][RY][TZ + 1];
-  __shared__ uint16_t items[BW_ITEMS];
-  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
-  __shared__ uint32_t aoff[4];
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
-  S* slot = reinterpret_cast<S*>(dyn_smem);  // [2][NP][4]: end 0 / end 1 adjoints of the current axis
+  __shared__ uint8_t f32[CX][CY];           // crossing flags of cell Z0 + TZ (first of the next chunk)
+  __shared__ uint32_t b0[CX][CY], b1[CX][CY];  // first edge of the cell row's chunks zc and zc + 1
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
   ptile_coords(ptile, g, X0, Y0, Z0);
@@ -864,236 +1086,176 @@ __device__ __forceinline__ void backward_tile(const Field<S>& f, const Geom& g, 
     return;
   }
   const int zc = Z0 / TZ;
-  const int WX0 = X0 - H, WY0 = Y0 - H;
+  // segment bases first, so that their loads overlap the mask loads
+  uint64_t sv = 0;
+  const int si = threadIdx.x, sk = si & 1, sy = (si >> 1) % CY, sx = (si >> 1) / CY;
+  if (si < CX * CY * 2) {
+    const int X = X0 + sx, Y = Y0 + sy, c = zc + sk;
+    if (X < g.c[0] && Y < g.c[1] && c < g.nzc) sv = seg[g.seg(X, Y, c)];
+  }
   S dmn, dmx;
   bool dseen = false;
-  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
-  for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
-    const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
-    const int X = X0 + x, Y = Y0 + y, c = zc + k;
-    const uint64_t s = (X < g.c[0] && Y < g.c[1] && c < g.nzc) ? seg[g.seg(X, Y, c)] : 0ull;
-    const uint32_t v = METHOD == MC ? Counts::lo(s) : Counts::hi(s);
-    if (k) b1[x][y] = v;
-    else b0[x][y] = v;
+  load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
+  if (si < CX * CY * 2) {
+    if (sk) b1[sx][sy] = Counts::lo(sv);
+    else b0[sx][sy] = Counts::lo(sv);
   }
   __syncthreads();
   const uint32_t valid = zvalid(g, Z0);
-  for (int i = threadIdx.x; i < CX * CY; i += blockDim.x) {
-    const int x = i / CY, y = i % CY;
+  if (threadIdx.x < CX * CY) {
+    const int x = threadIdx.x / CY, y = threadIdx.x % CY;
     RowBits r = {0u, 0u, 0u, 0u};
     int fl = 0;
     if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
-      const uint64_t a = m[x + H][y + H], b = m[x + H + 1][y + H], c = m[x + H][y + H + 1], d = m[x + H + 1][y + H + 1];
-      r = row_bits(a, b, c, d, valid);
-      if (Z0 + TZ < g.c[2]) fl = flags_at(a, b, c, TZ + 1);
+      r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+      if (Z0 + TZ < g.c[2]) fl = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
     }
     rb[x][y] = r;
     f32[x][y] = (uint8_t)fl;
   }
-  if constexpr (METHOD == DMC) {
-    // resolved codes and in-segment patch prefixes of the window cells
-    for (int r = warp; r < CX * CY; r += TY) {
-      const int x = r / CY, y = r % CY, X = X0 + x, Y = Y0 + y;
-      const bool row = X < g.c[0] && Y < g.c[1];
-      const uint64_t a = m[x + H][y + H], b = m[x + H + 1][y + H], c = m[x + H][y + H + 1], d = m[x + H + 1][y + H + 1];
-      const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
-      int code = 0;
-      if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
-      const uint32_t np = dmc_npatch(dmc_case(code));
-      const uint32_t inc = nt ? warp_incl(np) : 0u;
-      rc[x][y][lane] = (uint8_t)code;
-      pre[x][y][lane] = (uint8_t)(inc - np);
-      if (lane == 0) {
-        int c32 = 0;
-        if (row && Z0 + TZ < g.c[2]) {
-          c32 = code8(a, b, c, d, TZ + 1);
-          if (c32 != 0 && c32 != 255) c32 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c32, X, Y, Z0 + TZ, g);
-        }
-        rc[x][y][TZ] = (uint8_t)c32;
-        pre[x][y][TZ] = 0;  // first cell of the next segment
-      }
-    }
-  }
   __syncthreads();
-  // work list: crossing edges touching the tile, grouped by axis
-  int ra = -1, rx = 0, ry = 0;
-  uint64_t bits = 0;
-  {
-    const int t = threadIdx.x;
-    if (t < BW_ROWS0) {
-      ra = 0;
-      rx = t / TY;
-      ry = 1 + t % TY;
-    } else if (t < BW_ROWS0 + BW_ROWS1) {
-      ra = 1;
-      rx = 1 + (t - BW_ROWS0) / (TY + 1);
-      ry = (t - BW_ROWS0) % (TY + 1);
-    } else if (t < BW_ROWS) {
-      ra = 2;
-      rx = 1 + (t - BW_ROWS0 - BW_ROWS1) / TY;
-      ry = 1 + (t - BW_ROWS0 - BW_ROWS1) % TY;
-    }
-    if (ra >= 0) {
-      const RowBits r = rb[rx][ry];
-      const uint32_t lo = ra == 0 ? r.xc : (ra == 1 ? r.yc : r.zc);
-      bits = (uint64_t)lo | ((uint64_t)((f32[rx][ry] >> ra) & 1) << TZ);
-      if (ra < 2) bits &= ~1ull;  // x / y edges of cell Z0 touch no point of the tile
-    }
-  }
-  uint32_t tot;
-  const uint32_t off = block_excl_scan((uint32_t)__popcll((long long)bits), wsum, tot);
-  if (threadIdx.x == 0) {
-    aoff[0] = 0;
-    aoff[3] = tot;
-  }
-  if (threadIdx.x == BW_ROWS0) aoff[1] = off;
-  if (threadIdx.x == BW_ROWS0 + BW_ROWS1) aoff[2] = off;
-  if (ra >= 0) put_items(items, off, bits, rx, ry, ra);
-  __syncthreads();
-
-  S scale[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) scale[k] = normalize ? S(1) / S(g.n[k] - 1) : S(1);
+  // edge along a owned by window cell (x, y, j): crossing?  and its index
   auto crossing = [&](int x, int y, int j, int a) -> int {
     return j == TZ ? (f32[x][y] >> a) & 1 : (row_flags(rb[x][y], j) >> a) & 1;
   };
-  S acc[TX][4];
-#pragma unroll
-  for (int ix = 0; ix < TX; ++ix) acc[ix][0] = acc[ix][1] = acc[ix][2] = acc[ix][3] = S(0);
+  auto eid = [&](int x, int y, int j, int a) -> int64_t {
+    if (j == TZ) return (int64_t)b1[x][y] + __popc(f32[x][y] & ((1 << a) - 1));
+    const RowBits r = rb[x][y];
+    return (int64_t)b0[x][y] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
+  };
 #pragma unroll 1
-  for (int a = 0; a < 3; ++a) {
-    for (uint32_t i = aoff[a] + threadIdx.x; i < aoff[a + 1]; i += blockDim.x) {
-      int x, y, j, ia;
-      item_decode(items[i], x, y, j, ia);
-      S gvec[3];
-      if constexpr (METHOD == MC) {
-        const int64_t v = j == TZ ? (int64_t)b1[x][y] + __popc(f32[x][y] & ((1 << a) - 1))
-                                  : (int64_t)b0[x][y] + row_prefix(rb[x][y], j) +
-                                        __popc(row_flags(rb[x][y], j) & ((1 << a) - 1));
-        load_grad<S>(gv, v, scale, gvec);
-      } else {
-        gvec[0] = gvec[1] = gvec[2] = S(0);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int db = k & 1, dc = k >> 1;
-          // the cell one step back along the two other axes (b, c) = (a+1, a+2) mod 3
-          const int cx = x - (a == 1 ? dc : (a == 2 ? db : 0));
-          const int cy = y - (a == 0 ? db : (a == 2 ? dc : 0));
-          const int cz = j - (a == 0 ? dc : (a == 1 ? db : 0));
-          const int start = (x - cx) | ((y - cy) << 1) | ((j - cz) << 2);
-          const uint64_t w = dmc_case(rc[cx][cy][cz]);
-          const int p = dmc_patch_of(w, g_edge_of[3 * start + a]);
-          const S inv = S(1) / S(dmc_patch_size(w, p));
-          const int64_t pid = (int64_t)(cz == TZ ? b1[cx][cy] : b0[cx][cy]) + pre[cx][cy][cz] + (exact ? p : 0);
-          S v[3];
-          load_grad<S>(gv, pid, scale, v);
-          gvec[0] += v[0] * inv;
-          gvec[1] += v[1] * inv;
-          gvec[2] += v[2] * inv;
-        }
-      }
-      S c0[4], c1[4];
-      edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
-      if (x >= 1 && y >= 1 && j >= 1) {
-        S* s0 = slot + 4 * (((x - 1) * TY + (y - 1)) * TZ + (j - 1));
-#pragma unroll
-        for (int k = 0; k < 4; ++k) s0[k] = c0[k];
-      }
-      const int x1 = x + (a == 0), y1 = y + (a == 1), j1 = j + (a == 2);
-      if (x1 <= TX && y1 <= TY && j1 <= TZ) {
-        S* s1 = slot + 4 * (NP + ((x1 - 1) * TY + (y1 - 1)) * TZ + (j1 - 1));
-#pragma unroll
-        for (int k = 0; k < 4; ++k) s1[k] = c1[k];
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ix = 0; ix < TX; ++ix) {
-      const int x = ix + 1, y = warp + 1, j = lane + 1;
-      const int p = (ix * TY + warp) * TZ + lane;
-      if (crossing(x, y, j, a)) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[ix][k] += slot[4 * p + k];
-      }
-      if (crossing(x - (a == 0), y - (a == 1), j - (a == 2), a)) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[ix][k] += slot[4 * (NP + p) + k];
-      }
-    }
-    __syncthreads();
-  }
-#pragma unroll
   for (int ix = 0; ix < TX; ++ix) {
+    const int x = ix + 1, y = warp + 1, j = lane + 1;
+    S acc[4] = {S(0), S(0), S(0), S(0)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      // the edge from this point along a (first point), then the edge ending here
+      if (crossing(x, y, j, a)) add_adj<S>(adj, eid(x, y, j, a), 0, acc);
+      const int xb = x - (a == 0), yb = y - (a == 1), jb = j - (a == 2);
+      if (crossing(xb, yb, jb, a)) add_adj<S>(adj, eid(xb, yb, jb, a), 1, acc);
+    }
     const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
-    if (!f.inside(X, Y, Z)) continue;
-    const int64_t i = f.lin(X, Y, Z);
-    gsdf[i] = acc[ix][0];
-    if (gdef) {
-      gdef[3 * i + 0] = acc[ix][1];
-      gdef[3 * i + 1] = acc[ix][2];
-      gdef[3 * i + 2] = acc[ix][3];
+    if (f.inside(X, Y, Z)) {
+      const int64_t i = f.lin(X, Y, Z);
+      gsdf[i] = acc[0];
+      if (gdef) {
+        gdef[3 * i + 0] = acc[1];
+        gdef[3 * i + 1] = acc[2];
+        gdef[3 * i + 2] = acc[3];
+      }
     }
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
-template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS) backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                            const uint8_t* __restrict__ tile_flag,
-                                                            const S* __restrict__ gv, int normalize, int exact,
-                                                            S* __restrict__ gsdf, S* __restrict__ gdef) {
-  backward_tile<S, METHOD>(f, g, seg, tile_flag, blockIdx.x, gv, normalize, exact, gsdf, gdef);
+template <class S>
+__global__ void __launch_bounds__(NTHREADS) gather_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                          const uint8_t* __restrict__ tile_flag,
+                                                          const void* __restrict__ record, S* __restrict__ gsdf,
+                                                          S* __restrict__ gdef) {
+  gather_tile<S>(f, g, seg, tile_flag, blockIdx.x, (const S*)record, gsdf, gdef);
 }
 
 // ------------------------------------------------------------------ batch emit / backward
 
+// MC: low half = vertices, high half = triangles; DMC: low = quads, high = patches
+template <int METHOD>
+__device__ __forceinline__ int64_t count_verts(uint64_t v) {
+  return METHOD == MC ? Counts::lo(v) : Counts::hi(v);
+}
+template <int METHOD>
+__device__ __forceinline__ int64_t count_faces(uint64_t v) {
+  return METHOD == MC ? Counts::hi(v) : Counts::lo(v);
+}
+
+// whether grid G's outputs fit the batch's capacities (vcap vertices, fcap faces)
+template <class S, int METHOD>
+__device__ __forceinline__ bool batch_fits(const BatchGrid<S>& G, int64_t vcap, int64_t fcap) {
+  const uint64_t b1 = *G.seg_end;
+  return count_verts<METHOD>(b1) <= vcap && count_faces<METHOD>(b1) <= fcap;
+}
+
 // Emit every active tile of a batch (persistent).  Outputs are concatenated in grid
 // order; faces hold grid-local vertex ids.  When a grid's outputs would pass the
 // capacities (vcap vertices, fcap faces) the grid is skipped and bit 1 of
-// stats[0].error is set; the host then retries with larger buffers.
+// stats[0].error is set; the host then retries with larger buffers.  The edge
+// record (optional) is laid out for the capacities.
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS) batch_emit_kernel(const BatchGrid<S>* __restrict__ grids,
                                                               const int* __restrict__ active,
                                                               const unsigned long long* __restrict__ n_active,
                                                               S* __restrict__ verts, int64_t* __restrict__ faces,
                                                               int64_t vcap, int64_t fcap, int normalize,
-                                                              Stats* stats) {
+                                                              Stats* stats, EdgeRecord<S> rec) {
   const int64_t n = (int64_t)*n_active;
 #pragma unroll 1
   for (int64_t t = blockIdx.x; t < n; t += gridDim.x) {
     const int code = active[t];
     const int i = (int)((unsigned)code >> BATCH_TILE_BITS), tile = code & ((1 << BATCH_TILE_BITS) - 1);
     const BatchGrid<S>& G = grids[i];
-    const uint64_t b0 = *G.seg, b1 = *G.seg_end;
-    // MC: low half = vertices, high half = triangles; DMC: low = quads, high = patches
-    const int64_t v0 = METHOD == MC ? Counts::lo(b0) : Counts::hi(b0);
-    const int64_t v1 = METHOD == MC ? Counts::lo(b1) : Counts::hi(b1);
-    const int64_t f1 = METHOD == MC ? Counts::hi(b1) : Counts::lo(b1);
-    if (v1 > vcap || f1 > fcap) {
+    if (!batch_fits<S, METHOD>(G, vcap, fcap)) {
       if (threadIdx.x == 0) atomicOr(&stats->error, 2ull);
       continue;
     }
+    const int64_t v0 = count_verts<METHOD>(*G.seg);
     if (METHOD == MC)
-      mc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0);
+      mc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0, rec);
     else
-      dmc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0);
+      dmc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0, rec);
   }
 }
 
-// dL/dsdf and dL/ddeform of every grid of a batch (persistent over the flattened
-// point tiles); dL/dverts is the concatenated [total vertices, 3] array.
+// edge pass over every edge of a batch (persistent); grids that did not fit the
+// capacities were not emitted and are skipped
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS) batch_backward_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
-                                                                  int64_t ntiles, const S* __restrict__ gv,
-                                                                  int normalize, int exact) {
+__global__ void __launch_bounds__(256) batch_edge_adjoint_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                                 EdgeRecord<S> r, int64_t vcap, int64_t fcap,
+                                                                 const S* __restrict__ gv, int normalize,
+                                                                 int exact) {
+  __shared__ int64_t estart[MAX_BATCH], vstart[MAX_BATCH];
+  __shared__ uint8_t fits[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) {
+    const uint64_t b0 = *grids[i].seg;
+    estart[i] = Counts::lo(b0);
+    vstart[i] = count_verts<METHOD>(b0);
+    fits[i] = batch_fits<S, METHOD>(grids[i], vcap, fcap) ? 1 : 0;
+  }
+  __syncthreads();
+  const int64_t E = Counts::lo(*grids[ngrids - 1].seg_end);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < E; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = batch_find(estart, ngrids, q);
+    if (!fits[i]) continue;
+    const BatchGrid<S>& G = grids[i];
+    S scale[3];
+    grad_scale<S>(G.g, normalize, scale);
+    edge_adjoint_at<S, METHOD>(G.f, r, q, vstart[i], gv, scale, exact);
+  }
+}
+
+// point pass over the flattened point tiles of a batch (persistent); the grids
+// that did not fit the capacities get zero gradients
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS) batch_gather_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                                int64_t ntiles, const void* __restrict__ record,
+                                                                int64_t vcap, int64_t fcap) {
   __shared__ int64_t start[MAX_BATCH];
-  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].ptile0;
+  __shared__ uint8_t fits[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) {
+    start[i] = grids[i].ptile0;
+    fits[i] = batch_fits<S, METHOD>(grids[i], vcap, fcap) ? 1 : 0;
+  }
   __syncthreads();
 #pragma unroll 1
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int i = batch_find(start, ngrids, t);
     const BatchGrid<S>& G = grids[i];
-    backward_tile<S, METHOD>(G.f, G.g, G.seg, G.tile_flag, t - start[i], gv, normalize, exact, G.gsdf, G.gdef);
+    if (fits[i]) {
+      gather_tile<S>(G.f, G.g, G.seg, G.tile_flag, t - start[i], (const S*)record, G.gsdf, G.gdef);
+    } else {
+      int x0, y0, z0;
+      ptile_coords(t - start[i], G.g, x0, y0, z0);
+      zero_ptile<S>(G.f, G.gsdf, G.gdef, x0, y0, z0);
+    }
   }
 }
 

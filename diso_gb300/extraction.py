@@ -9,9 +9,11 @@ Differences that are invisible to callers of the reference API:
 * the empty-surface guard (diso/__init__.py:49, 103) reuses the min/max that the
   counting kernel computes, so a forward synchronises with the host once (the
   reference syncs for min, max and three output sizes);
-* the backward does not re-run the forward (diso/__init__.py:32, 86): it
-  recomputes crossings, codes and vertex indices from the SDF inside one kernel
-  that writes every gradient element once, deterministically (no atomics);
+* the backward does not re-run the forward (diso/__init__.py:32, 86): the
+  forward records every crossing edge (its cell and axis, for DMC the patches
+  around it) when a gradient will be wanted; the backward computes each edge's
+  adjoint once and then writes every gradient element once, deterministically
+  (no atomics);
 * vertices are shifted and normalised, and faces written as int64, inside the
   kernels; the DMC quad split runs on the GPU in one pass plus a scan.
 
@@ -65,8 +67,12 @@ class _ExtractFunction(Function):
         width = 3 if ex.method == N.MC else 4
         verts = torch.empty((nv, 3), dtype=g.dtype, device=g.device)
         faces = torch.empty((nf, width), dtype=torch.int64, device=g.device)
+        # the edge record only when a gradient can be asked for
+        wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        record = (torch.empty(max(1, ex.record_slots(counts)), dtype=torch.int64, device=g.device)
+                  if wants_grad else None)
         _mark("emit", "start")
-        ex.emit(g, d, iso, pad, seg, normalize, verts, faces)
+        ex.emit(g, d, iso, pad, seg, normalize, verts, faces, record)
         _mark("emit", "end")
         if ex.method == N.DMC and not return_quads:
             tris = torch.empty((2 * nf, 3), dtype=torch.int64, device=g.device)
@@ -77,13 +83,14 @@ class _ExtractFunction(Function):
         ctx.ex = ex
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
         ctx.has_deform = deform is not None
-        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg)
+        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg,
+                              record if record is not None else seg.new_empty(0))
         ctx.mark_non_differentiable(faces)
         return verts, faces
 
     @staticmethod
     def backward(ctx, grad_verts, grad_faces):
-        grid, deform, seg = ctx.saved_tensors
+        grid, deform, seg, record = ctx.saved_tensors
         g = grid.detach().contiguous()
         d = deform.detach().contiguous() if ctx.has_deform else None
         with torch.cuda.device(g.device):
@@ -93,7 +100,7 @@ class _ExtractFunction(Function):
             gs = torch.empty_like(g)
             gd = torch.empty_like(d) if d is not None else None
             _mark("backward", "start")
-            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, ctx.normalize, gv, gs, gd, ctx.exact_grad)
+            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad)
             _mark("backward", "end")
         return gs, gd, None, None, None, None, None, None, None, None
 

@@ -131,12 +131,13 @@ class Worker(threading.Thread):
             width = 3 if method == N.MC else 4
             verts = torch.empty((nv, 3), dtype=srv.dtype, device=dev)
             faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
-            bx.emit(batch[0].normalize, verts, faces, dev)
+            edges = bx.edge_record(nv, nf, dev)
+            bx.emit(batch[0].normalize, verts, faces, dev, edges)
             gv = torch.empty_like(verts)
             for i, (r, x) in enumerate(zip(batch, ins)):
                 v0, c = int(res.voff[i]), res.counts[i]
                 gv[v0:v0 + c.n_verts] = x[2](c.n_verts)
-            bx.backward(batch[0].normalize, False, gv, dev)
+            bx.backward(batch[0].normalize, False, gv, edges, nv, nf, dev)
             self.stream.synchronize()
             t = srv.now()
             for i, r in enumerate(batch):

@@ -21,9 +21,11 @@
  * sizes (one device-to-host copy, the only synchronisation of the forward);
  * the caller then allocates verts/faces and calls diso_forward_emit with the
  * same inputs and `seg`.  `seg` (diso_segment_slots() uint64 values: the
- * scanned per-segment counts, their total and one activity byte per tile) is all
- * the per-call state: keep it to run diso_backward later; the backward recomputes
- * every crossing, case code and vertex index from the SDF.
+ * scanned per-segment counts, their total and one activity byte per tile) and,
+ * when gradients will be wanted, the edge record that diso_forward_emit fills
+ * (diso_edge_record_slots() uint64 values: every crossing edge's cell and axis,
+ * for DMC the patches around it, and room for the backward's per-edge adjoints)
+ * are all the per-call state: keep both to run diso_backward later.
  *
  * An extractor owns small scratch buffers (scan look-back state, the list of
  * tiles with crossings, status words) that grow on demand; calls on one
@@ -83,13 +85,20 @@ int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int 
 
 /* Forward, phase 2: writes verts [n_verts][3] (grid dtype) and faces as int64
  * [n_faces][3] (MC) or [n_faces][4] (DMC quads).  deform may be NULL.
+ * edge_record (32-byte aligned, diso_edge_record_slots() uint64 values) is filled
+ * for a later diso_backward; pass NULL when no gradient will be taken.
  * Replaces create_cell_mc_verts / create_cell_mc_tris (src/cumc.cu:370-410, 564-649),
  * index_cell_mc_verts / create_dmc_verts / create_quads (src/cudualmc.cu:753-794,
  * 907-955, 1027-1056), the outputs' clone (src/pybind.cpp:78-87, 271-280) and the
  * shift / normalisation (diso/__init__.py:56-60). */
 int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
                       double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
-                      int64_t* faces, void* stream);
+                      int64_t* faces, uint64_t* edge_record, void* stream);
+
+/* uint64 slots of the edge record of a forward with these counts (diso_counts.n_verts,
+ * .n_faces); 0 on bad input.  No counterpart in the reference, whose backward re-runs
+ * the forward (diso/__init__.py:32, 86). */
+int64_t diso_edge_record_slots(int method, int dtype, int64_t n_verts, int64_t n_faces);
 
 /* DMC quads -> triangles: for each quad the triangle pair with the smaller largest
  * corner cosine, config (0,1,3),(1,2,3) first for all quads that pick it, then
@@ -101,7 +110,9 @@ int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads
 
 /* Backward: dL/dsdf [nx][ny][nz] and dL/ddeform [nx][ny][nz][3] (when deform is
  * not NULL) from dL/dverts [n_verts][3] of the final (shifted, normalised)
- * vertices.  Every element of both outputs is written; nothing needs zeroing.
+ * vertices, with the `seg` and the edge record of the forward (the record's
+ * adjoint slots are overwritten).  Every element of both outputs is written;
+ * nothing needs zeroing; the result is deterministic (no atomics).
  * flags = 0 reproduces the reference's gradients exactly, including its DMC
  * backward, which hands every patch of a multi-patch cell the gradient of the
  * cell's first patch (src/cudualmc.cu:990); flags = DISO_GRAD_EXACT gives the
@@ -110,8 +121,8 @@ int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads
  * 84-98: the forward re-run, the zero fills and the F.pad backward) and
  * CuMC::backward / CUDualMC::backward (src/cumc.cu:734-743, src/cudualmc.cu:1130-1138). */
 int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
-                  double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
-                  void* grad_sdf, void* grad_deform, void* stream);
+                  double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
+                  const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
 
 /* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
  * device memory: code running while a stream is being captured, where cudaMalloc
@@ -170,13 +181,17 @@ int diso_batch_results(diso_extractor* ex, diso_counts* per_grid, int64_t* vert_
 
 /* Emit every grid into concatenated verts [vcap][3] and faces [fcap][3] (MC) or [fcap][4]
  * (DMC quads); faces hold grid-local vertex ids.  A grid whose outputs would pass the
- * capacities is skipped and reported through diso_batch_results. */
+ * capacities is skipped and reported through diso_batch_results.  edge_record (32-byte
+ * aligned, diso_edge_record_slots(method, dtype, vcap, fcap) slots, or NULL without a
+ * backward) is filled for diso_batch_backward. */
 int diso_batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
-                    void* stream);
+                    uint64_t* edge_record, void* stream);
 
-/* Backward of every grid from the concatenated dL/dverts; writes each grid's grad_sdf and
- * grad_deform (flags as for diso_backward). */
-int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, void* stream);
+/* Backward of every grid of the prepared batch from the concatenated dL/dverts, with the
+ * edge record and the capacities of its diso_batch_emit; writes each grid's grad_sdf and
+ * grad_deform (flags as for diso_backward).  Grids that the emit skipped get zero gradients. */
+int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, uint64_t* edge_record,
+                        int64_t vcap, int64_t fcap, void* stream);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* diso_last_error(void);

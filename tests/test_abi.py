@@ -72,6 +72,31 @@ def test_segment_slots(lib):
     assert lib.diso_segment_slots(0, 5, 7) == 0
 
 
+def test_edge_record_slots(lib):
+    # adjoints (8 values per edge, in 8-byte slots), then for DMC 4 int32 patch ids per
+    # edge, then the packed edge locations, then for DMC one byte per vertex
+    mc, dmc, f32, f64 = 0, 1, 0, 1
+    assert lib.diso_edge_record_slots(mc, f32, 10, 7) == 10 * 4 + 10
+    assert lib.diso_edge_record_slots(mc, f64, 10, 7) == 10 * 8 + 10
+    assert lib.diso_edge_record_slots(dmc, f32, 10, 7) == 7 * 4 + 7 * 2 + 7 + 2
+    assert lib.diso_edge_record_slots(dmc, f64, 9, 7) == 7 * 8 + 7 * 2 + 7 + 2
+    assert lib.diso_edge_record_slots(2, f32, 10, 7) == 0
+    assert lib.diso_edge_record_slots(mc, f32, -1, 7) == 0
+
+
+def test_backward_needs_an_aligned_edge_record(lib):
+    h = ctypes.c_void_p()
+    assert lib.diso_create(1, 0, ctypes.byref(h)) == 0
+    p = ctypes.c_void_p(4096)
+    args = (h, p, None, 4, 4, 4, 0.0, 1.0, p)
+    tail = (1, 0, p, p, None, None)
+    assert lib.diso_backward(*args, None, *tail) == 1
+    assert b"null edge record" in lib.diso_last_error()
+    assert lib.diso_backward(*args, ctypes.c_void_p(4096 + 8), *tail) == 1
+    assert b"32-byte aligned" in lib.diso_last_error()
+    lib.diso_destroy(h)
+
+
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     from diso_gb300 import _native
 
