@@ -692,6 +692,19 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
 
 // ------------------------------------------------------------------ DMC emit
 
+// Edge window of a DMC tile: the cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ] own
+// every edge of the tile's cells.  Their crossing edges get window slots in
+// (row, cell, axis) order; when they fit, each one's lerp vertex is computed once
+// into shared memory and the dual vertices read it from there (a tile's cells share
+// most of their edges).  Tiles with more crossing edges compute them per patch.
+constexpr int EW_ROWS = (TX + 1) * (TY + 1);
+constexpr int EW_ITEMS = EW_ROWS * 3 * (TZ + 1);
+constexpr int EPOS_BYTES = 24576;
+template <class S>
+__host__ __device__ constexpr int epos_cap() {
+  return EPOS_BYTES / (3 * (int)sizeof(S));
+}
+
 // One active tile: its dual vertices and quads; patch ids written into quads are
 // reduced by vsub (as in mc_emit_tile).
 template <class S>
@@ -699,28 +712,38 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
                                               int tile, S* __restrict__ verts, int64_t* __restrict__ quads,
                                               int normalize, int64_t vsub, const EdgeRecord<S>& rec) {
   constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
-  constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
+  constexpr int CX = TX + 1, CY = TY + 1;  // code rows: cells [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
+  constexpr int CAP = epos_cap<S>();
   __shared__ uint64_t m[WX][WY];
   __shared__ uint8_t rc[CX][CY][TZ + 1];  // resolved codes; z index j+1 for cell Z0+j, 0 for Z0-1
   __shared__ int16_t pp[CX][CY][TZ + 1];  // first patch of the cell inside its segment
   __shared__ uint32_t pb[CX][CY];
   __shared__ uint32_t qb[TX][TY];
-  __shared__ uint16_t qitems[EMIT_ITEMS];
+  __shared__ RowBits wb[TX + 1][TY + 1];  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
+  __shared__ uint8_t w32[TX + 1][TY + 1];  // crossing flags of the row's cell Z0 + TZ
+  __shared__ uint16_t wbase[TX + 1][TY + 1];
+  __shared__ uint16_t witems[EW_ITEMS];
   __shared__ uint16_t citems[TX * TY * TZ];
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
-  __shared__ uint32_t nqi, nci;
+  __shared__ uint32_t nwi, nci;
+  __shared__ __align__(16) S epos[CAP][3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
   const int WX0 = X0 - 1, WY0 = Y0 - 1;
+  // segment bases first, so that their loads overlap the mask loads
+  uint64_t sv = 0;
+  const int sy = threadIdx.x % CY, sx = threadIdx.x / CY;
+  if (threadIdx.x < CX * CY) {
+    const int X = X0 - 1 + sx, Y = Y0 - 1 + sy;
+    if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) sv = seg[g.seg(X, Y, tz)];
+  }
   S dmn, dmx;
   bool dseen = false;
   load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
-  for (int i = threadIdx.x; i < CX * CY; i += blockDim.x) {
-    const int y = i % CY, x = i / CY, X = X0 - 1 + x, Y = Y0 - 1 + y;
-    const uint64_t s = (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) ? seg[g.seg(X, Y, tz)] : 0ull;
-    pb[x][y] = Counts::hi(s);
-    if (x >= 1 && y >= 1) qb[x - 1][y - 1] = Counts::lo(s);
+  if (threadIdx.x < CX * CY) {
+    pb[sx][sy] = Counts::hi(sv);
+    if (sx >= 1 && sy >= 1) qb[sx - 1][sy - 1] = Counts::lo(sv);
   }
   __syncthreads();
   const uint32_t valid = zvalid(g, Z0);
@@ -747,45 +770,66 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
       pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
     }
   }
-  // work lists of the own rows: crossing edges (quads) and non-trivial cells (dual vertices)
-  uint32_t cq = 0, cc = 0;
-  RowBits own = {0u, 0u, 0u, 0u};
-  const int ox = threadIdx.x / TY, oy = threadIdx.x % TY;
-  if (threadIdx.x < TX * TY && X0 + ox < g.c[0] && Y0 + oy < g.c[1]) {
-    own = row_bits(m[ox + 1][oy + 1], m[ox + 2][oy + 1], m[ox + 1][oy + 2], m[ox + 2][oy + 2], valid);
-    cq = __popc(own.xc) + __popc(own.yc) + __popc(own.zc);
-    cc = __popc(own.nt);
+  // edge rows: crossing edges (window items) and, for the own rows, the non-trivial
+  // cells (dual vertex items)
+  uint32_t ce = 0, cc = 0;
+  RowBits w = {0u, 0u, 0u, 0u};
+  int fl32 = 0;
+  const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
+  if (threadIdx.x < EW_ROWS && X0 + ex_ < g.c[0] && Y0 + ey < g.c[1]) {
+    const uint64_t a = m[ex_ + 1][ey + 1], b = m[ex_ + 2][ey + 1], c = m[ex_ + 1][ey + 2], d = m[ex_ + 2][ey + 2];
+    w = row_bits(a, b, c, d, valid);
+    if (Z0 + TZ < g.c[2]) fl32 = flags_at(a, b, c, TZ + 1);
+    ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(fl32);
+    if (ex_ < TX && ey < TY) cc = __popc(w.nt);
   }
   uint32_t tot;
-  const uint32_t off = block_excl_scan(cq | (cc << 16), wsum, tot);
+  const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
   if (threadIdx.x == 0) {
-    nqi = tot & 0xffffu;
-    nci = tot >> 16;
+    nwi = tot & 0x1fffu;
+    nci = tot >> 13;
   }
-  if (threadIdx.x < TX * TY) {
-    uint32_t o = off & 0xffffu;
-    uint32_t b = own.xc | own.yc | own.zc;
-    while (b) {
-      const int j = __ffs(b) - 1;
-      b &= b - 1;
-      const int fl = row_flags(own, j);
+  if (threadIdx.x < EW_ROWS) {
+    wb[ex_][ey] = w;
+    w32[ex_][ey] = (uint8_t)fl32;
+    uint32_t o = off & 0x1fffu;
+    wbase[ex_][ey] = (uint16_t)o;
+    // window items in slot order: cells ascending, axes ascending per cell
+    uint32_t bits = w.xc | w.yc | w.zc;
+    while (bits) {
+      const int j = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int fl = row_flags(w, j);
 #pragma unroll
       for (int a = 0; a < 3; ++a)
-        if (fl & (1 << a)) qitems[o++] = item_code(ox, oy, j, a);
+        if (fl & (1 << a)) witems[o++] = item_code(ex_, ey, j, a);
     }
-    put_items(citems, off >> 16, own.nt, ox, oy, 0);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      if (fl32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
+    if (ex_ < TX && ey < TY) put_items(citems, off >> 13, w.nt, ex_, ey, 0);
   }
   __syncthreads();
-  // quads: one per crossing edge owned by the cell (src/cudualmc.cu:753-794, 1019-1056);
+  const bool cached = nwi <= (uint32_t)CAP;
+  // window edges: lerp vertices into the cache; the tile's own edges also give its quads
+  // (one per crossing edge owned by a tile cell, src/cudualmc.cu:753-794, 1019-1056);
   // the edge exits (value falls through iso) when its start point is >= iso
-  for (uint32_t i = threadIdx.x; i < nqi; i += blockDim.x) {
+  for (uint32_t i = threadIdx.x; i < nwi; i += blockDim.x) {
     int ix, iy, j, a;
-    item_decode(qitems[i], ix, iy, j, a);
-    const int x = ix + 1, y = iy + 1;  // window cell / mask row of the own row
-    const RowBits r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+    item_decode(witems[i], ix, iy, j, a);
+    if (cached) {
+      S p[3];
+      edge_vertex<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+      epos[i][0] = p[0];
+      epos[i][1] = p[1];
+      epos[i][2] = p[2];
+    }
+    if (ix >= TX || iy >= TY || j >= TZ) continue;
+    const int x = ix + 1, y = iy + 1;  // code row / mask row of the own row
+    const RowBits& r = wb[ix][iy];
     const int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
     const int type = a + 3 * (int)((m[x][y] >> (j + 1)) & 1);
-    int rid[4];
+    int4 rid = make_int4(0, 0, 0, 0);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int q = g_dmc_quad[4 * type + k];
@@ -795,13 +839,25 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
       quads[4 * qid + k] = id;
       // the record orders the cells by their steps back (db, dc) along axes a+1, a+2
       const int db = -(a == 0 ? oy : (a == 1 ? oz : ox)), dc = -(a == 0 ? oz : (a == 1 ? ox : oy));
-      rid[db + 2 * dc] = (int)id;
+      const int at = db + 2 * dc;
+      rid.x = at == 0 ? (int)id : rid.x;
+      rid.y = at == 1 ? (int)id : rid.y;
+      rid.z = at == 2 ? (int)id : rid.z;
+      rid.w = at == 3 ? (int)id : rid.w;
     }
     if (rec.loc) {
       rec.loc[qid] = pack_loc(X0 + ix, Y0 + iy, Z0 + j, a);
-      reinterpret_cast<int4*>(rec.ids)[qid] = make_int4(rid[0], rid[1], rid[2], rid[3]);
+      reinterpret_cast<int4*>(rec.ids)[qid] = rid;
     }
   }
+  __syncthreads();
+  // window slot of the edge along a owned by edge-row cell (x, y, j), j in [0, TZ]
+  auto wslot = [&](int x, int y, int j, int a) -> int {
+    const RowBits r = wb[x][y];
+    if (j == TZ)
+      return wbase[x][y] + __popc(r.xc) + __popc(r.yc) + __popc(r.zc) + __popc(w32[x][y] & ((1 << a) - 1));
+    return wbase[x][y] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
+  };
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
   // (create_dmc_verts_kernel, src/cudualmc.cu:907-955)
   for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
@@ -809,8 +865,8 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     item_decode(citems[i], ix, iy, j, a);
     const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
     const int code = rc[x][y][j + 1];
-    const uint64_t w = dmc_case(code);
-    const int np = dmc_npatch(w);
+    const uint64_t wc = dmc_case(code);
+    const int np = dmc_npatch(wc);
     S acc[4][3];
     int cnt[4] = {0, 0, 0, 0};
 #pragma unroll
@@ -819,9 +875,16 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     for (int e = 0; e < 12; ++e) {
       const int ge = g_edge[e], s = ge & 7, ax = ge >> 3;
       if ((((code >> s) ^ (code >> (s | (1 << ax)))) & 1) == 0) continue;
-      const int p = dmc_patch_of(w, e);
+      const int p = dmc_patch_of(wc, e);
       S v[3];
-      edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
+      if (cached) {
+        const int k = wslot(ix + (s & 1), iy + ((s >> 1) & 1), j + ((s >> 2) & 1), ax);
+        v[0] = epos[k][0];
+        v[1] = epos[k][1];
+        v[2] = epos[k][2];
+      } else {
+        edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q)
         if (q == p) {
