@@ -1,5 +1,6 @@
 // Host side of the C ABI declared in include/diso_gb300.h: argument checks,
 // scratch management and kernel launches on the caller's stream.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -48,6 +49,7 @@ struct diso_extractor {
   int64_t split_cap = 0;
   int64_t last_active = 0;       // from the last forward count
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
+  int tma_ctas = 0;              // the same for the TMA count kernel
   int sms = 0;
 
   // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
@@ -104,6 +106,64 @@ int grow(T*& p, int64_t& cap, int64_t need) {
   return DISO_OK;
 }
 
+// ------------------------------------------------------------------ TMA tensor maps
+
+// cuTensorMapEncodeTiled from the driver, looked up once
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+// Tensor maps of the SDF for the TMA count: full boxes (32 x 33 x 9 points, z
+// innermost) and the 4-deep boxes below / above a unit.  False when the SDF cannot
+// be described (address not 16-byte aligned, rows not a multiple of 16 bytes).
+template <class S>
+bool count_tensor_maps(const void* sdf, int nx, int ny, int nz, CUtensorMap* wide, CUtensorMap* narrow) {
+  if (((uintptr_t)sdf & 15u) != 0 || ((int64_t)nz * (int64_t)sizeof(S)) % 16 != 0) return false;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const CUtensorMapDataType dt = sizeof(S) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const cuuint64_t dims[3] = {(cuuint64_t)nz, (cuuint64_t)ny, (cuuint64_t)nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)nz * sizeof(S), (cuuint64_t)nz * ny * sizeof(S)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint32_t wbox[3] = {32, (cuuint32_t)(CR + 1), (cuuint32_t)(CP + 1)};
+  const cuuint32_t nbox[3] = {(cuuint32_t)TBN, (cuuint32_t)(CR + 1), (cuuint32_t)(CP + 1)};
+  if (enc(wide, dt, 3, const_cast<void*>(sdf), dims, strides, wbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return false;
+  return enc(narrow, dt, 3, const_cast<void*>(sdf), dims, strides, nbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// resident CTAs per SM of the TMA count kernel (sets its shared-memory size)
+template <class S>
+cudaError_t tma_occupancy(int method, int* per_sm) {
+  const int smem = (int)count_tma_smem<S>();
+  cudaError_t e;
+  if (method == DISO_MC) {
+    if ((e = cudaFuncSetAttribute(count_tma_kernel<S, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+      return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, count_tma_kernel<S, MC>, NTHREADS, smem);
+  }
+  if ((e = cudaFuncSetAttribute(count_tma_kernel<S, DMC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
+    return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, count_tma_kernel<S, DMC>, NTHREADS, smem);
+}
+
 int bind_device(diso_extractor* ex) {
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
@@ -124,6 +184,12 @@ int bind_device(diso_extractor* ex) {
           &per_sm, ex->method == DISO_MC ? count_kernel<double, MC> : count_kernel<double, DMC>, NTHREADS, 0));
     ex->resident_ctas = sms * std::max(per_sm, 1);
     ex->sms = sms;
+    int per_tma = 0;
+    if (ex->dtype == DISO_F32)
+      CUDA_TRY(tma_occupancy<float>(ex->method, &per_tma));
+    else
+      CUDA_TRY(tma_occupancy<double>(ex->method, &per_tma));
+    ex->tma_ctas = sms * std::max(per_tma, 1);
   }
   return DISO_OK;
 }
@@ -193,15 +259,30 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
-  // persistent grid: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
-  const int64_t units = count_units(g);
-  const int64_t want =
-      std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
-  const unsigned grid = (unsigned)std::min<int64_t>(want, units);
-  if (ex->method == DISO_MC)
-    count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
-  else
-    count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
+  // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
+  CUtensorMap wide, narrow;
+  if (count_tensor_maps<S>(sdf, nx, ny, nz, &wide, &narrow)) {
+    const int64_t units = count_tma_units(g);
+    const int64_t want =
+        std::max<int64_t>(ex->tma_ctas, (units * TMA_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+    const unsigned grid = (unsigned)std::min<int64_t>(want, units);
+    const size_t smem = count_tma_smem<S>();
+    if (ex->method == DISO_MC)
+      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->stats,
+                                                           ex->active);
+    else
+      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->stats,
+                                                            ex->active);
+  } else {
+    const int64_t units = count_units(g);
+    const int64_t want =
+        std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+    const unsigned grid = (unsigned)std::min<int64_t>(want, units);
+    if (ex->method == DISO_MC)
+      count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
+    else
+      count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
+  }
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
@@ -210,6 +291,7 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   CUDA_TRY(cudaStreamSynchronize(s));
   const Stats& h = *ex->stats_host;
   if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
+  if (h.error & 4ull) return fail(DISO_ERR_SCAN, "count: wait for a TMA copy gave up");
   // the low half counts crossings, the high half triangles (MC) or patches (DMC)
   if (ex->method == DISO_MC) {
     out->n_verts = Counts::lo(total);

@@ -89,24 +89,6 @@ struct Field {
   }
 };
 
-// A box of padded points staged in shared memory, with a global-memory fallback
-// for points outside it.
-template <class S, int WX, int WY, int WZ>
-struct Window {
-  S v[WX][WY][WZ];
-  __device__ void load(const Field<S>& f, int X0, int Y0, int Z0) {
-    for (int i = threadIdx.x; i < WX * WY * WZ; i += blockDim.x) {
-      int z = i % WZ, y = (i / WZ) % WY, x = i / (WZ * WY);
-      v[x][y][z] = f.at(X0 + x, Y0 + y, Z0 + z);
-    }
-  }
-  __device__ __forceinline__ S get(const Field<S>& f, int X0, int Y0, int Z0, int X, int Y, int Z) const {
-    unsigned x = (unsigned)(X - X0), y = (unsigned)(Y - Y0), z = (unsigned)(Z - Z0);
-    if (x < (unsigned)WX && y < (unsigned)WY && z < (unsigned)WZ) return v[x][y][z];
-    return f.at(X, Y, Z);
-  }
-};
-
 // ----------------------------------------------------------------- case codes
 
 __device__ const uint64_t g_mc_tri[256] = DISO_MC_TRIANGLES;
@@ -121,55 +103,27 @@ __device__ __forceinline__ int dmc_npatch(uint64_t w) { return (int)((w >> 24) &
 __device__ __forceinline__ int dmc_patch_of(uint64_t w, int e) { return (int)((w >> (2 * e)) & 3); }
 __device__ __forceinline__ int dmc_patch_size(uint64_t w, int p) { return (int)((w >> (32 + 4 * p)) & 15); }
 
-// Morton code of a cell: bit i set when corner (i&1, i>>1&1, i>>2&1) >= iso
-// (the DMC corner order, src/cudualmc.cu:95-104)
-template <class S, class Get>
-__device__ __forceinline__ int morton_code(Get get, int X, int Y, int Z, S iso) {
-  int m = 0;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) m |= (get(X + (i & 1), Y + ((i >> 1) & 1), Z + ((i >> 2) & 1)) >= iso) << i;
-  return m;
-}
-
 // MC case code (corner order of src/cumc.cu:107) from the Morton code: swap corners 2<->3, 6<->7
 __device__ __forceinline__ int mc_from_morton(int m) {
   return (m & 0x33) | ((m & 0x44) << 1) | ((m & 0x88) >> 1);
 }
 
-// crossing flags of a cell's three owned edges (+x, +y, +z from its corner 0);
-// the reference tests (d0 < iso && d1 >= iso) || (d1 < iso && d0 >= iso)
-// (src/cumc.cu:334-339), i.e. the two corner bits differ.  Flipping all bits of a
-// code (DMC ambiguity resolution) leaves the flags unchanged.
-__device__ __forceinline__ int cross_flags(int m) {
-  return ((m ^ (m >> 1)) & 1) | (((m ^ (m >> 2)) & 1) << 1) | (((m ^ (m >> 4)) & 1) << 2);
+// The twelve cell edges (DISO_EDGE_TABLE: start corner | axis << 3, in the
+// reference's edge order), packed 5 bits each so that edge_desc(e) needs no load.
+namespace detail {
+constexpr int kEdgeTable[12] = DISO_EDGE_TABLE;
+constexpr uint64_t pack_edges(int i) {
+  return i == 12 ? 0ull : (((uint64_t)kEdgeTable[i] << (5 * i)) | pack_edges(i + 1));
 }
+}  // namespace detail
+constexpr uint64_t kEdgePack = detail::pack_edges(0);
+__device__ __forceinline__ int edge_desc(int e) { return (int)((kEdgePack >> (5 * e)) & 31); }
 
-// DMC code after the face-neighbour ambiguity test (src/cudualmc.cu:815-839):
-// a "problematic" code looks at the cell across its ambiguous face; when that
-// (raw) code is problematic too, the code is complemented.
-template <class S, class Get>
-__device__ __forceinline__ int dmc_resolve(Get get, int m, int X, int Y, int Z, const int C[3], S iso) {
-  int dir = dmc_dir(dmc_case(m));
-  if (dir != 7) {
-    int nb[3] = {X, Y, Z};
-    int comp = dir >> 1;
-    nb[comp] += (dir & 1) ? 1 : -1;
-    if (nb[comp] >= 0 && nb[comp] < C[comp]) {
-      int nm = morton_code<S>(get, nb[0], nb[1], nb[2], iso);
-      if (dmc_dir(dmc_case(nm)) != 7) m ^= 0xff;
-    }
-  }
-  return m;
-}
-
-// edge id of the cell-local edge starting at corner (sx, sy, sz) along axis a
-__device__ __forceinline__ int edge_id(int sx, int sy, int sz, int a) {
-  // inverse of DISO_EDGE_TABLE
-  const int start = sx | (sy << 1) | (sz << 2);
-#pragma unroll
-  for (int e = 0; e < 12; ++e)
-    if (g_edge[e] == (start | (a << 3))) return e;
-  return 0;
+// Bit (s + 8 a) set when the cell edge from corner s along axis a crosses (its two
+// corner bits in the Morton code differ); with desc = s | a << 3 the bit of edge e
+// is bit edge_desc(e).
+__device__ __forceinline__ uint32_t cross_bits(int m) {
+  return (uint32_t)(((m ^ (m >> 1)) & 0x55) | (((m ^ (m >> 2)) & 0x33) << 8) | (((m ^ (m >> 4)) & 0x0f) << 16));
 }
 
 // ----------------------------------------------------------------- reductions

@@ -20,6 +20,7 @@
 // handful of instructions.
 #pragma once
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace diso {
 
@@ -184,6 +185,15 @@ __device__ __forceinline__ int code8(uint64_t a, uint64_t b, uint64_t c, uint64_
   return (int)(lo | (hi << 4));
 }
 
+// Morton code of cell (X, Y, Z) from global memory
+template <class S>
+__device__ __forceinline__ int cell_code_far(const Field<S>& f, int X, int Y, int Z) {
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c |= (f.at(X + (i & 1), Y + ((i >> 1) & 1), Z + ((i >> 2) & 1)) >= f.iso) << i;
+  return c;
+}
+
 // Morton code of cell (X, Y, Z) from the masks when its corners are in the
 // window, otherwise from global memory
 template <class S, int WX, int WY>
@@ -195,10 +205,7 @@ __device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const Fiel
   const int s = Z - Z0 + 1;
   if (x < (unsigned)(WX - 1) && y < (unsigned)(WY - 1) && s >= 0 && s + 1 <= MASK_TOP)
     return code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], s);
-  int c = 0;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) c |= (f.at(X + (i & 1), Y + ((i >> 1) & 1), Z + ((i >> 2) & 1)) >= f.iso) << i;
-  return c;
+  return cell_code_far<S>(f, X, Y, Z);
 }
 
 // DMC code after the face-neighbour ambiguity test (src/cudualmc.cu:815-839):
@@ -350,13 +357,78 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
   __syncwarp();
 }
 
+// Counts of the unit's chunk tz from the masks in sh.m (complete: the caller
+// synchronised), the activity bytes of the chunk's tiles; active tiles are appended
+// (as tile | tag) to sh.list.  Ends with a block barrier.
+template <class S, int METHOD>
+__device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag, int X0,
+                                            int Y0, int tz, int tag) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Z0 = tz * TZ;
+  const int X = X0 + warp, Y = Y0 + lane;
+  uint32_t nv = 0, nf = 0;
+  if (X < g.c[0] && Y < g.c[1]) {
+    const int x = warp, y = lane;
+    const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
+    const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
+    nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
+    uint32_t nt = rw.nt;
+    while (nt) {
+      const int j = __ffs(nt) - 1;
+      nt &= nt - 1;
+      const int code = code8(a, b, c, d, j + 1);
+      if (METHOD == MC)
+        nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
+      else
+        nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g)));
+    }
+    seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
+  }
+  // a cell can emit faces / patches without owning a crossing edge (its
+  // crossings may all sit on edges owned by its +1 neighbours)
+  const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
+  if (lane == 0) sh.act[warp] = busy;
+  __syncthreads();
+  if (threadIdx.x < (CP / TX) * (CR / TY)) {
+    const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
+    const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
+    if (tx < g.tiles_x() && ty < g.tiles_y()) {
+      uint32_t any = 0;
+#pragma unroll
+      for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
+      const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
+      tile_flag[tile] = any ? 1 : 0;
+      if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
+    }
+  }
+}
+
+// row masks of chunk t - 1 from the ballots of chunk t in sh.bal and the history of
+// the lane's rows (i = lane, lane + 32 of this warp): p2 = chunk t - 2, p1 = chunk t - 1;
+// vrows: bit i = the warp's point row i lies in the grid (used rows only)
+template <class S, int METHOD>
+__device__ __forceinline__ void count_combine(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
+                                              uint32_t (&p2)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int i = lane + 32 * k, r = warp + 8 * i;
+    if (i < CRPW && r < CROWS) {
+      const uint32_t cur = sh.bal[r];
+      if (write) (&sh.m[0][0])[r] = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
+      p2[k] = p1[k];
+      p1[k] = cur;
+    }
+  }
+}
+
 // One unit: per-segment counts, activity bytes of its tiles, the grid's min / max;
 // active tiles are appended (as tile | tag) to sh.list.
 template <class S, int METHOD>
 __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
                                            Stats* stats, int64_t unit, int tag) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // a row of nzc chunks is cut into nbz near-equal runs of at most KZ chunks
   const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
   const int tz0 = (int)(unit % nbz) * kz;
@@ -379,56 +451,10 @@ __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Fie
 #pragma unroll 1
   for (int t = tz0 - 1; t <= tz1; ++t) {
     count_ballots<S, METHOD>(sh, f, t, t < tz0 ? 0xc0000000u : (t == tz1 ? 1u : 0xffffffffu), mn, mx);
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int i = lane + 32 * k, r = warp + 8 * i;
-      if (i < CRPW && r < CROWS) {
-        const uint32_t cur = sh.bal[r];
-        if (t >= tz0 + 1)
-          (&sh.m[0][0])[r] = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
-        p2[k] = p1[k];
-        p1[k] = cur;
-      }
-    }
+    count_combine<S, METHOD>(sh, t >= tz0 + 1, p1, p2);
     if (t < tz0 + 1) continue;
-    const int tz = t - 1, Z0 = tz * TZ;
     __syncthreads();
-    const int X = X0 + warp, Y = Y0 + lane;
-    uint32_t nv = 0, nf = 0;
-    if (X < g.c[0] && Y < g.c[1]) {
-      const int x = warp, y = lane;
-      const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
-      const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
-      nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
-      uint32_t nt = rw.nt;
-      while (nt) {
-        const int j = __ffs(nt) - 1;
-        nt &= nt - 1;
-        const int code = code8(a, b, c, d, j + 1);
-        if (METHOD == MC)
-          nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-        else
-          nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g)));
-      }
-      seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-    }
-    // a cell can emit faces / patches without owning a crossing edge (its
-    // crossings may all sit on edges owned by its +1 neighbours)
-    const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
-    if (lane == 0) sh.act[warp] = busy;
-    __syncthreads();
-    if (threadIdx.x < (CP / TX) * (CR / TY)) {
-      const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
-      const int tx = X0 / TX + tp, ty = Y0 / TY + tr;
-      if (tx < g.tiles_x() && ty < g.tiles_y()) {
-        uint32_t any = 0;
-#pragma unroll
-        for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
-        const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
-        tile_flag[tile] = any ? 1 : 0;
-        if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
-      }
-    }
+    count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, X0, Y0, t - 1, tag);
   }
   publish_minmax<S>(stats, mn, mx);
 }
@@ -452,6 +478,210 @@ __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, 
   const int64_t nunits = count_units(g);
 #pragma unroll 1
   for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x) count_unit<S, METHOD>(sh, f, g, seg, tile_flag, stats, u, 0);
+  count_flush<S, METHOD>(sh, &stats->n_active, active);
+}
+
+// ------------------------------------------------------------------ count through TMA
+
+// The count pass with the SDF brought into shared memory by the TMA unit: for every
+// chunk of a unit one bulk tensor copy of the box of 9 x 33 point rows x 32 points
+// (out-of-grid points arrive as zeros and are replaced by the pad value), the chunks
+// below and above a unit as boxes 4 points deep.  A ring of TMA_STAGES boxes per CTA
+// keeps copies in flight while the warps turn the previous box into ballots; the
+// counting itself is count_chunk.  Needs a 16-byte aligned SDF whose rows are a
+// multiple of 16 bytes (the tensor map's strides); otherwise count_kernel runs.
+constexpr int KZT = 8;                        // chunks per unit (at most)
+constexpr int TBN = 4;                        // depth of the boxes below / above a unit
+constexpr int TMA_STAGES = 2;
+constexpr int TMA_TILES_PER_UNIT = (CP / TX) * (CR / TY) * KZT;
+constexpr long long TMA_WAIT_CYCLES = 1ll << 32;  // about two seconds
+
+template <class S>
+__host__ __device__ constexpr int tma_box_bytes() {
+  return CROWS * 32 * (int)sizeof(S);
+}
+template <class S>
+__host__ __device__ constexpr int tma_narrow_bytes() {
+  return CROWS * TBN * (int)sizeof(S);
+}
+// dynamic shared memory of count_tma_kernel: the stages, plus room to align them to 128 bytes
+template <class S>
+__host__ __device__ constexpr size_t count_tma_smem() {
+  return (size_t)TMA_STAGES * tma_box_bytes<S>() + 128;
+}
+
+__host__ __device__ inline int64_t count_tma_units(const Geom& g) {
+  return (int64_t)((g.c[0] + CP - 1) / CP) * ((g.c[1] + CR - 1) / CR) * ((g.nzc + KZT - 1) / KZT);
+}
+
+// a position in a CTA's stream of boxes: the unit (rows from (X0, Y0), chunks
+// [tz0, tz1)) and the box's chunk t in [tz0 - 1, tz1]
+struct BoxCursor {
+  int64_t unit;
+  int X0, Y0, tz0, tz1, t;
+  __device__ void start(const Geom& g, int64_t u) {
+    const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZT - 1) / KZT, kz = (g.nzc + nbz - 1) / nbz;
+    unit = u;
+    tz0 = (int)(u % nbz) * kz;
+    const int64_t col = u / nbz;
+    X0 = (int)(col / nby) * CP;
+    Y0 = (int)(col % nby) * CR;
+    tz1 = min(tz0 + kz, g.nzc);
+    t = tz0 - 1;
+  }
+  __device__ void next(const Geom& g, int64_t nunits) {
+    if (++t > tz1) {
+      unit += gridDim.x;
+      if (unit < nunits) start(g, unit);
+    }
+  }
+  __device__ bool valid(int64_t nunits) const { return unit < nunits; }
+  // 0: a full chunk; 1: the 4 points below the unit (lanes 28..31); 2: the 4 above (lanes 0..3)
+  __device__ int kind() const { return t == tz0 - 1 ? 1 : (t == tz1 ? 2 : 0); }
+};
+
+template <class S>
+__device__ __forceinline__ void issue_box(const CUtensorMap* wide, const CUtensorMap* narrow, void* dst,
+                                          uint64_t* bar, const BoxCursor& c) {
+  const int k = c.kind();
+  if (k == 0) {
+    mbar_expect_tx(bar, (uint32_t)tma_box_bytes<S>());
+    tma_load_3d(dst, wide, bar, 32 * c.t, c.Y0 - 1, c.X0 - 1);
+  } else {
+    mbar_expect_tx(bar, (uint32_t)tma_narrow_bytes<S>());
+    tma_load_3d(dst, narrow, bar, 32 * c.t + (k == 1 ? 32 - TBN : 0), c.Y0 - 1, c.X0 - 1);
+  }
+}
+
+// ballots of chunk t from a box in shared memory (row r at box + r * width); the
+// 4-deep boxes contribute bits only (their points are counted by the unit that owns
+// their chunk), full boxes also the min / max
+template <class S, int METHOD>
+__device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Field<S>& f, const S* box, int t,
+                                            int kind, uint64_t vrows, S& mn, S& mx) {
+  constexpr int NB = 4, HALF = (CRPW + NB - 1) / NB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t used = warp + 8 * (CRPW - 1) < CROWS ? (1ull << CRPW) - 1 : (1ull << (CRPW - 1)) - 1;
+  if (kind == 0 && vrows == used && t >= 0 && 32 * t + 32 <= f.n2) {
+    // every point of the warp's rows lies in the grid: one load, compare and ballot per row
+    const S* p = box + warp * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < CRPW; ++i) {
+      if (i == CRPW - 1 && !((used >> i) & 1ull)) break;
+      const S v = p[8 * 32 * i];
+      const uint32_t b = __ballot_sync(0xffffffffu, v >= f.iso);
+      if (lane == 0) sh.bal[warp + 8 * i] = b;
+      mn = smin(mn, v);
+      mx = smax(mx, v);
+    }
+    __syncwarp();
+    return;
+  }
+  const int l0 = kind == 1 ? 32 - TBN : 0, width = kind == 0 ? 32 : TBN;
+  const int e = lane - l0;
+  const bool zin = (unsigned)e < (unsigned)width && (unsigned)(32 * t + lane) < (unsigned)f.n2;
+  const bool track = kind == 0;
+#pragma unroll
+  for (int h = 0; h < NB; ++h) {
+    S v[HALF];
+    bool in[HALF];
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      const int i = h * HALF + k, r = warp + 8 * i;
+      in[k] = zin && i < CRPW && ((vrows >> i) & 1ull);
+      const S b = box[in[k] ? r * width + e : 0];  // every read stays inside the box
+      v[k] = in[k] ? b : f.pad;
+    }
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      const int i = h * HALF + k, r = warp + 8 * i;
+      if (i < CRPW && r < CROWS) {
+        const uint32_t b = __ballot_sync(0xffffffffu, v[k] >= f.iso);
+        if (lane == 0) sh.bal[r] = b;
+      }
+      if (track && in[k]) {
+        mn = smin(mn, v[k]);
+        mx = smax(mx, v[k]);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_constant__ CUtensorMap wide,
+                                                                const __grid_constant__ CUtensorMap narrow,
+                                                                Field<S> f, Geom g, uint64_t* __restrict__ seg,
+                                                                uint8_t* __restrict__ tile_flag, Stats* stats,
+                                                                int* __restrict__ active) {
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  __shared__ CountShared<S, METHOD> sh;
+  __shared__ __align__(8) uint64_t full[TMA_STAGES];
+  unsigned char* stage_mem = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
+  const int warp = threadIdx.x >> 5;
+  const int64_t nunits = count_tma_units(g);
+  if (threadIdx.x == 0) {
+    sh.nlist = 0;
+#pragma unroll
+    for (int st = 0; st < TMA_STAGES; ++st) mbar_init(&full[st], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  BoxCursor pc, cc;  // producer (thread 0) and consumer positions
+  pc.unit = cc.unit = nunits;
+  if (blockIdx.x < nunits) {
+    pc.start(g, blockIdx.x);
+    cc = pc;
+  }
+  int64_t issued = 0;
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < TMA_STAGES && pc.valid(nunits); ++st, ++issued) {
+      issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
+      pc.next(g, nunits);
+    }
+  }
+  S mn = S(INFINITY), mx = S(-INFINITY);
+  uint32_t p1[2] = {0u, 0u}, p2[2] = {0u, 0u};
+  uint64_t vrows = 0;
+  bool failed = false;
+  int64_t k = 0;
+  for (; cc.valid(nunits); ++k) {
+    const int st = (int)(k % TMA_STAGES);
+    if (cc.t == cc.tz0 - 1) {
+      // a new unit: which of the warp's point rows lie in the grid
+      vrows = 0;
+#pragma unroll
+      for (int i = 0; i < CRPW; ++i) {
+        const int r = warp + 8 * i;
+        const int X = cc.X0 + r / (CR + 1), Y = cc.Y0 + r % (CR + 1);
+        if (r < CROWS && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1) vrows |= 1ull << i;
+      }
+    }
+    const bool ok = mbar_wait_bounded(&full[st], (uint32_t)((k / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
+    box_ballots<S, METHOD>(sh, f, reinterpret_cast<const S*>(stage_mem + st * tma_box_bytes<S>()), cc.t, cc.kind(),
+                           vrows, mn, mx);
+    count_combine<S, METHOD>(sh, cc.t >= cc.tz0 + 1, p1, p2);
+    // every warp is done with the stage (and sh.m is complete): refill the stage
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    if (threadIdx.x == 0 && pc.valid(nunits)) {
+      fence_proxy_async();
+      issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
+      pc.next(g, nunits);
+      ++issued;
+    }
+    if (cc.t >= cc.tz0 + 1) count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, cc.X0, cc.Y0, cc.t - 1, 0);
+    cc.next(g, nunits);
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicOr(&stats->error, 4ull);
+    // let the copies in flight land before the CTA's shared memory goes away
+    for (int64_t j = k; j < issued; ++j)
+      mbar_wait_bounded(&full[j % TMA_STAGES], (uint32_t)((j / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
+  }
+  publish_minmax<S>(stats, mn, mx);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
 
@@ -665,7 +895,7 @@ __device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, c
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int e = (int)((w >> (4 + 4 * (3 * t + k))) & 15);
-        const int ge = g_edge[e];
+        const int ge = edge_desc(e);
         faces[3 * (f0 + t) + k] = vid(x + (ge & 1), y + ((ge >> 1) & 1), j + ((ge >> 2) & 1), ge >> 3) - vsub;
       }
     }
@@ -722,6 +952,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   __shared__ RowBits wb[TX + 1][TY + 1];  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint8_t w32[TX + 1][TY + 1];  // crossing flags of the row's cell Z0 + TZ
   __shared__ uint16_t wbase[TX + 1][TY + 1];
+  __shared__ uint16_t cbase[TX][TY];
   __shared__ uint16_t witems[EW_ITEMS];
   __shared__ uint16_t citems[TX * TY * TZ];
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
@@ -771,43 +1002,54 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     }
   }
   // edge rows: crossing edges (window items) and, for the own rows, the non-trivial
-  // cells (dual vertex items)
-  uint32_t ce = 0, cc = 0;
-  RowBits w = {0u, 0u, 0u, 0u};
-  int fl32 = 0;
-  const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
-  if (threadIdx.x < EW_ROWS && X0 + ex_ < g.c[0] && Y0 + ey < g.c[1]) {
-    const uint64_t a = m[ex_ + 1][ey + 1], b = m[ex_ + 2][ey + 1], c = m[ex_ + 1][ey + 2], d = m[ex_ + 2][ey + 2];
-    w = row_bits(a, b, c, d, valid);
-    if (Z0 + TZ < g.c[2]) fl32 = flags_at(a, b, c, TZ + 1);
-    ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(fl32);
-    if (ex_ < TX && ey < TY) cc = __popc(w.nt);
-  }
-  uint32_t tot;
-  const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
-  if (threadIdx.x == 0) {
-    nwi = tot & 0x1fffu;
-    nci = tot >> 13;
-  }
-  if (threadIdx.x < EW_ROWS) {
-    wb[ex_][ey] = w;
-    w32[ex_][ey] = (uint8_t)fl32;
-    uint32_t o = off & 0x1fffu;
-    wbase[ex_][ey] = (uint16_t)o;
-    // window items in slot order: cells ascending, axes ascending per cell
-    uint32_t bits = w.xc | w.yc | w.zc;
-    while (bits) {
-      const int j = __ffs(bits) - 1;
-      bits &= bits - 1;
-      const int fl = row_flags(w, j);
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        if (fl & (1 << a)) witems[o++] = item_code(ex_, ey, j, a);
+  // cells (dual vertex items); row bases by a block scan, then one warp per row
+  // writes the row's items
+  {
+    uint32_t ce = 0, cc = 0;
+    RowBits w = {0u, 0u, 0u, 0u};
+    int fl32 = 0;
+    const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
+    if (threadIdx.x < EW_ROWS && X0 + ex_ < g.c[0] && Y0 + ey < g.c[1]) {
+      const uint64_t a = m[ex_ + 1][ey + 1], b = m[ex_ + 2][ey + 1], c = m[ex_ + 1][ey + 2], d = m[ex_ + 2][ey + 2];
+      w = row_bits(a, b, c, d, valid);
+      if (Z0 + TZ < g.c[2]) fl32 = flags_at(a, b, c, TZ + 1);
+      ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(fl32);
+      if (ex_ < TX && ey < TY) cc = __popc(w.nt);
     }
+    if (threadIdx.x < EW_ROWS) {
+      wb[ex_][ey] = w;
+      w32[ex_][ey] = (uint8_t)fl32;
+    }
+    uint32_t tot;
+    const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
+    if (threadIdx.x == 0) {
+      nwi = tot & 0x1fffu;
+      nci = tot >> 13;
+    }
+    if (threadIdx.x < EW_ROWS) {
+      wbase[ex_][ey] = (uint16_t)(off & 0x1fffu);
+      if (ex_ < TX && ey < TY) cbase[ex_][ey] = (uint16_t)(off >> 13);
+    }
+  }
+  __syncthreads();
+  for (int r = warp; r < EW_ROWS; r += NTHREADS / 32) {
+    const int ex_ = r / (TY + 1), ey = r % (TY + 1);
+    const RowBits w = wb[ex_][ey];
+    // window items in slot order: cells ascending, axes ascending per cell
+    const int fl = row_flags(w, lane);
+    const uint32_t before = row_prefix(w, lane);
+    uint32_t o = wbase[ex_][ey] + before;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-      if (fl32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
-    if (ex_ < TX && ey < TY) put_items(citems, off >> 13, w.nt, ex_, ey, 0);
+      if (fl & (1 << a)) witems[o++] = item_code(ex_, ey, lane, a);
+    if (lane == 31) {
+      const int f32 = w32[ex_][ey];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        if (f32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
+    }
+    if (ex_ < TX && ey < TY && ((w.nt >> lane) & 1))
+      citems[cbase[ex_][ey] + __popc(w.nt & ((1u << lane) - 1u))] = item_code(ex_, ey, lane, 0);
   }
   __syncthreads();
   const bool cached = nwi <= (uint32_t)CAP;
@@ -867,14 +1109,15 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int code = rc[x][y][j + 1];
     const uint64_t wc = dmc_case(code);
     const int np = dmc_npatch(wc);
+    const uint32_t cb = cross_bits(code);
     S acc[4][3];
     int cnt[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int p = 0; p < 4; ++p) acc[p][0] = acc[p][1] = acc[p][2] = S(0);
-#pragma unroll
+#pragma unroll 1
     for (int e = 0; e < 12; ++e) {
-      const int ge = g_edge[e], s = ge & 7, ax = ge >> 3;
-      if ((((code >> s) ^ (code >> (s | (1 << ax)))) & 1) == 0) continue;
+      const int ge = edge_desc(e), s = ge & 7, ax = ge >> 3;
+      if (((cb >> ge) & 1u) == 0) continue;
       const int p = dmc_patch_of(wc, e);
       S v[3];
       if (cached) {
@@ -908,7 +1151,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
 }
 
 template <class S>
-__global__ void __launch_bounds__(NTHREADS) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+__global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                             const int* __restrict__ active, S* __restrict__ verts,
                                                             int64_t* __restrict__ quads, int normalize,
                                                             void* record) {

@@ -48,7 +48,7 @@ enum {
   DISO_OK = 0,
   DISO_ERR_ARG = 1,      /* bad argument (size, null pointer, method, dtype) */
   DISO_ERR_CUDA = 2,     /* a CUDA call failed */
-  DISO_ERR_SCAN = 3,     /* the look-back scan gave up waiting on a predecessor */
+  DISO_ERR_SCAN = 3,     /* a bounded device-side wait gave up (scan look-back, TMA copy) */
   DISO_ERR_CAPACITY = 4, /* an output would exceed the caller's capacity */
 };
 
