@@ -50,7 +50,13 @@ struct diso_extractor {
   int64_t last_active = 0;       // from the last forward count
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
   int tma_ctas = 0;              // the same for the TMA count kernel
+  int gather_ctas = 0;           // the same for the point gather
   int sms = 0;
+  cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int* plist = nullptr;          // active point tiles of the backward, and their count
+  int64_t plist_cap = 0;
+  unsigned* plist_n = nullptr;
 
   // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
   void* bdesc = nullptr;         // device BatchGrid<S>[MAX_BATCH]
@@ -83,6 +89,16 @@ struct diso_extractor {
     cudaFree(scan_incl);
     cudaFree(active);
     cudaFree(split);
+    cudaFree(plist);
+    cudaFree(plist_n);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    side = nullptr;
+    ev_fork = ev_join = nullptr;
+    plist = nullptr;
+    plist_n = nullptr;
+    plist_cap = 0;
     stats = nullptr;
     stats_host = nullptr;
     scan_flag = nullptr;
@@ -190,6 +206,16 @@ int bind_device(diso_extractor* ex) {
     else
       CUDA_TRY(tma_occupancy<double>(ex->method, &per_tma));
     ex->tma_ctas = sms * std::max(per_tma, 1);
+    int per_g = 0;
+    if (ex->dtype == DISO_F32)
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_g, gather_list_kernel<float>, NTHREADS, 0));
+    else
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_g, gather_list_kernel<double>, NTHREADS, 0));
+    ex->gather_ctas = sms * std::max(per_g, 1);
+    CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(cudaMalloc((void**)&ex->plist_n, sizeof(unsigned)));
   }
   return DISO_OK;
 }
@@ -234,7 +260,7 @@ int check_common(diso_extractor* ex, const void* sdf, int nx, int ny, int nz) {
   return bind_device(ex);
 }
 
-// the per-call record: segment bases [nseg], the total [1], then one activity byte per forward tile
+// the per-call record: segment bases [nseg], the total [1], then two activity bytes per forward tile
 inline uint8_t* tile_flags(const uint64_t* seg, const Geom& g) { return (uint8_t*)(seg + g.nseg + 1); }
 
 template <class S>
@@ -330,6 +356,23 @@ int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx
 // CTAs of the persistent edge pass
 inline unsigned edge_ctas(const diso_extractor* ex) { return (unsigned)std::max(1, ex->sms * 8); }
 
+// CTAs of a grid-stride pass over n items of 256 threads, at most `cap`
+inline unsigned stride_ctas(int64_t n, unsigned cap) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, cap));
+}
+
+// the zeros of the inactive point tiles run on the side stream, between fork and join
+int side_fork(diso_extractor* ex, cudaStream_t s) {
+  CUDA_TRY(cudaEventRecord(ex->ev_fork, s));
+  CUDA_TRY(cudaStreamWaitEvent(ex->side, ex->ev_fork, 0));
+  return DISO_OK;
+}
+int side_join(diso_extractor* ex, cudaStream_t s) {
+  CUDA_TRY(cudaEventRecord(ex->ev_join, ex->side));
+  CUDA_TRY(cudaStreamWaitEvent(s, ex->ev_join, 0));
+  return DISO_OK;
+}
+
 template <class S>
 int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
              double padval, const uint64_t* seg, void* record, int normalize, int flags, const void* gv, void* gsdf,
@@ -338,15 +381,25 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   g.init(nx, ny, nz);
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  int rc;
+  if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
+  if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
+  // few CTAs per SM, so that the gather of the active tiles finds room beside them
+  zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf, (S*)gdef);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
+  active_ptiles_kernel<<<stride_ctas(g.nptiles(), ex->sms * 8), 256, 0, s>>>(g, tile_flags(seg, g), ex->plist,
+                                                                             ex->plist_n);
+  CUDA_TRY(cudaGetLastError());
   if (ex->method == DISO_MC)
     edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, 0);
   else
     edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, exact);
   CUDA_TRY(cudaGetLastError());
-  gather_kernel<S><<<(unsigned)g.nptiles(), NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), record, (S*)gsdf,
-                                                               (S*)gdef);
+  gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(f, g, seg, ex->plist, ex->plist_n, record,
+                                                                      (S*)gsdf, (S*)gdef);
   CUDA_TRY(cudaGetLastError());
-  return DISO_OK;
+  return side_join(ex, s);
 }
 
 template <class S>
@@ -397,8 +450,8 @@ int64_t batch_record_slots(const diso_grid* grids, int n, int64_t* seg_total, in
   }
   if (seg_total) *seg_total = segs;
   if (tiles_total) *tiles_total = tiles;
-  // segments of every grid, the total slot, then one activity byte per tile of every grid
-  return segs + 1 + (tiles + 7) / 8;
+  // segments of every grid, the total slot, then two activity bytes per tile of every grid
+  return segs + 1 + (2 * tiles + 7) / 8;
 }
 
 template <class S>
@@ -440,7 +493,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     offs[i] = seg_off;
     ex->bseg_off[i] = seg_off;
     seg_off += b.g.nseg;
-    tile_off += b.g.ntiles();
+    tile_off += 2 * b.g.ntiles();
     cblk += count_units(b.g);
     ptile += b.g.nptiles();
   }
@@ -454,6 +507,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
   ex->bptiles = ptile;
   int rc;
   if ((rc = grow(ex->active, ex->active_cap, tiles_total)) != DISO_OK) return rc;
+  if ((rc = grow(ex->plist, ex->plist_cap, ex->bptiles)) != DISO_OK) return rc;
   // grow the scan state now so that count allocates nothing
   const int64_t scan_tiles = (seg_total + 1 + SCAN_TILE - 1) / SCAN_TILE;
   if (scan_tiles > ex->scan_cap) {
@@ -534,19 +588,34 @@ int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv,
   const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
   const EdgeRecord<S> rec = batch_record<S>(ex, record, vcap, fcap);
+  (void)grid;
+  int rc;
+  if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
+  const unsigned zgrid = (unsigned)(ex->sms * 2), lgrid = stride_ctas(ex->bptiles, ex->sms * 8);
+  if (ex->method == DISO_MC)
+    batch_zero_tiles_kernel<S, MC><<<zgrid, 256, 0, ex->side>>>(d, ex->bn, ex->bptiles, vcap, fcap);
+  else
+    batch_zero_tiles_kernel<S, DMC><<<zgrid, 256, 0, ex->side>>>(d, ex->bn, ex->bptiles, vcap, fcap);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
   if (ex->method == DISO_MC) {
+    batch_active_ptiles_kernel<S, MC><<<lgrid, 256, 0, s>>>(d, ex->bn, ex->bptiles, vcap, fcap, ex->plist,
+                                                            ex->plist_n);
+    CUDA_TRY(cudaGetLastError());
     batch_edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(d, ex->bn, rec, vcap, fcap, (const S*)gv,
                                                                    normalize, 0);
-    CUDA_TRY(cudaGetLastError());
-    batch_gather_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, ex->bn, ex->bptiles, record, vcap, fcap);
   } else {
+    batch_active_ptiles_kernel<S, DMC><<<lgrid, 256, 0, s>>>(d, ex->bn, ex->bptiles, vcap, fcap, ex->plist,
+                                                             ex->plist_n);
+    CUDA_TRY(cudaGetLastError());
     batch_edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(d, ex->bn, rec, vcap, fcap, (const S*)gv,
                                                                     normalize, exact);
-    CUDA_TRY(cudaGetLastError());
-    batch_gather_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(d, ex->bn, ex->bptiles, record, vcap, fcap);
   }
   CUDA_TRY(cudaGetLastError());
-  return DISO_OK;
+  batch_gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(d, ex->bn, ex->plist, ex->plist_n,
+                                                                            record);
+  CUDA_TRY(cudaGetLastError());
+  return side_join(ex, s);
 }
 
 int batch_results(diso_extractor* ex, diso_counts* out, int64_t* voff, int64_t* foff, int* overflow,
@@ -609,7 +678,7 @@ int64_t diso_segment_slots(int nx, int ny, int nz) {
   if (nx < 1 || ny < 1 || nz < 1) return 0;
   Geom g;
   g.init(nx, ny, nz);
-  return g.nseg + 1 + (g.ntiles() + 7) / 8;
+  return g.nseg + 1 + (2 * g.ntiles() + 7) / 8;
 }
 
 int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double isovalue, double padval,

@@ -1,13 +1,14 @@
 // Forward and backward kernels of DiffMC / DiffDMC.
 //
-//   count_kernel      all tiles: per-segment crossing / face (MC) or crossing / patch
-//                     (DMC) counts, the min/max of the SDF for the empty-surface
-//                     guard, one activity byte per tile and the list of active tiles
+//   count_kernel /    all tiles: per-segment crossing / face (MC) or crossing / patch
+//   count_tma_kernel  (DMC) counts, the min/max of the SDF for the empty-surface
+//                     guard, two activity bytes per tile and the list of active tiles
 //   scan              scan.cuh
-//   mc_emit_kernel    active tiles: MC vertices and triangles
-//   dmc_emit_kernel   active tiles: DMC dual vertices and quads
-//   backward_kernel   all point tiles: dL/dsdf and dL/ddeform, every element written
-//                     once (zeros away from the surface), crossings recomputed
+//   mc_emit_kernel    active tiles: MC vertices and triangles (and the edge record)
+//   dmc_emit_kernel   active tiles: DMC dual vertices and quads (and the edge record)
+//   edge_adjoint_kernel  backward, every crossing edge: its adjoint at both ends
+//   zero_tiles_kernel /  backward, every point tile: dL/dsdf and dL/ddeform, written
+//   gather_list_kernel   once (zeros away from the surface, sums of edge adjoints near it)
 //   split_*           DMC quad -> triangle split (return_quads=False)
 //
 // Row masks.  Every kernel first turns the SDF rows its tile needs into bit masks:
@@ -293,7 +294,7 @@ struct CountShared {
   uint64_t m[CP + 1][CR + 1];  // masks of the current chunk, point row r = x * (CR + 1) + y
   int64_t rowoff[CROWS];       // offset of point row r in the SDF, -1 outside the grid
   uint32_t bal[CROWS];         // ballots of the chunk just read (each row read and used by one warp)
-  uint32_t act[CP];
+  uint32_t act[CP], actc[CP], actf[CP];
   int list[COUNT_LIST];
   int nlist, base;
 };
@@ -360,6 +361,13 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
 // Counts of the unit's chunk tz from the masks in sh.m (complete: the caller
 // synchronised), the activity bytes of the chunk's tiles; active tiles are appended
 // (as tile | tag) to sh.list.  Ends with a block barrier.
+//
+// Two bytes per tile: tile_flag[tile] = 1 when the tile's cells have crossings or
+// faces (the emit's tiles); tile_flag[ntiles + tile] bit (dx | dy << 1 | dz << 2) =
+// the tile's cells own a crossing edge, among them only the first x plane when dx,
+// the first y row when dy, the first z cell when dz: the cells of this tile whose
+// edges can touch the point tile one step back by (dx, dy, dz) (the backward's
+// activity test).
 template <class S, int METHOD>
 __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                             uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag, int X0,
@@ -367,11 +375,12 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z0 = tz * TZ;
   const int X = X0 + warp, Y = Y0 + lane;
-  uint32_t nv = 0, nf = 0;
+  uint32_t nv = 0, nf = 0, own = 0;
   if (X < g.c[0] && Y < g.c[1]) {
     const int x = warp, y = lane;
     const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
     const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
+    own = rw.xc | rw.yc | rw.zc;
     nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
     uint32_t nt = rw.nt;
     while (nt) {
@@ -388,7 +397,12 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
   // a cell can emit faces / patches without owning a crossing edge (its
   // crossings may all sit on edges owned by its +1 neighbours)
   const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
-  if (lane == 0) sh.act[warp] = busy;
+  const uint32_t anyc = __ballot_sync(0xffffffffu, own != 0), first = __ballot_sync(0xffffffffu, (own & 1u) != 0);
+  if (lane == 0) {
+    sh.act[warp] = busy;
+    sh.actc[warp] = anyc;
+    sh.actf[warp] = first;
+  }
   __syncthreads();
   if (threadIdx.x < (CP / TX) * (CR / TY)) {
     const int tp = threadIdx.x / (CR / TY), tr = threadIdx.x % (CR / TY);
@@ -397,8 +411,18 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
       uint32_t any = 0;
 #pragma unroll
       for (int p = 0; p < TX; ++p) any |= (sh.act[tp * TX + p] >> (tr * TY)) & ((1u << TY) - 1u);
+      uint32_t bw = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+        uint32_t v = 0;
+#pragma unroll
+        for (int p = 0; p < (dx ? 1 : TX); ++p) v |= ((dz ? sh.actf : sh.actc)[tp * TX + p] >> (tr * TY));
+        if (v & (dy ? 1u : (1u << TY) - 1u)) bw |= 1u << k;
+      }
       const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
       tile_flag[tile] = any ? 1 : 0;
+      tile_flag[g.ntiles() + tile] = (uint8_t)bw;
       if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
     }
   }
@@ -985,6 +1009,9 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
     const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
     const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
+    const int c0raw = (row && Z0 >= 1) ? code8(a, b, c, d, 0) : 0;
+    // a row without non-trivial cells (Z0 - 1 included) is never read
+    if (nt == 0 && (c0raw == 0 || c0raw == 255)) continue;
     int code = 0;
     if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
     const uint32_t np = dmc_npatch(dmc_case(code));
@@ -992,11 +1019,8 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     rc[x][y][lane + 1] = (uint8_t)code;
     pp[x][y][lane + 1] = (int16_t)(inc - np);
     if (lane == 0) {
-      int c0 = 0;
-      if (row && Z0 >= 1) {
-        c0 = code8(a, b, c, d, 0);
-        if (c0 != 0 && c0 != 255) c0 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c0, X, Y, Z0 - 1, g);
-      }
+      int c0 = c0raw;
+      if (c0 != 0 && c0 != 255) c0 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c0, X, Y, Z0 - 1, g);
       rc[x][y][0] = (uint8_t)c0;
       pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
     }
@@ -1198,52 +1222,46 @@ __device__ __forceinline__ void edge_adjoint2(const Field<S>& f, int X, int Y, i
   }
 }
 
-// Point tiles: unpadded points [x0, x0+TX) x [y0, y0+TY) x [z0, z0+TZ); in padded
-// coordinates the points are (X0+1.., Y0+1.., Z0+1..) with (X0, Y0, Z0) = (x0, y0, z0),
-// and the cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ] own every edge that touches
-// them.  Those cells lie in the forward tiles (x0/TX + {0,1}, y0/TY + {0,1},
-// z0/TZ + {0,1}); the point tile is inactive when none of them holds a crossing.
-__device__ __forceinline__ bool ptile_active(const Geom& g, const uint8_t* __restrict__ tile_flag, int x0, int y0,
-                                             int z0) {
-  int a = 0;
-  if (threadIdx.x < 8) {
-    const int tx = x0 / TX + (threadIdx.x & 1), ty = y0 / TY + ((threadIdx.x >> 1) & 1),
-              tz = z0 / TZ + (threadIdx.x >> 2);
-    if (tx < g.tiles_x() && ty < g.tiles_y() && tz < g.nzc) a = tile_flag[((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz];
-  }
-  return __syncthreads_or(a) != 0;
+// whether forward tile k = (dx, dy, dz) of point tile (x0, y0, z0) (the tile one step
+// further by (dx, dy, dz)) owns a crossing edge that can touch the point tile (the
+// backward bits that count_chunk writes after the tiles' emit flags)
+__device__ __forceinline__ int ptile_flag(const Geom& g, const uint8_t* __restrict__ tile_flag, int x0, int y0, int z0,
+                                          int k) {
+  const int tx = x0 / TX + (k & 1), ty = y0 / TY + ((k >> 1) & 1), tz = z0 / TZ + (k >> 2);
+  if (tx >= g.tiles_x() || ty >= g.tiles_y() || tz >= g.nzc) return 0;
+  return (tile_flag[g.ntiles() + ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz] >> k) & 1;
 }
 
-// zero dL/dsdf and dL/ddeform of a point tile; float4 stores when rows are 16-byte aligned
+// zero dL/dsdf and dL/ddeform of a point tile with one warp: per row (x, y) of the
+// tile, 8 lanes write the row's 32 gradient values and 24 lanes its 96 deform
+// gradients as float4 when the rows are 16-byte aligned
 template <class S>
-__device__ __forceinline__ void zero_ptile(const Field<S>& f, S* __restrict__ gsdf, S* __restrict__ gdef, int x0, int y0,
-                                           int z0) {
+__device__ __forceinline__ void zero_ptile_warp(const Field<S>& f, S* __restrict__ gsdf, S* __restrict__ gdef, int x0,
+                                                int y0, int z0) {
+  const int lane = threadIdx.x & 31;
   const int nz = min(TZ, f.n2 - z0);
-  if (sizeof(S) == 4 && (f.n2 & 3) == 0) {
-    const int r = threadIdx.x >> 3, k = threadIdx.x & 7;  // 32 rows x 8 float4
-    const int x = x0 + r / TY, y = y0 + r % TY;
-    if (x < f.n0 && y < f.n1) {
+  if (sizeof(S) == 4 && (f.n2 & 3) == 0 && (((uintptr_t)gsdf | (uintptr_t)gdef) & 15u) == 0) {
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int q = 0; q < TX * TY; ++q) {
+      const int x = x0 + q / TY, y = y0 + q % TY;
+      if (x >= f.n0 || y >= f.n1) continue;
       const int64_t base = ((int64_t)x * f.n1 + y) * f.n2 + z0;
-      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (4 * k < nz) reinterpret_cast<float4*>(gsdf + base)[k] = z4;
-      if (gdef) {
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const int q = k + 8 * j;
-          if (4 * q < 3 * nz) reinterpret_cast<float4*>(gdef + 3 * base)[q] = z4;
-        }
+      if (lane < 8) {
+        if (4 * lane < nz) reinterpret_cast<float4*>(gsdf + base)[lane] = z4;
+      } else if (gdef && 4 * (lane - 8) < 3 * nz) {
+        reinterpret_cast<float4*>(gdef + 3 * base)[lane - 8] = z4;
       }
     }
     return;
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int ix = 0; ix < TX; ++ix) {
-    const int x = x0 + ix, y = y0 + warp, z = z0 + lane;
-    if (x < f.n0 && y < f.n1 && z < f.n2) {
-      const int64_t i = ((int64_t)x * f.n1 + y) * f.n2 + z;
-      gsdf[i] = S(0);
-      if (gdef) gdef[3 * i] = gdef[3 * i + 1] = gdef[3 * i + 2] = S(0);
-    }
+  for (int q = 0; q < TX * TY; ++q) {
+    const int x = x0 + q / TY, y = y0 + q % TY;
+    if (x >= f.n0 || y >= f.n1) continue;
+    const int64_t base = ((int64_t)x * f.n1 + y) * f.n2 + z0;
+    if (lane < nz) gsdf[base + lane] = S(0);
+    if (gdef)
+      for (int k = lane; k < 3 * nz; k += 32) gdef[3 * base + k] = S(0);
   }
 }
 
@@ -1372,12 +1390,13 @@ __global__ void __launch_bounds__(256) edge_adjoint_kernel(Field<S> f, Geom g, c
 // coordinates the points are (X0+1.., Y0+1.., Z0+1..) with (X0, Y0, Z0) = (x0, y0, z0),
 // and the cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ] own every edge that touches
 // them.  Those cells lie in the forward tiles (x0/TX + {0,1}, y0/TY + {0,1},
-// z0/TZ + {0,1}); the point tile is inactive when none of them holds a crossing.
-// adj: the record's adjoints, indexed by the scanned crossing counts of seg.
+// z0/TZ + {0,1}); the point tile is inactive when none of them owns a crossing edge
+// among the cells that can touch it (ptile_flag).  gather_tile handles an active
+// tile; adj: the record's adjoints, indexed by the scanned crossing counts of seg.
 template <class S>
 __device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
-                                            const uint8_t* __restrict__ tile_flag, int64_t ptile,
-                                            const S* __restrict__ adj, S* __restrict__ gsdf, S* __restrict__ gdef) {
+                                            int64_t ptile, const S* __restrict__ adj, S* __restrict__ gsdf,
+                                            S* __restrict__ gdef) {
   constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint64_t m[WX][WY];
@@ -1387,10 +1406,6 @@ __device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, co
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
   ptile_coords(ptile, g, X0, Y0, Z0);
-  if (!ptile_active(g, tile_flag, X0, Y0, Z0)) {
-    zero_ptile<S>(f, gsdf, gdef, X0, Y0, Z0);
-    return;
-  }
   const int zc = Z0 / TZ;
   // segment bases first, so that their loads overlap the mask loads
   uint64_t sv = 0;
@@ -1454,12 +1469,56 @@ __device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, co
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
+// The point pass in two parts that run side by side: the point tiles with no
+// crossing nearby (most of them) only get zeros, written by independent warps on a
+// second stream while the edge pass and the gather of the active tiles run.
+
+// zeros of the inactive point tiles, one warp per tile (persistent)
 template <class S>
-__global__ void __launch_bounds__(NTHREADS) gather_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                          const uint8_t* __restrict__ tile_flag,
-                                                          const void* __restrict__ record, S* __restrict__ gsdf,
-                                                          S* __restrict__ gdef) {
-  gather_tile<S>(f, g, seg, tile_flag, blockIdx.x, (const S*)record, gsdf, gdef);
+__global__ void __launch_bounds__(256) zero_tiles_kernel(Field<S> f, Geom g, const uint8_t* __restrict__ tile_flag,
+                                                         S* __restrict__ gsdf, S* __restrict__ gdef) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < g.nptiles(); p += nw) {
+    int x0, y0, z0;
+    ptile_coords(p, g, x0, y0, z0);
+    const int a = lane < 8 ? ptile_flag(g, tile_flag, x0, y0, z0, lane) : 0;
+    if (!__any_sync(0xffffffffu, a)) zero_ptile_warp<S>(f, gsdf, gdef, x0, y0, z0);
+  }
+}
+
+// the list of active point tiles (any order)
+__global__ void __launch_bounds__(256) active_ptiles_kernel(Geom g, const uint8_t* __restrict__ tile_flag,
+                                                            int* __restrict__ list, unsigned* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = g.nptiles();
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;
+    bool act = false;
+    if (p < n) {
+      int x0, y0, z0;
+      ptile_coords(p, g, x0, y0, z0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) act = act || ptile_flag(g, tile_flag, x0, y0, z0, k) != 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    unsigned at = 0;
+    if (lane == 0 && m) at = atomicAdd(count, (unsigned)__popc(m));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (act) list[at + __popc(m & ((1u << lane) - 1u))] = (int)p;
+  }
+}
+
+// gather of the active point tiles in the list (persistent)
+template <class S>
+__global__ void __launch_bounds__(NTHREADS) gather_list_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+                                                               const int* __restrict__ list,
+                                                               const unsigned* __restrict__ count,
+                                                               const void* __restrict__ record, S* __restrict__ gsdf,
+                                                               S* __restrict__ gdef) {
+  const unsigned n = *count;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
+    gather_tile<S>(f, g, seg, list[i], (const S*)record, gsdf, gdef);
 }
 
 // ------------------------------------------------------------------ batch emit / backward
@@ -1538,12 +1597,11 @@ __global__ void __launch_bounds__(256) batch_edge_adjoint_kernel(const BatchGrid
   }
 }
 
-// point pass over the flattened point tiles of a batch (persistent); the grids
-// that did not fit the capacities get zero gradients
+// point pass of a batch over the flattened point tiles: zeros of the inactive tiles
+// (and of every tile of a grid that did not fit the capacities), one warp per tile
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS) batch_gather_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
-                                                                int64_t ntiles, const void* __restrict__ record,
-                                                                int64_t vcap, int64_t fcap) {
+__global__ void __launch_bounds__(256) batch_zero_tiles_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                               int64_t ntiles, int64_t vcap, int64_t fcap) {
   __shared__ int64_t start[MAX_BATCH];
   __shared__ uint8_t fits[MAX_BATCH];
   for (int i = threadIdx.x; i < ngrids; i += blockDim.x) {
@@ -1551,17 +1609,68 @@ __global__ void __launch_bounds__(NTHREADS) batch_gather_kernel(const BatchGrid<
     fits[i] = batch_fits<S, METHOD>(grids[i], vcap, fcap) ? 1 : 0;
   }
   __syncthreads();
-#pragma unroll 1
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nw) {
     const int i = batch_find(start, ngrids, t);
     const BatchGrid<S>& G = grids[i];
-    if (fits[i]) {
-      gather_tile<S>(G.f, G.g, G.seg, G.tile_flag, t - start[i], (const S*)record, G.gsdf, G.gdef);
-    } else {
-      int x0, y0, z0;
-      ptile_coords(t - start[i], G.g, x0, y0, z0);
-      zero_ptile<S>(G.f, G.gsdf, G.gdef, x0, y0, z0);
+    int x0, y0, z0;
+    ptile_coords(t - start[i], G.g, x0, y0, z0);
+    const int a = (fits[i] && lane < 8) ? ptile_flag(G.g, G.tile_flag, x0, y0, z0, lane) : 0;
+    if (!__any_sync(0xffffffffu, a)) zero_ptile_warp<S>(G.f, G.gsdf, G.gdef, x0, y0, z0);
+  }
+}
+
+// the list of active flattened point tiles of a batch (grids that fit the capacities)
+template <class S, int METHOD>
+__global__ void __launch_bounds__(256) batch_active_ptiles_kernel(const BatchGrid<S>* __restrict__ grids, int ngrids,
+                                                                  int64_t ntiles, int64_t vcap, int64_t fcap,
+                                                                  int* __restrict__ list,
+                                                                  unsigned* __restrict__ count) {
+  __shared__ int64_t start[MAX_BATCH];
+  __shared__ uint8_t fits[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) {
+    start[i] = grids[i].ptile0;
+    fits[i] = batch_fits<S, METHOD>(grids[i], vcap, fcap) ? 1 : 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < ntiles; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    bool act = false;
+    if (t < ntiles) {
+      const int i = batch_find(start, ngrids, t);
+      if (fits[i]) {
+        const BatchGrid<S>& G = grids[i];
+        int x0, y0, z0;
+        ptile_coords(t - start[i], G.g, x0, y0, z0);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) act = act || ptile_flag(G.g, G.tile_flag, x0, y0, z0, k) != 0;
+      }
     }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    unsigned at = 0;
+    if (lane == 0 && m) at = atomicAdd(count, (unsigned)__popc(m));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (act) list[at + __popc(m & ((1u << lane) - 1u))] = (int)t;
+  }
+}
+
+// gather of the listed point tiles of a batch (persistent)
+template <class S>
+__global__ void __launch_bounds__(NTHREADS) batch_gather_list_kernel(const BatchGrid<S>* __restrict__ grids,
+                                                                     int ngrids, const int* __restrict__ list,
+                                                                     const unsigned* __restrict__ count,
+                                                                     const void* __restrict__ record) {
+  __shared__ int64_t start[MAX_BATCH];
+  for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].ptile0;
+  __syncthreads();
+  const unsigned n = *count;
+  for (unsigned k = blockIdx.x; k < n; k += gridDim.x) {
+    const int64_t t = list[k];
+    const int i = batch_find(start, ngrids, t);
+    const BatchGrid<S>& G = grids[i];
+    gather_tile<S>(G.f, G.g, G.seg, t - start[i], (const S*)record, G.gsdf, G.gdef);
   }
 }
 

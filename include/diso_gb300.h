@@ -21,7 +21,7 @@
  * sizes (one device-to-host copy, the only synchronisation of the forward);
  * the caller then allocates verts/faces and calls diso_forward_emit with the
  * same inputs and `seg`.  `seg` (diso_segment_slots() uint64 values: the
- * scanned per-segment counts, their total and one activity byte per tile) and,
+ * scanned per-segment counts, their total and two activity bytes per tile) and,
  * when gradients will be wanted, the edge record that diso_forward_emit fills
  * (diso_edge_record_slots() uint64 values: every crossing edge's cell and axis,
  * for DMC the patches around it, and room for the backward's per-edge adjoints)

@@ -65,10 +65,10 @@ def test_argument_errors_are_status_codes(lib):
 
 
 def test_segment_slots(lib):
-    # cells (n+1)^3, rows cut into 32-cell chunks, the total slot, then one byte per
+    # cells (n+1)^3, rows cut into 32-cell chunks, the total slot, then two bytes per
     # 4x8x32-cell tile
-    assert lib.diso_segment_slots(64, 64, 64) == 65 * 65 * 3 + 1 + (17 * 9 * 3 + 7) // 8
-    assert lib.diso_segment_slots(31, 5, 7) == 32 * 6 * 1 + 1 + (8 * 1 * 1 + 7) // 8
+    assert lib.diso_segment_slots(64, 64, 64) == 65 * 65 * 3 + 1 + (2 * 17 * 9 * 3 + 7) // 8
+    assert lib.diso_segment_slots(31, 5, 7) == 32 * 6 * 1 + 1 + (2 * 8 * 1 * 1 + 7) // 8
     assert lib.diso_segment_slots(0, 5, 7) == 0
 
 
