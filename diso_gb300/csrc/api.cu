@@ -45,6 +45,8 @@ struct diso_extractor {
   int64_t scan_cap = 0;          // look-back tiles
   int* active = nullptr;         // tiles with crossings (forward)
   int64_t active_cap = 0;
+  uint8_t* codes = nullptr;      // cell codes of the active segments (count -> emit)
+  int64_t codes_cap = 0;
   uint64_t* split = nullptr;     // split counts (n_quads + 1)
   int64_t split_cap = 0;
   int64_t last_active = 0;       // from the last forward count
@@ -88,6 +90,9 @@ struct diso_extractor {
     cudaFree(scan_agg);
     cudaFree(scan_incl);
     cudaFree(active);
+    cudaFree(codes);
+    codes = nullptr;
+    codes_cap = 0;
     cudaFree(split);
     cudaFree(plist);
     cudaFree(plist_n);
@@ -283,6 +288,7 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   g.init(nx, ny, nz);
   int rc;
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
+  if ((rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
@@ -294,20 +300,22 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     const size_t smem = count_tma_smem<S>();
     if (ex->method == DISO_MC)
-      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->stats,
-                                                           ex->active);
+      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->codes,
+                                                           ex->stats, ex->active);
     else
-      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->stats,
-                                                            ex->active);
+      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->codes,
+                                                            ex->stats, ex->active);
   } else {
     const int64_t units = count_units(g);
     const int64_t want =
         std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     if (ex->method == DISO_MC)
-      count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
+      count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->codes, ex->stats,
+                                                    ex->active);
     else
-      count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->stats, ex->active);
+      count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->codes, ex->stats,
+                                                     ex->active);
   }
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
@@ -348,7 +356,8 @@ int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx
   if (ex->method == DISO_MC)
     mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
   else
-    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
+    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->codes, ex->active, (S*)verts, faces, normalize,
+                                                 record);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
@@ -473,10 +482,17 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
   CUDA_TRY(cudaStreamSynchronize(s));
   BatchGrid<S>* d = (BatchGrid<S>*)ex->bdesc_host;
   int64_t* offs = (int64_t*)((char*)ex->bdesc_host + sizeof(BatchGrid<double>) * MAX_BATCH);
-  int64_t seg_off = 0, tile_off = 0, cblk = 0, ptile = 0;
-  int64_t seg_total = 0, tiles_total = 0;
+  int64_t seg_off = 0, tile_off = 0, cblk = 0, ptile = 0, code_off = 0;
+  int64_t seg_total = 0, tiles_total = 0, codes_total = 0;
   batch_record_slots(grids, n, &seg_total, &tiles_total);
   uint8_t* flags = (uint8_t*)(record + seg_total + 1);
+  for (int i = 0; i < n; ++i) {
+    Geom g;
+    g.init(grids[i].nx, grids[i].ny, grids[i].nz);
+    codes_total += g.ncodes();
+  }
+  int rc;
+  if ((rc = grow(ex->codes, ex->codes_cap, codes_total)) != DISO_OK) return rc;
   for (int i = 0; i < n; ++i) {
     const diso_grid& q = grids[i];
     BatchGrid<S> b;
@@ -485,6 +501,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     b.seg = record + seg_off;
     b.seg_end = record + seg_off + b.g.nseg;
     b.tile_flag = flags + tile_off;
+    b.codes = ex->codes + code_off;
     b.cblk0 = cblk;
     b.ptile0 = ptile;
     b.gsdf = (S*)q.grad_sdf;
@@ -494,6 +511,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     ex->bseg_off[i] = seg_off;
     seg_off += b.g.nseg;
     tile_off += 2 * b.g.ntiles();
+    code_off += b.g.ncodes();
     cblk += count_units(b.g);
     ptile += b.g.nptiles();
   }
@@ -505,7 +523,6 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
   ex->btiles = tiles_total;
   ex->bblocks = cblk;
   ex->bptiles = ptile;
-  int rc;
   if ((rc = grow(ex->active, ex->active_cap, tiles_total)) != DISO_OK) return rc;
   if ((rc = grow(ex->plist, ex->plist_cap, ex->bptiles)) != DISO_OK) return rc;
   // grow the scan state now so that count allocates nothing
@@ -878,9 +895,9 @@ int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sd
   const int64_t want = std::max<int64_t>(ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
   const unsigned grid = (unsigned)std::min<int64_t>(want, units);
   if (method == DISO_MC)
-    count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), &sc->stats, sc->active);
+    count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), nullptr, &sc->stats, sc->active);
   else
-    count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), &sc->stats, sc->active);
+    count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), nullptr, &sc->stats, sc->active);
   CUDA_TRY(cudaGetLastError());
   const int64_t tiles = (g.nseg + 1 + SCAN_TILE - 1) / SCAN_TILE;
   CUDA_TRY(cudaMemsetAsync(sc->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));

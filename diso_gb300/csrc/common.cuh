@@ -49,6 +49,9 @@ struct Geom {
     nseg = (int64_t)c[0] * c[1] * nzc;
   }
   __host__ __device__ int64_t seg(int X, int Y, int zc) const { return ((int64_t)X * c[1] + Y) * nzc + zc; }
+  // byte of cell (X, Y, Z) in the array of cell codes (rows padded to whole chunks)
+  __host__ __device__ int64_t code(int X, int Y, int Z) const { return ((int64_t)X * c[1] + Y) * (nzc * TZ) + Z; }
+  __host__ __device__ int64_t ncodes() const { return (int64_t)c[0] * c[1] * nzc * TZ; }
   // tiles of cells for the forward passes
   __host__ __device__ int tiles_x() const { return (c[0] + TX - 1) / TX; }
   __host__ __device__ int tiles_y() const { return (c[1] + TY - 1) / TY; }
@@ -106,6 +109,14 @@ __device__ __forceinline__ int dmc_patch_size(uint64_t w, int p) { return (int)(
 // MC case code (corner order of src/cumc.cu:107) from the Morton code: swap corners 2<->3, 6<->7
 __device__ __forceinline__ int mc_from_morton(int m) {
   return (m & 0x33) | ((m & 0x44) << 1) | ((m & 0x88) >> 1);
+}
+
+// crossing flags of a cell's three owned edges (+x, +y, +z from its corner 0);
+// the reference tests (d0 < iso && d1 >= iso) || (d1 < iso && d0 >= iso)
+// (src/cumc.cu:334-339), i.e. the two corner bits differ.  Flipping all bits of a
+// code (DMC ambiguity resolution) leaves the flags unchanged.
+__device__ __forceinline__ int cross_flags(int m) {
+  return ((m ^ (m >> 1)) & 1) | (((m ^ (m >> 2)) & 1) << 1) | (((m ^ (m >> 4)) & 1) << 2);
 }
 
 // The twelve cell edges (DISO_EDGE_TABLE: start corner | axis << 3, in the

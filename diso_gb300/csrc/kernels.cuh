@@ -186,6 +186,32 @@ __device__ __forceinline__ int code8(uint64_t a, uint64_t b, uint64_t c, uint64_
   return (int)(lo | (hi << 4));
 }
 
+// The four masks of a cell row (a, b, c, d as for code8) as eight shifted copies, so
+// that the Morton code of cell j of the row (mask bits j+1 and j+2) takes one funnel
+// shift and one logic op per code bit: copy k holds mask (k & 3) shifted so that
+// the bit code8 reads for code bit k sits at bit j + k.
+struct CodeRow {
+  uint32_t lo[8], hi[8];
+};
+__device__ __forceinline__ CodeRow code_row(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+  const uint64_t m[4] = {a, b, c, d};
+  CodeRow r;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const uint64_t p = (k < 4 ? (m[k] << k) : (m[k - 4] << (k - 1))) >> 1;
+    r.lo[k] = (uint32_t)p;
+    r.hi[k] = (uint32_t)(p >> 32);
+  }
+  return r;
+}
+// Morton code of cell j in [0, 32) of the row: code8(a, b, c, d, j + 1)
+__device__ __forceinline__ int code_at(const CodeRow& r, int j) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) c |= __funnelshift_r(r.lo[k], r.hi[k], j) & (1u << k);
+  return (int)c;
+}
+
 // Morton code of cell (X, Y, Z) from global memory
 template <class S>
 __device__ __forceinline__ int cell_code_far(const Field<S>& f, int X, int Y, int Z) {
@@ -295,6 +321,7 @@ struct CountShared {
   int64_t rowoff[CROWS];       // offset of point row r in the SDF, -1 outside the grid
   uint32_t bal[CROWS];         // ballots of the chunk just read (each row read and used by one warp)
   uint32_t act[CP], actc[CP], actf[CP];
+  __align__(16) uint8_t code[CP][32][TZ];  // Morton codes of each lane's segment (staging)
   int list[COUNT_LIST];
   int nlist, base;
 };
@@ -370,29 +397,41 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
 // activity test).
 template <class S, int METHOD>
 __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
-                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag, int X0,
-                                            int Y0, int tz, int tag) {
+                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
+                                            uint8_t* __restrict__ codes, int X0, int Y0, int tz, int tag) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z0 = tz * TZ;
   const int X = X0 + warp, Y = Y0 + lane;
-  uint32_t nv = 0, nf = 0, own = 0;
+  uint32_t nv = 0, nf = 0, own = 0, nt = 0;
+  uint4* stage = reinterpret_cast<uint4*>(sh.code[warp][lane]);
+  if (codes) stage[0] = stage[1] = make_uint4(0u, 0u, 0u, 0u);
   if (X < g.c[0] && Y < g.c[1]) {
     const int x = warp, y = lane;
     const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
     const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
     own = rw.xc | rw.yc | rw.zc;
+    nt = rw.nt;
     nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
-    uint32_t nt = rw.nt;
-    while (nt) {
-      const int j = __ffs(nt) - 1;
-      nt &= nt - 1;
-      const int code = code8(a, b, c, d, j + 1);
+    uint32_t left = nt;
+    const CodeRow cr = code_row(a, b, c, d);
+    while (left) {
+      const int j = __ffs(left) - 1;
+      left &= left - 1;
+      const int code = code_at(cr, j);
+      if (codes) sh.code[warp][lane][j] = (uint8_t)code;
       if (METHOD == MC)
         nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
       else
         nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g)));
     }
     seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
+    // the Morton codes of a segment with non-trivial cells (0 for the trivial ones),
+    // read by the emit for the segments whose count is not zero
+    if (codes && nt) {
+      uint4* out = reinterpret_cast<uint4*>(codes + g.code(X, Y, Z0));
+      out[0] = stage[0];
+      out[1] = stage[1];
+    }
   }
   // a cell can emit faces / patches without owning a crossing edge (its
   // crossings may all sit on edges owned by its +1 neighbours)
@@ -452,7 +491,7 @@ __device__ __forceinline__ void count_combine(CountShared<S, METHOD>& sh, bool w
 template <class S, int METHOD>
 __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
-                                           Stats* stats, int64_t unit, int tag) {
+                                           uint8_t* __restrict__ codes, Stats* stats, int64_t unit, int tag) {
   // a row of nzc chunks is cut into nbz near-equal runs of at most KZ chunks
   const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
   const int tz0 = (int)(unit % nbz) * kz;
@@ -478,7 +517,7 @@ __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Fie
     count_combine<S, METHOD>(sh, t >= tz0 + 1, p1, p2);
     if (t < tz0 + 1) continue;
     __syncthreads();
-    count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, X0, Y0, t - 1, tag);
+    count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, X0, Y0, t - 1, tag);
   }
   publish_minmax<S>(stats, mn, mx);
 }
@@ -495,13 +534,15 @@ __device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned
 
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
-                                                            uint8_t* __restrict__ tile_flag, Stats* stats,
+                                                            uint8_t* __restrict__ tile_flag,
+                                                            uint8_t* __restrict__ codes, Stats* stats,
                                                             int* __restrict__ active) {
   __shared__ CountShared<S, METHOD> sh;
   if (threadIdx.x == 0) sh.nlist = 0;
   const int64_t nunits = count_units(g);
 #pragma unroll 1
-  for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x) count_unit<S, METHOD>(sh, f, g, seg, tile_flag, stats, u, 0);
+  for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x)
+    count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, u, 0);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
 
@@ -636,7 +677,8 @@ template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_constant__ CUtensorMap wide,
                                                                 const __grid_constant__ CUtensorMap narrow,
                                                                 Field<S> f, Geom g, uint64_t* __restrict__ seg,
-                                                                uint8_t* __restrict__ tile_flag, Stats* stats,
+                                                                uint8_t* __restrict__ tile_flag,
+                                                                uint8_t* __restrict__ codes, Stats* stats,
                                                                 int* __restrict__ active) {
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   __shared__ CountShared<S, METHOD> sh;
@@ -696,7 +738,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
       pc.next(g, nunits);
       ++issued;
     }
-    if (cc.t >= cc.tz0 + 1) count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, cc.X0, cc.Y0, cc.t - 1, 0);
+    if (cc.t >= cc.tz0 + 1) count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, cc.X0, cc.Y0, cc.t - 1, 0);
     cc.next(g, nunits);
   }
   if (failed && threadIdx.x == 0) {
@@ -721,6 +763,7 @@ struct BatchGrid {
   uint64_t* seg;        // this grid's first segment in the concatenated, globally scanned array
   uint64_t* seg_end;    // the next grid's first segment (or the total slot)
   uint8_t* tile_flag;   // this grid's tile bytes
+  uint8_t* codes;       // this grid's cell codes (count -> emit)
   int64_t cblk0;        // first count unit of the grid in the flattened queue
   int64_t ptile0;       // first point tile (backward)
   S* gsdf;              // backward outputs
@@ -756,7 +799,7 @@ __global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGri
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
     const int i = batch_find(start, ngrids, b);
     const BatchGrid<S>& G = grids[i];
-    count_unit<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, stats + i, b - start[i], i << BATCH_TILE_BITS);
+    count_unit<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, G.codes, stats + i, b - start[i], i << BATCH_TILE_BITS);
   }
   count_flush<S, METHOD>(sh, n_active, active);
 }
@@ -864,11 +907,12 @@ __device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, c
     cv = __popc(own.xc) + __popc(own.yc) + __popc(own.zc);
     cc = __popc(own.nt);
     uint32_t nt = own.nt, run = 0;
+    const CodeRow cr = code_row(m[ox][oy], m[ox + 1][oy], m[ox][oy + 1], m[ox + 1][oy + 1]);
     while (nt) {
       const int j = __ffs(nt) - 1;
       nt &= nt - 1;
       fpre[ox][oy][j] = (uint8_t)run;
-      run += (uint32_t)(mc_tri(mc_from_morton(code8(m[ox][oy], m[ox + 1][oy], m[ox][oy + 1], m[ox + 1][oy + 1], j + 1))) & 15);
+      run += (uint32_t)(mc_tri(mc_from_morton(code_at(cr, j))) & 15);
     }
   }
   uint32_t tot;
@@ -960,15 +1004,20 @@ __host__ __device__ constexpr int epos_cap() {
 }
 
 // One active tile: its dual vertices and quads; patch ids written into quads are
-// reduced by vsub (as in mc_emit_tile).
+// reduced by vsub (as in mc_emit_tile).  The cells' Morton codes come from the codes
+// array the count filled (valid for the segments whose count is not zero; the
+// others hold trivial cells only), so the SDF is read only for the edge vertices.
 template <class S>
 __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
-                                              int tile, S* __restrict__ verts, int64_t* __restrict__ quads,
-                                              int normalize, int64_t vsub, const EdgeRecord<S>& rec) {
-  constexpr int WX = TX + 3, WY = TY + 3;  // point rows [X0-1, X0+TX+1] x [Y0-1, Y0+TY+1]
+                                              const uint8_t* __restrict__ codes, int tile, S* __restrict__ verts,
+                                              int64_t* __restrict__ quads, int normalize, int64_t vsub,
+                                              const EdgeRecord<S>& rec) {
+  constexpr int KX = TX + 2, KY = TY + 2;  // code window: cells [X0-1, X0+TX] x [Y0-1, Y0+TY], z index j+1 for Z0+j,
+  constexpr int KZ2 = TZ + 2;              // j in [-1, TZ]
   constexpr int CX = TX + 1, CY = TY + 1;  // code rows: cells [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
   constexpr int CAP = epos_cap<S>();
-  __shared__ uint64_t m[WX][WY];
+  __shared__ uint8_t cw[KX][KY][KZ2];     // raw Morton codes of the window
+  __shared__ uint8_t sact[KX][KY];        // bit 0/1/2: the row's segment tz-1 / tz / tz+1 has a non-zero count
   __shared__ uint8_t rc[CX][CY][TZ + 1];  // resolved codes; z index j+1 for cell Z0+j, 0 for Z0-1
   __shared__ int16_t pp[CX][CY][TZ + 1];  // first patch of the cell inside its segment
   __shared__ uint32_t pb[CX][CY];
@@ -985,42 +1034,81 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
-  const int WX0 = X0 - 1, WY0 = Y0 - 1;
-  // segment bases first, so that their loads overlap the mask loads
-  uint64_t sv = 0;
-  const int sy = threadIdx.x % CY, sx = threadIdx.x / CY;
-  if (threadIdx.x < CX * CY) {
-    const int X = X0 - 1 + sx, Y = Y0 - 1 + sy;
-    if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) sv = seg[g.seg(X, Y, tz)];
-  }
-  S dmn, dmx;
-  bool dseen = false;
-  load_masks<S, WX, WY, false>(m, f, WX0, WY0, Z0, dmn, dmx, dseen);
-  if (threadIdx.x < CX * CY) {
-    pb[sx][sy] = Counts::hi(sv);
-    if (sx >= 1 && sy >= 1) qb[sx - 1][sy - 1] = Counts::lo(sv);
+  // segment values of the window rows: activity of chunks tz-1, tz, tz+1, the bases
+  if (threadIdx.x < KX * KY) {
+    const int wx = threadIdx.x / KY, wy = threadIdx.x % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+    uint32_t act = 0;
+    uint64_t s0 = 0;
+    if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) {
+      const int64_t i = g.seg(X, Y, tz);
+      s0 = seg[i];
+      const uint64_t s1 = seg[i + 1];
+      if (s1 != s0) act |= 2;
+      if (tz > 0 && seg[i - 1] != s0) act |= 1;
+      if (tz + 1 < g.nzc && seg[i + 2] != s1) act |= 4;
+    }
+    sact[wx][wy] = (uint8_t)act;
+    if (wx < CX && wy < CY) {
+      pb[wx][wy] = Counts::hi(s0);
+      if (wx >= 1 && wy >= 1) qb[wx - 1][wy - 1] = Counts::lo(s0);
+    }
   }
   __syncthreads();
-  const uint32_t valid = zvalid(g, Z0);
-  // resolved codes and in-segment patch prefixes of the tile's cells and their -1 halo;
-  // the mask row of cell (X0-1+x, Y0-1+y) is (x, y)
+  // codes of the window, one warp per row; the edge rows' crossing bits from them
+  for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
+    const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+    const uint32_t act = sact[wx][wy];
+    const int c = (act & 2) ? codes[g.code(X, Y, Z0 + lane)] : 0;
+    cw[wx][wy][lane + 1] = (uint8_t)c;
+    int e = 0;
+    if (lane == 0 && (act & 1)) e = codes[g.code(X, Y, Z0 - 1)];
+    if (lane == 31 && (act & 4)) e = codes[g.code(X, Y, Z0 + TZ)];
+    if (lane == 0) cw[wx][wy][0] = (uint8_t)e;
+    if (lane == 31) cw[wx][wy][TZ + 1] = (uint8_t)e;
+    if (wx >= 1 && wy >= 1) {
+      const int cf = cross_flags(c);
+      RowBits w;
+      w.xc = __ballot_sync(0xffffffffu, cf & 1);
+      w.yc = __ballot_sync(0xffffffffu, cf & 2);
+      w.zc = __ballot_sync(0xffffffffu, cf & 4);
+      w.nt = __ballot_sync(0xffffffffu, c != 0 && c != 255);
+      if (lane == 0) wb[wx - 1][wy - 1] = w;
+      if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e);
+    }
+  }
+  __syncthreads();
+  // resolved codes and in-segment patch prefixes of the tile's cells and their -1 halo
+  // (the ambiguity test, src/cudualmc.cu:815-839, with the neighbour's code from the
+  // window, or from the SDF outside it)
+  auto resolve = [&](int wx, int wy, int jj, int code) -> int {
+    const int dir = dmc_dir(dmc_case(code));
+    if (dir == 7) return code;
+    const int comp = dir >> 1, d = (dir & 1) ? 1 : -1;
+    const int X = X0 - 1 + wx, Y = Y0 - 1 + wy, Z = Z0 - 1 + jj;
+    const int nx = wx + (comp == 0 ? d : 0), ny = wy + (comp == 1 ? d : 0), nj = jj + (comp == 2 ? d : 0);
+    const int nc = comp == 0 ? X + d : (comp == 1 ? Y + d : Z + d);
+    if (nc < 0 || nc >= g.c[comp]) return code;
+    const int ncode = ((unsigned)nx < (unsigned)KX && (unsigned)ny < (unsigned)KY && (unsigned)nj < (unsigned)KZ2)
+                          ? cw[nx][ny][nj]
+                          : cell_code_far<S>(f, X + (comp == 0 ? d : 0), Y + (comp == 1 ? d : 0), Z + (comp == 2 ? d : 0));
+    return dmc_dir(dmc_case(ncode)) != 7 ? (code ^ 0xff) : code;
+  };
   for (int r = warp; r < CX * CY; r += TY) {
-    const int x = r / CY, y = r % CY, X = X0 - 1 + x, Y = Y0 - 1 + y;
-    const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
-    const uint64_t a = m[x][y], b = m[x + 1][y], c = m[x][y + 1], d = m[x + 1][y + 1];
-    const uint32_t nt = row ? row_bits(a, b, c, d, valid).nt : 0u;
-    const int c0raw = (row && Z0 >= 1) ? code8(a, b, c, d, 0) : 0;
+    const int x = r / CY, y = r % CY;
+    const int craw = cw[x][y][lane + 1];
+    const bool nontriv = craw != 0 && craw != 255;
+    const uint32_t nt = __ballot_sync(0xffffffffu, nontriv);
+    const int c0raw = cw[x][y][0];
     // a row without non-trivial cells (Z0 - 1 included) is never read
     if (nt == 0 && (c0raw == 0 || c0raw == 255)) continue;
-    int code = 0;
-    if ((nt >> lane) & 1) code = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, code8(a, b, c, d, lane + 1), X, Y, Z0 + lane, g);
+    const int code = nontriv ? resolve(x, y, lane + 1, craw) : 0;
     const uint32_t np = dmc_npatch(dmc_case(code));
     const uint32_t inc = nt ? warp_incl(np) : 0u;
     rc[x][y][lane + 1] = (uint8_t)code;
     pp[x][y][lane + 1] = (int16_t)(inc - np);
     if (lane == 0) {
       int c0 = c0raw;
-      if (c0 != 0 && c0 != 255) c0 = dmc_resolve_m<S>(m, f, WX0, WY0, Z0, c0, X, Y, Z0 - 1, g);
+      if (c0 != 0 && c0 != 255) c0 = resolve(x, y, 0, c0);
       rc[x][y][0] = (uint8_t)c0;
       pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
     }
@@ -1030,19 +1118,11 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   // writes the row's items
   {
     uint32_t ce = 0, cc = 0;
-    RowBits w = {0u, 0u, 0u, 0u};
-    int fl32 = 0;
     const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
-    if (threadIdx.x < EW_ROWS && X0 + ex_ < g.c[0] && Y0 + ey < g.c[1]) {
-      const uint64_t a = m[ex_ + 1][ey + 1], b = m[ex_ + 2][ey + 1], c = m[ex_ + 1][ey + 2], d = m[ex_ + 2][ey + 2];
-      w = row_bits(a, b, c, d, valid);
-      if (Z0 + TZ < g.c[2]) fl32 = flags_at(a, b, c, TZ + 1);
-      ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(fl32);
-      if (ex_ < TX && ey < TY) cc = __popc(w.nt);
-    }
     if (threadIdx.x < EW_ROWS) {
-      wb[ex_][ey] = w;
-      w32[ex_][ey] = (uint8_t)fl32;
+      const RowBits w = wb[ex_][ey];
+      ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(w32[ex_][ey]);
+      if (ex_ < TX && ey < TY) cc = __popc(w.nt);
     }
     uint32_t tot;
     const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
@@ -1094,7 +1174,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int x = ix + 1, y = iy + 1;  // code row / mask row of the own row
     const RowBits& r = wb[ix][iy];
     const int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
-    const int type = a + 3 * (int)((m[x][y] >> (j + 1)) & 1);
+    const int type = a + 3 * (cw[x][y][j + 1] & 1);  // corner 0 of the owner cell (Morton bit 0)
     int4 rid = make_int4(0, 0, 0, 0);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -1176,11 +1256,12 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
 
 template <class S>
 __global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                            const int* __restrict__ active, S* __restrict__ verts,
+                                                               const uint8_t* __restrict__ codes,
+                                                               const int* __restrict__ active, S* __restrict__ verts,
                                                             int64_t* __restrict__ quads, int normalize,
                                                             void* record) {
   const EdgeRecord<S> rec = grid_record<S, DMC>(record, g, seg);
-  dmc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, quads, normalize, 0, rec);
+  dmc_emit_tile<S>(f, g, seg, codes, active[blockIdx.x], verts, quads, normalize, 0, rec);
 }
 
 // ------------------------------------------------------------------ backward
@@ -1566,7 +1647,7 @@ __global__ void __launch_bounds__(NTHREADS) batch_emit_kernel(const BatchGrid<S>
     if (METHOD == MC)
       mc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0, rec);
     else
-      dmc_emit_tile<S>(G.f, G.g, G.seg, tile, verts, faces, normalize, v0, rec);
+      dmc_emit_tile<S>(G.f, G.g, G.seg, G.codes, tile, verts, faces, normalize, v0, rec);
   }
 }
 
