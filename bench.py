@@ -21,6 +21,7 @@ the data path); the time is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import glob
 import json
 import os
 import re
@@ -40,7 +41,6 @@ import torch  # noqa: E402
 SEED = 2
 DEFORM = 0.45
 METRIC = "fwd+bwd grids/s @512^3 (DiffDMC, fp32, deform, return_quads)"
-PROFILE = os.path.join(ROOT, "profiles", "dmc_backward_512.txt")
 
 
 def spheres_field(n, device, dtype=torch.float32, seed=SEED):
@@ -290,14 +290,41 @@ class PhaseEvents:
         return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in self.done.items()}
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    try:
-        txt = open(PROFILE).read()
-    except OSError:
-        return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-    return float(m.group(1)) if m else None
+def kernel_bytes(vol, nseg, nv, nq, s):
+    """Algorithmic bytes of one launch of each kernel of the 512^3 DMC step: what the
+    kernel's function must read and write at least (nq crossing edges = quads, nv
+    patches = vertices, s bytes per scalar)."""
+    return {
+        # the SDF once; the scanned per-segment counts out
+        "count": vol * s + nseg * 8,
+        # segment counts in and out
+        "scan": 2 * nseg * 8,
+        # both end points of every crossing edge (SDF + deform) in; vertices, quads and
+        # the edge record (cell + axis, four patch ids, a byte per vertex) out
+        "emit": 2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8 + nq * (8 + 16) + nv,
+        # the two gradient arrays
+        "zero_grads": vol * 4 * s,
+        # per edge: record (cell, 4 patch ids), 4 patch bytes and 4 dL/dverts in, end points
+        # (SDF + deform) in, 2 x 4 adjoints out
+        "edge": nq * (8 + 16 + 4 + 4 * 3 * s + 2 * 4 * s + 8 * s),
+        # the adjoints of every edge, once from each end
+        "gather": nq * 8 * s,
+    }
+
+
+def read_profile_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summaries (None when
+    no summary covers it)."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.txt"))):
+        try:
+            txt = open(path).read()
+        except OSError:
+            continue
+        m = re.search(r"kernel:\s*(\S+)", txt)
+        t = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+        if m and t and m.group(1) == kernel:
+            return float(t.group(1))
+    return None
 
 
 def measured_peaks():
@@ -338,6 +365,7 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize()
     ph = PhaseEvents()
     X.phase_timer = ph
+    ext._ex.timing(True)  # CUDA events around every launch of the extractor, on its stream
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(smi_id(device)) as clk:
         t0.record()
@@ -346,6 +374,8 @@ def run_ours(args, rank, world, device):
         t1.record()
         torch.cuda.synchronize()
     X.phase_timer = None
+    kernels = ext._ex.timing_read()
+    ext._ex.timing(False)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -392,21 +422,17 @@ def run_ours(args, rank, world, device):
         torch.distributed.all_reduce(e_ms, op=torch.distributed.ReduceOp.MAX)
     e_ms = float(e_ms.item())
 
-    # roofline of the dominant phase
+    # roofline of the dominant kernel (per-launch event times of the timed region)
     s_b = 4
     vol = n ** 3
-    algo = {
-        # SDF read (the dense pass); the per-segment counts and their scan are design overhead
-        "count": vol * s_b,
-        # deform gathers at both ends of every crossing, SDF of the active tiles, vertices and quads out
-        "emit": 2 * nq * 3 * s_b + nv * 3 * s_b + nq * 4 * 8,
-        # SDF re-read, dL/dsdf and dL/ddeform written, dL/dverts read, deform gathered at crossings
-        "backward": vol * s_b * (1 + 1 + 3) + nv * 3 * s_b + 2 * nq * 3 * s_b,
-    }
-    dom = max((k for k in phases if k in algo), key=lambda k: phases[k])
+    nseg = (n + 1) ** 2 * ((n + 1 + 31) // 32)
+    algo = kernel_bytes(vol, nseg, nv, nq, s_b)
+    per_launch = {k: ms / max(cnt, 1) for k, (cnt, ms) in kernels.items()}
+    ours = {k: v for k, v in per_launch.items() if k in algo and k != "zero_grads"}
+    dom = max(ours, key=lambda k: ours[k] * kernels[k][0])
     peak, peak_kind = measured_peaks()
-    achieved = algo[dom] / (phases[dom] * 1e-3) / 1e9
-    traffic = read_profile_traffic() if dom == "backward" else None
+    achieved = algo[dom] / (per_launch[dom] * 1e-3) / 1e9
+    traffic = read_profile_traffic(dom)
     step_bytes = vol * s_b * (3 + 3) + 4 * nq * 3 * s_b + 2 * nv * 3 * s_b + 8 * nq * 4
     ms_step = ms_max / args.steps
     res = {
@@ -426,14 +452,17 @@ def run_ours(args, rank, world, device):
                    "deform": True, "normalize": True, "verts": nv, "quads": nq,
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
                    "phase_ms": {k: round(v, 4) for k, v in phases.items()},
+                   "kernel_ms_per_step": {k: round(ms / args.steps, 4) for k, (cnt, ms) in kernels.items()},
+                   "kernel_gbs": {k: round(algo[k] / (per_launch[k] * 1e-3) / 1e9, 1) for k in per_launch
+                                  if k in algo},
                    "step_algorithmic_gbs": step_bytes / (ms_step * 1e-3) / 1e9,
                    "step_hbm_frac": step_bytes / (ms_step * 1e-3) / 1e9 / peak},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes": algo[dom],
-                     "traffic": traffic},
+                     "ms_per_launch": per_launch[dom], "traffic": traffic},
         "e2e": {"value": world * e2e_steps / (e_ms / 1e3), "unit": "grids/s",
                 "h2d_bytes_per_step": int(sdf.numel() * 4 + deform.numel() * 4), "d2h_bytes_per_step": 4},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": sum(cnt for k, (cnt, _) in kernels.items() if k != "zero_grads"),
         "clocks": clk.summary(),
     }
     return res

@@ -19,9 +19,14 @@ LIB_PATH = os.path.join(HERE, "libdiso_gb300.so")
 MC, DMC = 0, 1
 F32, F64 = 0, 1
 GRAD_EXACT = 1
+GRAD_ZEROED = 2
 
 _lock = threading.Lock()
 _lib = None
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
 
 
 class Counts(ctypes.Structure):
@@ -58,6 +63,11 @@ EXPORTS = {
     "diso_forward_count_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
+    "diso_zero_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]),
     "diso_last_error": (ctypes.c_char_p, []),
     "diso_version": (ctypes.c_char_p, []),
 }
@@ -143,6 +153,17 @@ class Extractor:
                                        stream_of(sdf.device), ctypes.byref(c)), "forward count")
         return c
 
+    def timing(self, enable: bool):
+        """Time every kernel this extractor launches (CUDA events on each launch's stream)."""
+        check(lib().diso_timing(self._h, int(bool(enable))), "timing")
+
+    def timing_read(self) -> dict:
+        """{kernel: (launches, total ms)} of the launches since the last read."""
+        arr = (KernelTime * 16)()
+        n = ctypes.c_int(0)
+        check(lib().diso_timing_read(self._h, arr, 16, ctypes.byref(n)), "timing read")
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(n.value)}
+
     def record_slots(self, counts) -> int:
         """int64 slots of the edge record of a forward with these counts."""
         return int(lib().diso_edge_record_slots(self.method, dtype_tag(self.dtype), int(counts.n_verts),
@@ -160,8 +181,24 @@ class Extractor:
                                      stream_of(verts.device)), "quad split")
         return int(n.value)
 
+    def zero_grads(self, grad_sdf, grad_deform):
+        """Zero the gradient buffers on a second stream of this extractor, beside the
+        forward's kernels (see diso_zero_grads); the buffers are recorded on that
+        stream, so torch does not reuse their memory before the zeros land."""
+        dev = grad_sdf.device
+        side = getattr(self, "_side", None)
+        if side is None or side.device != dev:
+            side = self._side = torch.cuda.Stream(dev)
+        nb = lambda t: 0 if t is None else t.numel() * t.element_size()
+        check(lib().diso_zero_grads(self._h, ptr(grad_sdf), nb(grad_sdf), ptr(grad_deform), nb(grad_deform),
+                                    stream_of(dev), ctypes.c_void_p(side.cuda_stream)), "zero grads")
+        grad_sdf.record_stream(side)
+        if grad_deform is not None:
+            grad_deform.record_stream(side)
+
     def backward(self, sdf, deform, iso, pad, seg, record, normalize, grad_verts, grad_sdf, grad_deform,
-                 exact=False):
+                 exact=False, zeroed=False):
+        flags = (GRAD_EXACT if exact else 0) | (GRAD_ZEROED if zeroed else 0)
         check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg), ptr(record),
-                                  int(bool(normalize)), GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_sdf),
+                                  int(bool(normalize)), flags, ptr(grad_verts), ptr(grad_sdf),
                                   ptr(grad_deform), stream_of(sdf.device)), "backward")

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "../../include/diso_gb300.h"
 #include "kernels.cuh"
@@ -35,8 +36,23 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+// kernels timed by diso_timing
+enum KernelId {
+  K_COUNT, K_SCAN, K_EMIT, K_ZERO_GRADS, K_ZERO_TILES, K_ACTIVE_PTILES, K_EDGE, K_GATHER, K_SPLIT, K_NKERNELS
+};
+static const char* const kKernelNames[K_NKERNELS] = {"count",       "scan", "emit",   "zero_grads", "zero_tiles",
+                                                      "active_list", "edge", "gather", "split"};
+
 struct diso_extractor {
   int method = 0, dtype = 0, device = -1;
+  // optional timing of every launch (diso_timing): event pairs on the launch's stream
+  struct Timed {
+    int id;
+    cudaEvent_t a, b;
+  };
+  bool timing = false;
+  std::vector<Timed> timed;
+  std::vector<cudaEvent_t> event_pool;
   Stats* stats = nullptr;        // device status words
   Stats* stats_host = nullptr;   // pinned mirror
   uint32_t* scan_flag = nullptr; // look-back state
@@ -56,6 +72,7 @@ struct diso_extractor {
   int sms = 0;
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_zero = nullptr;  // end of the last diso_zero_grads on the side stream
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
   unsigned* plist_n = nullptr;
@@ -73,7 +90,29 @@ struct diso_extractor {
   int64_t bseg_off[MAX_BATCH + 1] = {};
   int bcount_ctas = 0, bwork_ctas = 0;
 
+  cudaEvent_t take_event() {
+    cudaEvent_t e = nullptr;
+    if (!event_pool.empty()) {
+      e = event_pool.back();
+      event_pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+      e = nullptr;
+    }
+    return e;
+  }
+
+  void release_events() {
+    for (const Timed& t : timed) {
+      cudaEventDestroy(t.a);
+      cudaEventDestroy(t.b);
+    }
+    for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+    timed.clear();
+    event_pool.clear();
+  }
+
   void release() {
+    release_events();
     cudaFree(bdesc);
     cudaFreeHost(bdesc_host);
     cudaFree(bstats);
@@ -99,8 +138,9 @@ struct diso_extractor {
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_zero) cudaEventDestroy(ev_zero);
     side = nullptr;
-    ev_fork = ev_join = nullptr;
+    ev_fork = ev_join = ev_zero = nullptr;
     plist = nullptr;
     plist_n = nullptr;
     plist_cap = 0;
@@ -114,6 +154,27 @@ struct diso_extractor {
 };
 
 namespace {
+
+// brackets one launch with timing events when the extractor's timing is on
+struct KernelTimer {
+  diso_extractor* ex;
+  int id;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr;
+  KernelTimer(diso_extractor* e, int k, cudaStream_t st) : ex(e), id(k), s(st) {
+    if (ex->timing && (a = ex->take_event())) cudaEventRecord(a, s);
+  }
+  ~KernelTimer() {
+    if (!a) return;
+    cudaEvent_t b = ex->take_event();
+    if (!b) {
+      ex->event_pool.push_back(a);
+      return;
+    }
+    cudaEventRecord(b, s);
+    ex->timed.push_back({id, a, b});
+  }
+};
 
 template <class T>
 int grow(T*& p, int64_t& cap, int64_t need) {
@@ -220,6 +281,9 @@ int bind_device(diso_extractor* ex) {
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_zero, cudaEventDisableTiming));
+    // recorded once so that a backward that waits on it before any zeroing proceeds
+    CUDA_TRY(cudaEventRecord(ex->ev_zero, ex->side));
     CUDA_TRY(cudaMalloc((void**)&ex->plist_n, sizeof(unsigned)));
   }
   return DISO_OK;
@@ -250,7 +314,10 @@ int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s) {
   CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
   CUDA_TRY(cudaMemsetAsync(&ex->stats->scan_tile, 0, sizeof(unsigned long long), s));
   ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
-  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats);
+  {
+    KernelTimer kt(ex, K_SCAN, s);
+    scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats);
+  }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
@@ -293,7 +360,9 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
   CUtensorMap wide, narrow;
-  if (count_tensor_maps<S>(sdf, nx, ny, nz, &wide, &narrow)) {
+  const bool tma = count_tensor_maps<S>(sdf, nx, ny, nz, &wide, &narrow);
+  KernelTimer* kt = new (std::nothrow) KernelTimer(ex, K_COUNT, s);
+  if (tma) {
     const int64_t units = count_tma_units(g);
     const int64_t want =
         std::max<int64_t>(ex->tma_ctas, (units * TMA_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
@@ -317,6 +386,7 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
       count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->codes, ex->stats,
                                                      ex->active);
   }
+  delete kt;  // the count's end event
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
@@ -353,6 +423,7 @@ int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx
   if (ex->last_active <= 0) return DISO_OK;
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const unsigned grid = (unsigned)ex->last_active;
+  KernelTimer kt(ex, K_EMIT, s);
   if (ex->method == DISO_MC)
     mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
   else
@@ -390,25 +461,54 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   g.init(nx, ny, nz);
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  const bool zeroed = (flags & DISO_GRAD_ZEROED) != 0;
   int rc;
   if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
-  if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
-  // few CTAs per SM, so that the gather of the active tiles finds room beside them
-  zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf, (S*)gdef);
-  CUDA_TRY(cudaGetLastError());
+  if (zeroed) {
+    CUDA_TRY(cudaStreamWaitEvent(s, ex->ev_zero, 0));
+  } else {
+    if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
+    // few CTAs per SM, so that the gather of the active tiles finds room beside them
+    KernelTimer kt(ex, K_ZERO_TILES, ex->side);
+    zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf,
+                                                                       (S*)gdef);
+    CUDA_TRY(cudaGetLastError());
+  }
   CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
-  active_ptiles_kernel<<<stride_ctas(g.nptiles(), ex->sms * 8), 256, 0, s>>>(g, tile_flags(seg, g), ex->plist,
-                                                                             ex->plist_n);
+  {
+    KernelTimer kt(ex, K_ACTIVE_PTILES, s);
+    active_ptiles_kernel<<<stride_ctas(g.nptiles(), ex->sms * 8), 256, 0, s>>>(g, tile_flags(seg, g), ex->plist,
+                                                                               ex->plist_n);
+  }
   CUDA_TRY(cudaGetLastError());
-  if (ex->method == DISO_MC)
-    edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, 0);
-  else
-    edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, exact);
+  {
+    KernelTimer kt(ex, K_EDGE, s);
+    if (ex->method == DISO_MC)
+      edge_adjoint_kernel<S, MC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, 0);
+    else
+      edge_adjoint_kernel<S, DMC><<<edge_ctas(ex), 256, 0, s>>>(f, g, seg, record, (const S*)gv, normalize, exact);
+  }
   CUDA_TRY(cudaGetLastError());
-  gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(f, g, seg, ex->plist, ex->plist_n, record,
-                                                                      (S*)gsdf, (S*)gdef);
+  {
+    KernelTimer kt(ex, K_GATHER, s);
+    gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(f, g, seg, ex->plist, ex->plist_n, record,
+                                                                        (S*)gsdf, (S*)gdef);
+  }
   CUDA_TRY(cudaGetLastError());
-  return side_join(ex, s);
+  return zeroed ? DISO_OK : side_join(ex, s);
+}
+
+int zero_grads(diso_extractor* ex, void* gsdf, int64_t sb, void* gdef, int64_t db, cudaStream_t s,
+               cudaStream_t z) {
+  CUDA_TRY(cudaEventRecord(ex->ev_fork, s));
+  CUDA_TRY(cudaStreamWaitEvent(z, ex->ev_fork, 0));
+  {
+    KernelTimer kt(ex, K_ZERO_GRADS, z);
+    if (sb) CUDA_TRY(cudaMemsetAsync(gsdf, 0, (size_t)sb, z));
+    if (db) CUDA_TRY(cudaMemsetAsync(gdef, 0, (size_t)db, z));
+  }
+  CUDA_TRY(cudaEventRecord(ex->ev_zero, z));
+  return DISO_OK;
 }
 
 template <class S>
@@ -419,6 +519,7 @@ int split_quads(diso_extractor* ex, const void* verts, const int64_t* quads, int
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
   const int threads = 256;
   const unsigned blocks = (unsigned)((nq + threads - 1) / threads);
+  KernelTimer kt(ex, K_SPLIT, s);
   split_count_kernel<S><<<blocks, threads, 0, s>>>((const S*)verts, quads, nq, ex->split);
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, ex->split, nq, s)) != DISO_OK) return rc;
@@ -763,6 +864,17 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                                                   deform ? grad_deform : nullptr, s);
 }
 
+int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void* grad_deform, int64_t deform_bytes,
+                    void* stream, void* zero_stream) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (sdf_bytes < 0 || deform_bytes < 0 || (sdf_bytes && !grad_sdf) || (deform_bytes && !grad_deform))
+    return fail(DISO_ERR_ARG, "bad gradient buffers");
+  int rc = bind_device(ex);
+  if (rc) return rc;
+  cudaStream_t z = zero_stream ? (cudaStream_t)zero_stream : ex->side;
+  return zero_grads(ex, grad_sdf, sdf_bytes, grad_deform, deform_bytes, (cudaStream_t)stream, z);
+}
+
 int64_t diso_batch_record_slots(const diso_grid* grids, int ngrids) {
   if (!grids || ngrids < 1 || ngrids > MAX_BATCH) return 0;
   return batch_record_slots(grids, ngrids, nullptr, nullptr);
@@ -825,6 +937,43 @@ int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void
   cudaStream_t s = (cudaStream_t)stream;
   return ex->dtype == DISO_F32 ? batch_backward<float>(ex, normalize, flags, grad_verts, edge_record, vcap, fcap, s)
                                : batch_backward<double>(ex, normalize, flags, grad_verts, edge_record, vcap, fcap, s);
+}
+
+int diso_timing(diso_extractor* ex, int enable) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  ex->timing = enable != 0;
+  for (const diso_extractor::Timed& t : ex->timed) {
+    ex->event_pool.push_back(t.a);
+    ex->event_pool.push_back(t.b);
+  }
+  ex->timed.clear();
+  return DISO_OK;
+}
+
+int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n) {
+  if (!ex || !n || (max > 0 && !out)) return fail(DISO_ERR_ARG, "null extractor or output");
+  double ms[K_NKERNELS] = {};
+  int64_t launches[K_NKERNELS] = {};
+  for (const diso_extractor::Timed& t : ex->timed) {
+    CUDA_TRY(cudaEventSynchronize(t.b));
+    float e = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&e, t.a, t.b));
+    ms[t.id] += e;
+    launches[t.id] += 1;
+  }
+  diso_timing(ex, ex->timing ? 1 : 0);  // recycle the events
+  int k = 0;
+  for (int i = 0; i < K_NKERNELS; ++i) {
+    if (!launches[i]) continue;
+    if (k < max) {
+      snprintf(out[k].name, sizeof out[k].name, "%s", kKernelNames[i]);
+      out[k].launches = launches[i];
+      out[k].total_ms = ms[i];
+    }
+    ++k;
+  }
+  *n = std::min(k, max);
+  return DISO_OK;
 }
 
 const char* diso_last_error(void) { return g_err; }

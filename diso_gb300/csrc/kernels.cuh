@@ -321,6 +321,7 @@ struct CountShared {
   int64_t rowoff[CROWS];       // offset of point row r in the SDF, -1 outside the grid
   uint32_t bal[CROWS];         // ballots of the chunk just read (each row read and used by one warp)
   uint32_t act[CP], actc[CP], actf[CP];
+  uint32_t mixed[3];                       // per chunk (rotating): OR of count_combine's bits
   __align__(16) uint8_t code[CP][32][TZ];  // Morton codes of each lane's segment (staging)
   int list[COUNT_LIST];
   int nlist, base;
@@ -470,18 +471,44 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
 // row masks of chunk t - 1 from the ballots of chunk t in sh.bal and the history of
 // the lane's rows (i = lane, lane + 32 of this warp): p2 = chunk t - 2, p1 = chunk t - 1;
 // vrows: bit i = the warp's point row i lies in the grid (used rows only)
+// (written masks only) bit 0: one of them is not all ones, bit 1: one is not all zeros
 template <class S, int METHOD>
-__device__ __forceinline__ void count_combine(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
-                                              uint32_t (&p2)[2]) {
+__device__ __forceinline__ uint32_t count_combine(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
+                                                  uint32_t (&p2)[2]) {
+  constexpr uint64_t ALL = (1ull << (MASK_TOP + 1)) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t mixed = 0;
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const int i = lane + 32 * k, r = warp + 8 * i;
     if (i < CRPW && r < CROWS) {
       const uint32_t cur = sh.bal[r];
-      if (write) (&sh.m[0][0])[r] = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
+      if (write) {
+        const uint64_t m = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
+        (&sh.m[0][0])[r] = m;
+        mixed |= (m != ALL ? 1u : 0u) | (m != 0 ? 2u : 0u);
+      }
       p2[k] = p1[k];
       p1[k] = cur;
+    }
+  }
+  return mixed;
+}
+
+// A chunk whose masks are all ones or all zeros has no non-trivial cell: its
+// segments count zero and its tiles are idle, with no shared-memory work.
+template <class S, int METHOD>
+__device__ __forceinline__ void count_chunk_empty(const Geom& g, uint64_t* __restrict__ seg,
+                                                  uint8_t* __restrict__ tile_flag, int X0, int Y0, int tz) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int X = X0 + warp, Y = Y0 + lane;
+  if (X < g.c[0] && Y < g.c[1]) seg[g.seg(X, Y, tz)] = 0;
+  if (threadIdx.x < (CP / TX) * (CR / TY)) {
+    const int tx = X0 / TX + threadIdx.x / (CR / TY), ty = Y0 / TY + threadIdx.x % (CR / TY);
+    if (tx < g.tiles_x() && ty < g.tiles_y()) {
+      const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
+      tile_flag[tile] = 0;
+      tile_flag[g.ntiles() + tile] = 0;
     }
   }
 }
@@ -491,7 +518,8 @@ __device__ __forceinline__ void count_combine(CountShared<S, METHOD>& sh, bool w
 template <class S, int METHOD>
 __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
-                                           uint8_t* __restrict__ codes, Stats* stats, int64_t unit, int tag) {
+                                           uint8_t* __restrict__ codes, Stats* stats, int64_t unit, int tag,
+                                           int64_t& ck) {
   // a row of nzc chunks is cut into nbz near-equal runs of at most KZ chunks
   const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
   const int tz0 = (int)(unit % nbz) * kz;
@@ -514,10 +542,20 @@ __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Fie
 #pragma unroll 1
   for (int t = tz0 - 1; t <= tz1; ++t) {
     count_ballots<S, METHOD>(sh, f, t, t < tz0 ? 0xc0000000u : (t == tz1 ? 1u : 0xffffffffu), mn, mx);
-    count_combine<S, METHOD>(sh, t >= tz0 + 1, p1, p2);
+    const uint32_t mixed = count_combine<S, METHOD>(sh, t >= tz0 + 1, p1, p2);
     if (t < tz0 + 1) continue;
+    // slots rotate over the CTA's chunks: slot (ck+2)%3 was last read before the
+    // previous barrier and is next written after the next one
+    const int slot = (int)(ck % 3);
+    if (mixed) atomicOr(&sh.mixed[slot], mixed);
     __syncthreads();
-    count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, X0, Y0, t - 1, tag);
+    const uint32_t mx3 = sh.mixed[slot];
+    if (threadIdx.x == 0) sh.mixed[(ck + 2) % 3] = 0;
+    ++ck;
+    if (mx3 == 3u)
+      count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, X0, Y0, t - 1, tag);
+    else
+      count_chunk_empty<S, METHOD>(g, seg, tile_flag, X0, Y0, t - 1);
   }
   publish_minmax<S>(stats, mn, mx);
 }
@@ -538,11 +576,15 @@ __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, 
                                                             uint8_t* __restrict__ codes, Stats* stats,
                                                             int* __restrict__ active) {
   __shared__ CountShared<S, METHOD> sh;
-  if (threadIdx.x == 0) sh.nlist = 0;
+  if (threadIdx.x == 0) {
+    sh.nlist = 0;
+    sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
+  }
   const int64_t nunits = count_units(g);
+  int64_t ck = 0;  // chunks this CTA has counted
 #pragma unroll 1
   for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x)
-    count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, u, 0);
+    count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, u, 0, ck);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
 
@@ -688,6 +730,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   const int64_t nunits = count_tma_units(g);
   if (threadIdx.x == 0) {
     sh.nlist = 0;
+    sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
 #pragma unroll
     for (int st = 0; st < TMA_STAGES; ++st) mbar_init(&full[st], 1);
     mbar_fence_init();
@@ -726,19 +769,32 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
     const bool ok = mbar_wait_bounded(&full[st], (uint32_t)((k / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
     box_ballots<S, METHOD>(sh, f, reinterpret_cast<const S*>(stage_mem + st * tma_box_bytes<S>()), cc.t, cc.kind(),
                            vrows, mn, mx);
-    count_combine<S, METHOD>(sh, cc.t >= cc.tz0 + 1, p1, p2);
+    const uint32_t mixed = count_combine<S, METHOD>(sh, cc.t >= cc.tz0 + 1, p1, p2);
+    // slots rotate over the CTA's boxes: slot (k+2)%3 was last read before the
+    // previous barrier and is next written after the next one
+    const int slot = (int)(k % 3);
+    if (mixed) atomicOr(&sh.mixed[slot], mixed);
     // every warp is done with the stage (and sh.m is complete): refill the stage
     if (__syncthreads_or(!ok)) {
       failed = true;
       break;
     }
-    if (threadIdx.x == 0 && pc.valid(nunits)) {
-      fence_proxy_async();
-      issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
-      pc.next(g, nunits);
-      ++issued;
+    const uint32_t mx3 = sh.mixed[slot];
+    if (threadIdx.x == 0) {
+      sh.mixed[(k + 2) % 3] = 0;
+      if (pc.valid(nunits)) {
+        fence_proxy_async();
+        issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
+        pc.next(g, nunits);
+        ++issued;
+      }
     }
-    if (cc.t >= cc.tz0 + 1) count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, cc.X0, cc.Y0, cc.t - 1, 0);
+    if (cc.t >= cc.tz0 + 1) {
+      if (mx3 == 3u)
+        count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, cc.X0, cc.Y0, cc.t - 1, 0);
+      else
+        count_chunk_empty<S, METHOD>(g, seg, tile_flag, cc.X0, cc.Y0, cc.t - 1);
+    }
     cc.next(g, nunits);
   }
   if (failed && threadIdx.x == 0) {
@@ -793,13 +849,18 @@ __global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGri
   __shared__ CountShared<S, METHOD> sh;
   __shared__ int64_t start[MAX_BATCH];
   for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].cblk0;
-  if (threadIdx.x == 0) sh.nlist = 0;
+  if (threadIdx.x == 0) {
+    sh.nlist = 0;
+    sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
+  }
   __syncthreads();
+  int64_t ck = 0;  // chunks this CTA has counted
 #pragma unroll 1
   for (int64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
     const int i = batch_find(start, ngrids, b);
     const BatchGrid<S>& G = grids[i];
-    count_unit<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, G.codes, stats + i, b - start[i], i << BATCH_TILE_BITS);
+    count_unit<S, METHOD>(sh, G.f, G.g, G.seg, G.tile_flag, G.codes, stats + i, b - start[i], i << BATCH_TILE_BITS,
+                          ck);
   }
   count_flush<S, METHOD>(sh, n_active, active);
 }

@@ -11,9 +11,9 @@ Differences that are invisible to callers of the reference API:
   reference syncs for min, max and three output sizes);
 * the backward does not re-run the forward (diso/__init__.py:32, 86): the
   forward records every crossing edge (its cell and axis, for DMC the patches
-  around it) when a gradient will be wanted; the backward computes each edge's
-  adjoint once and then writes every gradient element once, deterministically
-  (no atomics);
+  around it) when a gradient will be wanted and zeroes the gradient buffers beside
+  its count; the backward computes each edge's adjoint once and writes the
+  gradients near the surface, deterministically (no atomics);
 * vertices are shifted and normalised, and faces written as int64, inside the
   kernels; the DMC quad split runs on the GPU in one pass plus a scan.
 
@@ -60,17 +60,19 @@ class _ExtractFunction(Function):
     DDMCFunction (diso/__init__.py:18-46, 72-100)."""
 
     @staticmethod
-    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad):
+    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads):
         g = grid.detach().contiguous()
         d = deform.detach().contiguous() if deform is not None else None
         nv, nf = int(counts.n_verts), int(counts.n_faces)
         width = 3 if ex.method == N.MC else 4
         verts = torch.empty((nv, 3), dtype=g.dtype, device=g.device)
         faces = torch.empty((nf, width), dtype=torch.int64, device=g.device)
-        # the edge record only when a gradient can be asked for
+        # the edge record only when a gradient can be asked for (the gradient buffers,
+        # zeroed beside the count, come with it)
         wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
         record = (torch.empty(max(1, ex.record_slots(counts)), dtype=torch.int64, device=g.device)
                   if wants_grad else None)
+        ctx.gs, ctx.gd = grads if (wants_grad and grads is not None) else (None, None)
         _mark("emit", "start")
         ex.emit(g, d, iso, pad, seg, normalize, verts, faces, record)
         _mark("emit", "end")
@@ -97,12 +99,17 @@ class _ExtractFunction(Function):
             if grad_verts is None:
                 grad_verts = torch.zeros(0, 3, dtype=g.dtype, device=g.device)
             gv = grad_verts.contiguous()
-            gs = torch.empty_like(g)
-            gd = torch.empty_like(d) if d is not None else None
+            gs, gd = ctx.gs, ctx.gd
+            zeroed = gs is not None
+            if not zeroed:  # a second backward of the same graph (retain_graph)
+                gs = torch.empty_like(g)
+                gd = torch.empty_like(d) if d is not None else None
+            ctx.gs = ctx.gd = None
             _mark("backward", "start")
-            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad)
+            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
+                            zeroed=zeroed)
             _mark("backward", "end")
-        return gs, gd, None, None, None, None, None, None, None, None
+        return gs, gd, None, None, None, None, None, None, None, None, None
 
 
 def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
@@ -117,6 +124,14 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
     with torch.cuda.device(grid.device):
         g = grid.detach().contiguous()
         seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=g.device)
+        # When a gradient can be asked for, its buffers are allocated now and zeroed on
+        # a second stream while the count runs (the count reads HBM far below its
+        # bandwidth); the backward then writes only the point tiles near the surface.
+        grads = None
+        if torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad)):
+            grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=g.device)
+                     if deform is not None else None)
+            ex.zero_grads(*grads)
         _mark("count", "start")
         counts = ex.count(g, iso, pad, seg)
         _mark("count", "end")
@@ -125,7 +140,7 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
             return (torch.zeros((0, 3), dtype=ex.dtype, device=grid.device),
                     torch.zeros((0, width), dtype=torch.int32, device=grid.device))
         return _ExtractFunction.apply(grid, deform, ex, seg, counts, iso, pad, bool(normalize), bool(return_quads),
-                                      bool(exact_grad))
+                                      bool(exact_grad), grads)
 
 
 class DiffMC(nn.Module):

@@ -43,7 +43,7 @@ extern "C" {
 
 enum { DISO_MC = 0, DISO_DMC = 1 };
 enum { DISO_F32 = 0, DISO_F64 = 1 };
-enum { DISO_GRAD_EXACT = 1 }; /* diso_backward flag, see there */
+enum { DISO_GRAD_EXACT = 1, DISO_GRAD_ZEROED = 2 }; /* diso_backward flags, see there */
 enum {
   DISO_OK = 0,
   DISO_ERR_ARG = 1,      /* bad argument (size, null pointer, method, dtype) */
@@ -111,8 +111,9 @@ int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads
 /* Backward: dL/dsdf [nx][ny][nz] and dL/ddeform [nx][ny][nz][3] (when deform is
  * not NULL) from dL/dverts [n_verts][3] of the final (shifted, normalised)
  * vertices, with the `seg` and the edge record of the forward (the record's
- * adjoint slots are overwritten).  Every element of both outputs is written;
- * nothing needs zeroing; the result is deterministic (no atomics).
+ * adjoint slots are overwritten).  Every element of both outputs is written
+ * (with DISO_GRAD_ZEROED: the buffers were zeroed by diso_zero_grads and only the
+ * point tiles near the surface are written); the result is deterministic (no atomics).
  * flags = 0 reproduces the reference's gradients exactly, including its DMC
  * backward, which hands every patch of a multi-patch cell the gradient of the
  * cell's first patch (src/cudualmc.cu:990); flags = DISO_GRAD_EXACT gives the
@@ -123,6 +124,16 @@ int diso_split_quads(diso_extractor* ex, const void* verts, const int64_t* quads
 int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
                   double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
                   const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
+
+/* Zero a forward's gradient buffers ahead of its backward, on `zero_stream` (after
+ * the work already queued on `stream`), so that the writes overlap the forward's
+ * kernels, which leave HBM bandwidth unused; the caller keeps the buffers alive until
+ * that stream has passed them (e.g. torch's Tensor.record_stream).  A later
+ * diso_backward on the same extractor with flags | DISO_GRAD_ZEROED waits for the
+ * zeros and writes only the point tiles near the surface.  No counterpart in the
+ * reference (its backward zero-fills the padded gradients, diso/__init__.py:35-37, 89-91). */
+int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void* grad_deform, int64_t deform_bytes,
+                    void* stream, void* zero_stream);
 
 /* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
  * device memory: code running while a stream is being captured, where cudaMalloc
@@ -192,6 +203,23 @@ int diso_batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap
  * grad_deform (flags as for diso_backward).  Grids that the emit skipped get zero gradients. */
 int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void* grad_verts, uint64_t* edge_record,
                         int64_t vcap, int64_t fcap, void* stream);
+
+/* ---------------------------------------------------------------- timing
+ *
+ * Optional timing of every kernel an extractor launches, for benchmarks: with
+ * timing on, each launch is bracketed by CUDA events on its own stream. */
+typedef struct {
+  char name[32];     /* count, scan, emit, zero_grads, zero_tiles, active_list, edge, gather, split */
+  int64_t launches;
+  double total_ms;   /* summed event time of those launches */
+} diso_kernel_time;
+
+/* Turn timing on (enable != 0) or off; drops the launches recorded so far. */
+int diso_timing(diso_extractor* ex, int enable);
+
+/* Per-kernel totals of the launches recorded since the last call (waits for their
+ * end events), at most `max` entries, *n = entries written; then starts over. */
+int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* diso_last_error(void);

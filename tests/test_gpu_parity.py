@@ -192,6 +192,29 @@ def test_backward_is_deterministic(cuda_device):
     assert torch.equal(grads[0], grads[1])
 
 
+def test_second_backward_and_forward_without_backward(cuda_device):
+    # the gradient buffers are zeroed during the forward and filled by the first
+    # backward; a second backward of the same graph (retain_graph) and forwards whose
+    # outputs are dropped before any backward give the same gradients
+    from diso_gb300 import DiffDMC, DiffMC
+
+    rng = np.random.default_rng(3)
+    sdf = torch.tensor(rng.uniform(-1, 1, (36, 28, 44)).astype(np.float32), device=cuda_device)
+    dfm = torch.tensor(rng.uniform(-0.3, 0.3, (36, 28, 44, 3)).astype(np.float32), device=cuda_device)
+    for mod in (DiffMC(torch.float32), DiffDMC(torch.float32)):
+        s = sdf.clone().requires_grad_(True)
+        d = dfm.clone().requires_grad_(True)
+        for _ in range(3):  # forwards without backward: their zeroed buffers are released
+            mod(s, d)
+        v, _ = mod(s, d)
+        loss = (v * v).sum()
+        loss.backward(retain_graph=True)
+        g1, d1 = s.grad.clone(), d.grad.clone()
+        loss.backward()
+        assert torch.equal(s.grad, 2 * g1) and torch.equal(d.grad, 2 * d1)
+        assert g1.abs().sum() > 0 and d1.abs().sum() > 0
+
+
 def test_empty_guard_and_errors(cuda_device):
     from diso_gb300 import DiffDMC, DiffMC
 
