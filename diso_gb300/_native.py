@@ -36,7 +36,7 @@ class Counts(ctypes.Structure):
         ("sdf_min", ctypes.c_double),
         ("sdf_max", ctypes.c_double),
         ("empty", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("emitted", ctypes.c_int32),
         ("n_active_tiles", ctypes.c_int64),
     ]
 
@@ -54,6 +54,10 @@ EXPORTS = {
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p]),
     "diso_edge_record_slots": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64]),
+    "diso_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
     "diso_split_quads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
     "diso_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
@@ -164,10 +168,20 @@ class Extractor:
         check(lib().diso_timing_read(self._h, arr, 16, ctypes.byref(n)), "timing read")
         return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(n.value)}
 
-    def record_slots(self, counts) -> int:
+    def record_slots(self, counts=None, n_verts=None, n_faces=None) -> int:
         """int64 slots of the edge record of a forward with these counts."""
-        return int(lib().diso_edge_record_slots(self.method, dtype_tag(self.dtype), int(counts.n_verts),
-                                                int(counts.n_faces)))
+        nv = int(counts.n_verts) if counts is not None else int(n_verts)
+        nf = int(counts.n_faces) if counts is not None else int(n_faces)
+        return int(lib().diso_edge_record_slots(self.method, dtype_tag(self.dtype), nv, nf))
+
+    def forward(self, sdf, deform, iso, pad, seg, normalize, verts, faces, record) -> Counts:
+        """Count, scan and emit into outputs of the given capacities in one call;
+        Counts.emitted says whether they fitted (see diso_forward)."""
+        c = Counts()
+        check(lib().diso_forward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg), int(bool(normalize)),
+                                 ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], ptr(record),
+                                 stream_of(sdf.device), ctypes.byref(c)), "forward")
+        return c
 
     def emit(self, sdf, deform, iso, pad, seg, normalize, verts, faces, record=None):
         check(lib().diso_forward_emit(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),

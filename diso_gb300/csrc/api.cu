@@ -69,10 +69,12 @@ struct diso_extractor {
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
   int tma_ctas = 0;              // the same for the TMA count kernel
   int gather_ctas = 0;           // the same for the point gather
+  int emit_ctas = 0;             // the same for the emit
   int sms = 0;
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_zero = nullptr;  // end of the last diso_zero_grads on the side stream
+  cudaEvent_t ev_counts = nullptr;  // the count's results are on the host
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
   unsigned* plist_n = nullptr;
@@ -139,8 +141,9 @@ struct diso_extractor {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (ev_zero) cudaEventDestroy(ev_zero);
+    if (ev_counts) cudaEventDestroy(ev_counts);
     side = nullptr;
-    ev_fork = ev_join = ev_zero = nullptr;
+    ev_fork = ev_join = ev_zero = ev_counts = nullptr;
     plist = nullptr;
     plist_n = nullptr;
     plist_cap = 0;
@@ -278,10 +281,21 @@ int bind_device(diso_extractor* ex) {
     else
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_g, gather_list_kernel<double>, NTHREADS, 0));
     ex->gather_ctas = sms * std::max(per_g, 1);
+    int per_e = 0;
+    if (ex->dtype == DISO_F32)
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_e, ex->method == DISO_MC ? (const void*)mc_emit_kernel<float> : (const void*)dmc_emit_kernel<float>,
+          NTHREADS, 0));
+    else
+      CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_e, ex->method == DISO_MC ? (const void*)mc_emit_kernel<double> : (const void*)dmc_emit_kernel<double>,
+          NTHREADS, 0));
+    ex->emit_ctas = sms * std::max(per_e, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_zero, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_counts, cudaEventDisableTiming));
     // recorded once so that a backward that waits on it before any zeroing proceeds
     CUDA_TRY(cudaEventRecord(ex->ev_zero, ex->side));
     CUDA_TRY(cudaMalloc((void**)&ex->plist_n, sizeof(unsigned)));
@@ -349,8 +363,8 @@ Field<S> make_field(const void* sdf, const void* deform, int nx, int ny, int nz,
 }
 
 template <class S>
-int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double iso, double padval,
-                  uint64_t* seg, cudaStream_t s, diso_counts* out) {
+int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double iso, double padval,
+                 uint64_t* seg, cudaStream_t s) {
   Geom g;
   g.init(nx, ny, nz);
   int rc;
@@ -388,12 +402,30 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   }
   delete kt;  // the count's end event
   CUDA_TRY(cudaGetLastError());
-  if ((rc = run_scan(ex, seg, g.nseg, s)) != DISO_OK) return rc;
+  return run_scan(ex, seg, g.nseg, s);
+}
+
+// the count's results to the host (into the pinned stats mirror; its pad[0] takes the
+// scanned total), then an event
+template <class S>
+int count_copy(diso_extractor* ex, const Geom& g, const uint64_t* seg, cudaStream_t s) {
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
-  uint64_t total = 0;
-  CUDA_TRY(cudaMemcpyAsync(&total, seg + g.nseg, sizeof total, cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
+  CUDA_TRY(cudaMemcpyAsync(&ex->stats_host->pad[0], seg + g.nseg, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaEventRecord(ex->ev_counts, s));
+  return DISO_OK;
+}
+
+// waits for count_copy's event and fills `out`
+template <class S>
+int count_read(diso_extractor* ex, int nx, int ny, int nz, double iso, const uint64_t* seg, cudaStream_t s,
+               diso_counts* out) {
+  Geom g;
+  g.init(nx, ny, nz);
+  (void)seg;
+  (void)s;
+  CUDA_TRY(cudaEventSynchronize(ex->ev_counts));
   const Stats& h = *ex->stats_host;
+  const uint64_t total = h.pad[0];
   if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
   if (h.error & 4ull) return fail(DISO_ERR_SCAN, "count: wait for a TMA copy gave up");
   // the low half counts crossings, the high half triangles (MC) or patches (DMC)
@@ -408,9 +440,41 @@ int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, d
   out->sdf_max = key_to_double(h.max_key);
   const double isoS = (double)(S)iso;
   out->empty = (out->sdf_min >= isoS || out->sdf_max <= isoS) ? 1 : 0;
-  out->pad_ = 0;
+  out->emitted = 0;
   out->n_active_tiles = (int64_t)h.n_active;
   ex->last_active = out->n_active_tiles;
+  return DISO_OK;
+}
+
+template <class S>
+int forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double iso, double padval,
+                  uint64_t* seg, cudaStream_t s, diso_counts* out) {
+  Geom g;
+  g.init(nx, ny, nz);
+  int rc;
+  if ((rc = count_launch<S>(ex, sdf, nx, ny, nz, iso, padval, seg, s)) != DISO_OK) return rc;
+  if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
+  return count_read<S>(ex, nx, ny, nz, iso, seg, s, out);
+}
+
+// the emit over the count's active tiles (persistent, `grid` CTAs); the outputs are
+// written only when they fit the capacities
+template <class S>
+int emit_launch(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
+                double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, void* record,
+                unsigned grid, int64_t vcap, int64_t fcap, cudaStream_t s) {
+  Geom g;
+  g.init(nx, ny, nz);
+  Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
+  CUDA_TRY(cudaMemsetAsync(&ex->stats->emit_tile, 0, sizeof(unsigned long long), s));
+  KernelTimer kt(ex, K_EMIT, s);
+  if (ex->method == DISO_MC)
+    mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, &ex->stats->n_active, (S*)verts, faces,
+                                                normalize, record, vcap, fcap, ex->stats);
+  else
+    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->codes, ex->active, &ex->stats->n_active, (S*)verts,
+                                                 faces, normalize, record, vcap, fcap, ex->stats);
+  CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
 
@@ -418,18 +482,29 @@ template <class S>
 int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
                  double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, void* record,
                  cudaStream_t s) {
+  if (ex->last_active <= 0) return DISO_OK;
+  const unsigned grid = (unsigned)std::min<int64_t>(ex->last_active, ex->emit_ctas);
+  return emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record, grid,
+                        INT64_MAX, INT64_MAX, s);
+}
+
+// count, scan and an emit into outputs of the given capacities, with one
+// synchronisation at the end (counts->emitted says whether the outputs were written)
+template <class S>
+int forward_all(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
+                double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces,
+                int64_t fcap, void* record, cudaStream_t s, diso_counts* out) {
   Geom g;
   g.init(nx, ny, nz);
-  if (ex->last_active <= 0) return DISO_OK;
-  Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
-  const unsigned grid = (unsigned)ex->last_active;
-  KernelTimer kt(ex, K_EMIT, s);
-  if (ex->method == DISO_MC)
-    mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, (S*)verts, faces, normalize, record);
-  else
-    dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->codes, ex->active, (S*)verts, faces, normalize,
-                                                 record);
-  CUDA_TRY(cudaGetLastError());
+  int rc;
+  if ((rc = count_launch<S>(ex, sdf, nx, ny, nz, iso, padval, seg, s)) != DISO_OK) return rc;
+  if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
+  // the emit is queued before the host waits for the counts, and still runs when it returns
+  if ((rc = emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record,
+                           (unsigned)ex->emit_ctas, vcap, fcap, s)) != DISO_OK)
+    return rc;
+  if ((rc = count_read<S>(ex, nx, ny, nz, iso, seg, s, out)) != DISO_OK) return rc;
+  out->emitted = (out->n_verts <= vcap && out->n_faces <= fcap) ? 1 : 0;
   return DISO_OK;
 }
 
@@ -755,7 +830,7 @@ int batch_results(diso_extractor* ex, diso_counts* out, int64_t* voff, int64_t* 
     out[i].sdf_min = key_to_double(h.min_key);
     out[i].sdf_max = key_to_double(h.max_key);
     out[i].empty = 0;  // the caller applies the guard with its own isovalue (see diso_batch_results)
-    out[i].pad_ = 0;
+    out[i].emitted = 0;
     out[i].n_active_tiles = 0;
     if (voff) voff[i] = va;
     if (foff) foff[i] = fa;
@@ -821,6 +896,21 @@ int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, i
                                                      verts, faces, edge_record, s)
                                : forward_emit<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
                                                       verts, faces, edge_record, s);
+}
+
+int diso_forward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
+                 double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                 uint64_t* edge_record, void* stream, diso_counts* out) {
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc) return rc;
+  if (!seg || !out) return fail(DISO_ERR_ARG, "null seg or counts");
+  if (vcap < 0 || fcap < 0 || (vcap && !verts) || (fcap && !faces)) return fail(DISO_ERR_ARG, "bad output buffers");
+  if (((uintptr_t)edge_record & 31u) != 0) return fail(DISO_ERR_ARG, "edge record must be 32-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? forward_all<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
+                                                    verts, vcap, faces, fcap, edge_record, s, out)
+                               : forward_all<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, normalize,
+                                                     verts, vcap, faces, fcap, edge_record, s, out);
 }
 
 int64_t diso_edge_record_slots(int method, int dtype, int64_t n_verts, int64_t n_faces) {
@@ -1070,7 +1160,7 @@ int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sd
   out->sdf_max = key_to_double(h.max_key);
   const double isoS = (double)(S)iso;
   out->empty = (out->sdf_min >= isoS || out->sdf_max <= isoS) ? 1 : 0;
-  out->pad_ = 0;
+  out->emitted = 0;
   out->n_active_tiles = (int64_t)h.n_active;
   return DISO_OK;
 }

@@ -186,9 +186,11 @@ struct Stats {
   unsigned long long min_key;   // order key of min(sdf)
   unsigned long long max_key;   // order key of max(sdf)
   unsigned long long n_active;  // active forward tiles
-  unsigned long long error;     // bit 0: scan look-back gave up, bit 1: output capacity exceeded
+  unsigned long long error;     // bit 0: scan look-back gave up, bit 1: output capacity exceeded,
+                                // bit 2: a TMA wait gave up
   unsigned long long scan_tile; // dynamic tile counter of the look-back scan
-  unsigned long long pad[3];
+  unsigned long long emit_tile; // dynamic tile counter of the emit
+  unsigned long long pad[2];
 };
 
 }  // namespace diso

@@ -1040,13 +1040,40 @@ __device__ __forceinline__ EdgeRecord<S> grid_record(void* record, const Geom& g
   return edge_record<S>(record, METHOD, METHOD == MC ? Counts::lo(tot) : Counts::hi(tot), Counts::lo(tot));
 }
 
+// Whether the outputs of the grid's scanned totals fit the capacities (vcap vertices,
+// fcap faces); when not, nothing is emitted and bit 1 of stats->error is set.
+template <int METHOD>
+__device__ __forceinline__ bool emit_fits(const Geom& g, const uint64_t* __restrict__ seg, int64_t vcap, int64_t fcap,
+                                          Stats* stats) {
+  const uint64_t tot = seg[g.nseg];
+  const int64_t V = METHOD == MC ? Counts::lo(tot) : Counts::hi(tot), F = METHOD == MC ? Counts::hi(tot) : Counts::lo(tot);
+  if (V <= vcap && F <= fcap) return true;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&stats->error, 2ull);
+  return false;
+}
+
+// persistent over the *n_active active tiles of the count, taken in turn from a
+// counter (tiles differ much in cost)
 template <class S>
 __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                           const int* __restrict__ active, S* __restrict__ verts,
-                                                           int64_t* __restrict__ faces, int normalize,
-                                                           void* record) {
+                                                           const int* __restrict__ active,
+                                                           const unsigned long long* __restrict__ n_active,
+                                                           S* __restrict__ verts, int64_t* __restrict__ faces,
+                                                           int normalize, void* record, int64_t vcap, int64_t fcap,
+                                                           Stats* stats) {
+  if (!emit_fits<MC>(g, seg, vcap, fcap, stats)) return;
   const EdgeRecord<S> rec = grid_record<S, MC>(record, g, seg);
-  mc_emit_tile<S>(f, g, seg, active[blockIdx.x], verts, faces, normalize, 0, rec);
+  const int64_t n = (int64_t)*n_active;
+  __shared__ int64_t next;
+#pragma unroll 1
+  for (;;) {
+    if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
+    __syncthreads();
+    const int64_t t = next;
+    __syncthreads();
+    if (t >= n) break;
+    mc_emit_tile<S>(f, g, seg, active[t], verts, faces, normalize, 0, rec);
+  }
 }
 
 // ------------------------------------------------------------------ DMC emit
@@ -1318,11 +1345,24 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
 template <class S>
 __global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                                const uint8_t* __restrict__ codes,
-                                                               const int* __restrict__ active, S* __restrict__ verts,
-                                                            int64_t* __restrict__ quads, int normalize,
-                                                            void* record) {
+                                                               const int* __restrict__ active,
+                                                               const unsigned long long* __restrict__ n_active,
+                                                               S* __restrict__ verts, int64_t* __restrict__ quads,
+                                                               int normalize, void* record, int64_t vcap,
+                                                               int64_t fcap, Stats* stats) {
+  if (!emit_fits<DMC>(g, seg, vcap, fcap, stats)) return;
   const EdgeRecord<S> rec = grid_record<S, DMC>(record, g, seg);
-  dmc_emit_tile<S>(f, g, seg, codes, active[blockIdx.x], verts, quads, normalize, 0, rec);
+  const int64_t n = (int64_t)*n_active;
+  __shared__ int64_t next;
+#pragma unroll 1
+  for (;;) {
+    if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
+    __syncthreads();
+    const int64_t t = next;
+    __syncthreads();
+    if (t >= n) break;
+    dmc_emit_tile<S>(f, g, seg, codes, active[t], verts, quads, normalize, 0, rec);
+  }
 }
 
 // ------------------------------------------------------------------ backward

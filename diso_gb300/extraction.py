@@ -29,8 +29,8 @@ from torch.autograd import Function
 from . import _native as N
 
 # Optional phase timer: when set to a callable, it is called as timer(name, "start"
-# | "end") around each native phase (count, emit, split, backward) on the
-# current stream; bench.py uses it to record CUDA events inside its timed region.
+# | "end") around each native phase (forward, split, backward) on the current
+# stream; bench.py uses it to record CUDA events inside its timed region.
 phase_timer = None
 
 
@@ -57,31 +57,23 @@ def _check_inputs(grid, deform, dtype):
 
 class _ExtractFunction(Function):
     """Autograd node of one extraction; the counterpart of DMCFunction /
-    DDMCFunction (diso/__init__.py:18-46, 72-100)."""
+    DDMCFunction (diso/__init__.py:18-46, 72-100).  The forward's kernels have run
+    when it is applied (extract below); it returns the outputs and keeps what the
+    backward needs."""
 
     @staticmethod
-    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads):
-        g = grid.detach().contiguous()
-        d = deform.detach().contiguous() if deform is not None else None
+    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads, out):
+        verts_buf, faces_buf, record = out
         nv, nf = int(counts.n_verts), int(counts.n_faces)
-        width = 3 if ex.method == N.MC else 4
-        verts = torch.empty((nv, 3), dtype=g.dtype, device=g.device)
-        faces = torch.empty((nf, width), dtype=torch.int64, device=g.device)
-        # the edge record only when a gradient can be asked for (the gradient buffers,
-        # zeroed beside the count, come with it)
-        wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
-        record = (torch.empty(max(1, ex.record_slots(counts)), dtype=torch.int64, device=g.device)
-                  if wants_grad else None)
-        ctx.gs, ctx.gd = grads if (wants_grad and grads is not None) else (None, None)
-        _mark("emit", "start")
-        ex.emit(g, d, iso, pad, seg, normalize, verts, faces, record)
-        _mark("emit", "end")
+        verts, faces = verts_buf[:nv], faces_buf[:nf]
         if ex.method == N.DMC and not return_quads:
-            tris = torch.empty((2 * nf, 3), dtype=torch.int64, device=g.device)
+            tris = torch.empty((2 * nf, 3), dtype=torch.int64, device=verts.device)
             _mark("split", "start")
             n = ex.split(verts, faces, tris)
             _mark("split", "end")
             faces = tris[:n]
+        wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        ctx.gs, ctx.gd = grads if (wants_grad and grads is not None) else (None, None)
         ctx.ex = ex
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
         ctx.has_deform = deform is not None
@@ -109,7 +101,11 @@ class _ExtractFunction(Function):
             ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
                             zeroed=zeroed)
             _mark("backward", "end")
-        return gs, gd, None, None, None, None, None, None, None, None, None
+        return gs, gd, None, None, None, None, None, None, None, None, None, None
+
+
+def _capacity(n):
+    return n + n // 8 + 1024
 
 
 def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
@@ -118,29 +114,61 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
 
     exact_grad (DMC only) replaces the reference's backward in cells with several
     patches, where every patch receives the first patch's gradient
-    (src/cudualmc.cu:990), by the true derivative."""
+    (src/cudualmc.cu:990), by the true derivative.
+
+    When the extractor has seen a grid of this shape before, the forward is one
+    native call (count, scan and emit with no host round trip in between) into
+    outputs sized from the last result with some headroom; the returned tensors
+    are views of them.  Otherwise, or when they do not fit, the emit follows the
+    count into outputs of the exact sizes."""
     _check_inputs(grid, deform, ex.dtype)
     iso, pad = N.iso_values(isovalue, ex.dtype)
+    width = 3 if ex.method == N.MC else 4
     with torch.cuda.device(grid.device):
+        dev = grid.device
         g = grid.detach().contiguous()
-        seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=g.device)
+        d = deform.detach().contiguous() if deform is not None else None
+        seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=dev)
+        wants_grad = torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad))
         # When a gradient can be asked for, its buffers are allocated now and zeroed on
         # a second stream while the count runs (the count reads HBM far below its
         # bandwidth); the backward then writes only the point tiles near the surface.
         grads = None
-        if torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad)):
-            grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=g.device)
-                     if deform is not None else None)
+        if wants_grad:
+            grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=dev)
+                     if d is not None else None)
             ex.zero_grads(*grads)
-        _mark("count", "start")
-        counts = ex.count(g, iso, pad, seg)
-        _mark("count", "end")
+        hints = ex.__dict__.setdefault("size_hints", {})
+        hint = hints.get(tuple(g.shape))
+        counts, out = None, None
+        _mark("forward", "start")
+        if hint is not None:
+            vcap, fcap = hint
+            verts = torch.empty((vcap, 3), dtype=ex.dtype, device=dev)
+            faces = torch.empty((fcap, width), dtype=torch.int64, device=dev)
+            record = (torch.empty(max(1, ex.record_slots(n_verts=vcap, n_faces=fcap)), dtype=torch.int64, device=dev)
+                      if wants_grad else None)
+            counts = ex.forward(g, d, iso, pad, seg, normalize, verts, faces, record)
+            if counts.emitted:
+                out = (verts, faces, record)
+        else:
+            counts = ex.count(g, iso, pad, seg)
+        hints[tuple(g.shape)] = (_capacity(int(counts.n_verts)), _capacity(int(counts.n_faces)))
         if counts.empty:
-            width = 3 if ex.method == N.MC else 4
-            return (torch.zeros((0, 3), dtype=ex.dtype, device=grid.device),
-                    torch.zeros((0, width), dtype=torch.int32, device=grid.device))
+            _mark("forward", "end")
+            return (torch.zeros((0, 3), dtype=ex.dtype, device=dev),
+                    torch.zeros((0, width), dtype=torch.int32, device=dev))
+        if out is None:
+            nv, nf = int(counts.n_verts), int(counts.n_faces)
+            verts = torch.empty((nv, 3), dtype=ex.dtype, device=dev)
+            faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
+            record = (torch.empty(max(1, ex.record_slots(counts)), dtype=torch.int64, device=dev)
+                      if wants_grad else None)
+            ex.emit(g, d, iso, pad, seg, normalize, verts, faces, record)
+            out = (verts, faces, record)
+        _mark("forward", "end")
         return _ExtractFunction.apply(grid, deform, ex, seg, counts, iso, pad, bool(normalize), bool(return_quads),
-                                      bool(exact_grad), grads)
+                                      bool(exact_grad), grads, out)
 
 
 class DiffMC(nn.Module):

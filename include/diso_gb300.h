@@ -61,7 +61,7 @@ typedef struct {
   double sdf_max;
   int32_t empty;          /* 1 when the reference's guard returns an empty mesh:
                              min >= isovalue or max <= isovalue (diso/__init__.py:49, 103) */
-  int32_t pad_;
+  int32_t emitted;        /* diso_forward: 1 when the outputs fitted their capacities and were written */
   int64_t n_active_tiles; /* 4x8x32-cell tiles holding a crossing, a face or a patch */
 } diso_counts;
 
@@ -94,6 +94,18 @@ int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int 
 int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
                       double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
                       int64_t* faces, uint64_t* edge_record, void* stream);
+
+/* The whole forward in one call: count, scan and emit into verts [vcap][3] and faces
+ * [fcap][3|4] (and edge_record, laid out for the actual counts; NULL without a
+ * backward), synchronising the stream once at the end, so that the emit follows the
+ * count on the GPU without a host round trip.  out->emitted = 1 when the outputs fitted
+ * (n_verts <= vcap and n_faces <= fcap) and were written; otherwise nothing was
+ * emitted and the caller runs diso_forward_emit with buffers of the reported sizes
+ * (the count is done).  Capacities come from the caller's expectation, e.g. the last
+ * call on grids of this size. */
+int diso_forward(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double isovalue,
+                 double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                 uint64_t* edge_record, void* stream, diso_counts* out);
 
 /* uint64 slots of the edge record of a forward with these counts (diso_counts.n_verts,
  * .n_faces); 0 on bad input.  No counterpart in the reference, whose backward re-runs

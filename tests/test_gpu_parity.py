@@ -215,6 +215,34 @@ def test_second_backward_and_forward_without_backward(cuda_device):
         assert g1.abs().sum() > 0 and d1.abs().sum() > 0
 
 
+@pytest.mark.parametrize("method", ["mc", "dmc"])
+def test_single_call_forward_and_capacity_fallback(cuda_device, method):
+    # a module that has seen a grid of this shape runs the forward as one native call
+    # into outputs sized from that grid; a larger surface than that falls back to an
+    # emit of the exact sizes; results equal those of a fresh module either way
+    from diso_gb300 import DiffDMC, DiffMC
+
+    mk = (lambda: DiffMC(torch.float32)) if method == "mc" else (lambda: DiffDMC(torch.float32))
+    rng = np.random.default_rng(4)
+    shape = (40, 33, 47)
+    small = torch.tensor(_field("spheres", shape, rng).astype(np.float32), device=cuda_device)
+    big = torch.tensor(rng.uniform(-1, 1, shape).astype(np.float32), device=cuda_device)
+    w = torch.tensor(rng.uniform(-1, 1, (200000, 3)).astype(np.float32), device=cuda_device)
+
+    def run(mod, grid):
+        s = grid.clone().requires_grad_(True)
+        v, f = mod(s)
+        (v * w[: v.shape[0]]).sum().backward()
+        return v.detach().clone(), f.clone(), s.grad.clone()
+
+    warm = mk()
+    for grid in (small, big, big, small):  # fallback, then fits, then fits with room
+        got = run(warm, grid)
+        ref = run(mk(), grid)
+        for a, b in zip(got, ref):
+            assert a.shape == b.shape and torch.equal(a, b)
+
+
 def test_empty_guard_and_errors(cuda_device):
     from diso_gb300 import DiffDMC, DiffMC
 
