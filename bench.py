@@ -313,17 +313,16 @@ def kernel_bytes(vol, nseg, nv, nq, s):
 
 
 def read_profile_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summaries (None when
-    no summary covers it)."""
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.txt"))):
+    """Per-launch DRAM bytes of `kernel` at the benchmark workload from the committed
+    ncu summary (lines "<kernel>: <bytes>"), None when it has no line."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "dram_traffic_*.txt"))):
         try:
             txt = open(path).read()
         except OSError:
             continue
-        m = re.search(r"kernel:\s*(\S+)", txt)
-        t = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-        if m and t and m.group(1) == kernel:
-            return float(t.group(1))
+        m = re.search(r"^%s:\s*([0-9.eE+]+)\s*$" % re.escape(kernel), txt, flags=re.M)
+        if m:
+            return float(m.group(1))
     return None
 
 
