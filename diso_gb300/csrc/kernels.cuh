@@ -31,6 +31,45 @@ constexpr int MASK_TOP = 34;  // highest valid mask bit: points Z0-1 .. Z0+33
 
 __device__ const uint8_t g_edge_of[24] = DISO_EDGE_LOOKUP;
 
+// ------------------------------------------------------------------ small tables
+
+__device__ const float g_recip_f[16] = {0.f,      1.f / 1,  1.f / 2,  1.f / 3,  1.f / 4,  1.f / 5,
+                                        1.f / 6,  1.f / 7,  1.f / 8,  1.f / 9,  1.f / 10, 1.f / 11,
+                                        1.f / 12, 1.f / 13, 1.f / 14, 1.f / 15};
+__device__ const double g_recip_d[16] = {0.,      1. / 1,  1. / 2,  1. / 3,  1. / 4,  1. / 5,  1. / 6,  1. / 7,
+                                         1. / 8,  1. / 9,  1. / 10, 1. / 11, 1. / 12, 1. / 13, 1. / 14, 1. / 15};
+// 1 / n, correctly rounded (what S(1) / S(n) gives)
+template <class S>
+__device__ __forceinline__ S recip(int n);
+template <>
+__device__ __forceinline__ float recip<float>(int n) { return __ldg(g_recip_f + n); }
+template <>
+__device__ __forceinline__ double recip<double>(int n) { return __ldg(g_recip_d + n); }
+
+// Per DMC case code, the crossing edges of each patch: bits 12p + e = edge e (the
+// reference's edge order) crosses and belongs to patch p.  Derived from the case table
+// at compile time.
+namespace detail {
+constexpr uint64_t kDmcCaseTable[256] = DISO_DMC_CASES;
+struct PatchMasks {
+  uint64_t m[256];
+};
+constexpr PatchMasks make_patch_masks() {
+  PatchMasks t{};
+  for (int code = 0; code < 256; ++code) {
+    uint64_t out = 0;
+    for (int e = 0; e < 12; ++e) {
+      const int ge = kEdgeTable[e], s = ge & 7, end = s | (1 << (ge >> 3));
+      if (((code >> s) ^ (code >> end)) & 1)
+        out |= 1ull << (12 * (int)((kDmcCaseTable[code] >> (2 * e)) & 3) + e);
+    }
+    t.m[code] = out;
+  }
+  return t;
+}
+}  // namespace detail
+__device__ const detail::PatchMasks g_dmc_pmask = detail::make_patch_masks();
+
 // ------------------------------------------------------------------ geometry helpers
 
 // lerp vertex of the edge from padded point (X,Y,Z) along axis a, in padded
@@ -1293,51 +1332,43 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     return wbase[x][y] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
   };
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
-  // (create_dmc_verts_kernel, src/cudualmc.cu:907-955)
+  // (create_dmc_verts_kernel, src/cudualmc.cu:907-955); a patch's edges come from the
+  // per-code patch masks
   for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
     int ix, iy, j, a;
     item_decode(citems[i], ix, iy, j, a);
     const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
     const int code = rc[x][y][j + 1];
-    const uint64_t wc = dmc_case(code);
-    const int np = dmc_npatch(wc);
-    const uint32_t cb = cross_bits(code);
-    S acc[4][3];
-    int cnt[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int p = 0; p < 4; ++p) acc[p][0] = acc[p][1] = acc[p][2] = S(0);
-#pragma unroll 1
-    for (int e = 0; e < 12; ++e) {
-      const int ge = edge_desc(e), s = ge & 7, ax = ge >> 3;
-      if (((cb >> ge) & 1u) == 0) continue;
-      const int p = dmc_patch_of(wc, e);
-      S v[3];
-      if (cached) {
-        const int k = wslot(ix + (s & 1), iy + ((s >> 1) & 1), j + ((s >> 2) & 1), ax);
-        v[0] = epos[k][0];
-        v[1] = epos[k][1];
-        v[2] = epos[k][2];
-      } else {
-        edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (q == p) {
-          acc[q][0] += v[0];
-          acc[q][1] += v[1];
-          acc[q][2] += v[2];
-          cnt[q] += 1;
-        }
-    }
+    const int np = dmc_npatch(dmc_case(code));
+    const uint64_t pm = __ldg(&g_dmc_pmask.m[code]);
     const int64_t p0 = (int64_t)pb[x][y] + pp[x][y][j + 1];
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (q < np) {
-        const S inv = S(1) / S(cnt[q]);
-        const S v[3] = {acc[q][0] * inv, acc[q][1] * inv, acc[q][2] * inv};
-        store_vertex<S>(verts, p0 + q, v, g, normalize);
-        if (rec.aux) rec.aux[p0 + q] = (uint8_t)(cnt[q] | (q << 4));
+#pragma unroll 1
+    for (int q = 0; q < np; ++q) {
+      uint32_t m = (uint32_t)(pm >> (12 * q)) & 0xfffu;
+      const int cnt = __popc(m);
+      S acc[3] = {S(0), S(0), S(0)};
+      while (m) {
+        const int e = __ffs(m) - 1;
+        m &= m - 1;
+        const int ge = edge_desc(e), s = ge & 7, ax = ge >> 3;
+        S v[3];
+        if (cached) {
+          const int k = wslot(ix + (s & 1), iy + ((s >> 1) & 1), j + ((s >> 2) & 1), ax);
+          v[0] = epos[k][0];
+          v[1] = epos[k][1];
+          v[2] = epos[k][2];
+        } else {
+          edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
+        }
+        acc[0] += v[0];
+        acc[1] += v[1];
+        acc[2] += v[2];
       }
+      const S inv = recip<S>(cnt);  // S(1) / S(cnt)
+      const S v[3] = {acc[0] * inv, acc[1] * inv, acc[2] * inv};
+      store_vertex<S>(verts, p0 + q, v, g, normalize);
+      if (rec.aux) rec.aux[p0 + q] = (uint8_t)(cnt | (q << 4));
+    }
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
@@ -1454,19 +1485,6 @@ __device__ __forceinline__ void ptile_coords(int64_t tile, const Geom& g, int& x
   x0 = (int)(r / g.ptiles_y()) * TX;
   z0 = tz * TZ;
 }
-
-__device__ const float g_recip_f[16] = {0.f,      1.f / 1,  1.f / 2,  1.f / 3,  1.f / 4,  1.f / 5,
-                                        1.f / 6,  1.f / 7,  1.f / 8,  1.f / 9,  1.f / 10, 1.f / 11,
-                                        1.f / 12, 1.f / 13, 1.f / 14, 1.f / 15};
-__device__ const double g_recip_d[16] = {0.,      1. / 1,  1. / 2,  1. / 3,  1. / 4,  1. / 5,  1. / 6,  1. / 7,
-                                         1. / 8,  1. / 9,  1. / 10, 1. / 11, 1. / 12, 1. / 13, 1. / 14, 1. / 15};
-// 1 / n, correctly rounded (what S(1) / S(n) gives)
-template <class S>
-__device__ __forceinline__ S recip(int n);
-template <>
-__device__ __forceinline__ float recip<float>(int n) { return __ldg(g_recip_f + n); }
-template <>
-__device__ __forceinline__ double recip<double>(int n) { return __ldg(g_recip_d + n); }
 
 // The backward runs in two passes.
 //
