@@ -61,7 +61,7 @@ struct diso_extractor {
   int64_t scan_cap = 0;          // look-back tiles
   int* active = nullptr;         // tiles with crossings (forward)
   int64_t active_cap = 0;
-  uint8_t* codes = nullptr;      // cell codes of the active segments (count -> emit)
+  CellRec* codes = nullptr;      // DMC cell records of the active segments (count -> emit)
   int64_t codes_cap = 0;
   uint64_t* split = nullptr;     // split counts (n_quads + 1)
   int64_t split_cap = 0;
@@ -369,8 +369,9 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   g.init(nx, ny, nz);
   int rc;
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
-  if ((rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
+  if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
   if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
   CUtensorMap wide, narrow;
@@ -383,10 +384,10 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     const size_t smem = count_tma_smem<S>();
     if (ex->method == DISO_MC)
-      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->codes,
+      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
                                                            ex->stats, ex->active);
     else
-      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), ex->codes,
+      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
                                                             ex->stats, ex->active);
   } else {
     const int64_t units = count_units(g);
@@ -394,11 +395,9 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
         std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     if (ex->method == DISO_MC)
-      count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->codes, ex->stats,
-                                                    ex->active);
+      count_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
     else
-      count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), ex->codes, ex->stats,
-                                                     ex->active);
+      count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
   }
   delete kt;  // the count's end event
   CUDA_TRY(cudaGetLastError());
@@ -668,7 +667,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     codes_total += g.ncodes();
   }
   int rc;
-  if ((rc = grow(ex->codes, ex->codes_cap, codes_total)) != DISO_OK) return rc;
+  if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, codes_total)) != DISO_OK) return rc;
   for (int i = 0; i < n; ++i) {
     const diso_grid& q = grids[i];
     BatchGrid<S> b;
@@ -677,7 +676,7 @@ int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* r
     b.seg = record + seg_off;
     b.seg_end = record + seg_off + b.g.nseg;
     b.tile_flag = flags + tile_off;
-    b.codes = ex->codes + code_off;
+    b.codes = ex->method == DISO_DMC ? ex->codes + code_off : nullptr;
     b.cblk0 = cblk;
     b.ptile0 = ptile;
     b.gsdf = (S*)q.grad_sdf;

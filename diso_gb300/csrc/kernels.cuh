@@ -29,6 +29,13 @@ enum Method { MC = 0, DMC = 1 };
 
 constexpr int MASK_TOP = 34;  // highest valid mask bit: points Z0-1 .. Z0+33
 
+// Cell record kept by the count for the DMC emit (2 bytes per cell, in an array of
+// the grid's cells with rows padded to whole chunks): bits 0-7 the Morton code after
+// the ambiguity test, bit 8 the raw bit of corner 0 (value >= iso), bits 9-15 the
+// patches of the segment's earlier cells.  A segment's records are valid when its
+// count is not zero (0 for its trivial cells).
+typedef uint16_t CellRec;
+
 __device__ const uint8_t g_edge_of[24] = DISO_EDGE_LOOKUP;
 
 // ------------------------------------------------------------------ small tables
@@ -361,7 +368,7 @@ struct CountShared {
   uint32_t bal[CROWS];         // ballots of the chunk just read (each row read and used by one warp)
   uint32_t act[CP], actc[CP], actf[CP];
   uint32_t mixed[3];                       // per chunk (rotating): OR of count_combine's bits
-  __align__(16) uint8_t code[CP][32][TZ];  // Morton codes of each lane's segment (staging)
+  __align__(16) CellRec code[CP][32][TZ];  // cell records of each lane's segment (staging)
   int list[COUNT_LIST];
   int nlist, base;
 };
@@ -427,7 +434,8 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
 
 // Counts of the unit's chunk tz from the masks in sh.m (complete: the caller
 // synchronised), the activity bytes of the chunk's tiles; active tiles are appended
-// (as tile | tag) to sh.list.  Ends with a block barrier.
+// (as tile | tag) to sh.list; the cell records of busy segments (DMC, when `codes` is
+// given).  Ends with a block barrier.
 //
 // Two bytes per tile: tile_flag[tile] = 1 when the tile's cells have crossings or
 // faces (the emit's tiles); tile_flag[ntiles + tile] bit (dx | dy << 1 | dz << 2) =
@@ -438,13 +446,13 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
 template <class S, int METHOD>
 __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                             uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
-                                            uint8_t* __restrict__ codes, int X0, int Y0, int tz, int tag) {
+                                            CellRec* __restrict__ codes, int X0, int Y0, int tz, int tag) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z0 = tz * TZ;
   const int X = X0 + warp, Y = Y0 + lane;
   uint32_t nv = 0, nf = 0, own = 0, nt = 0;
   uint4* stage = reinterpret_cast<uint4*>(sh.code[warp][lane]);
-  if (codes) stage[0] = stage[1] = make_uint4(0u, 0u, 0u, 0u);
+  if (codes) stage[0] = stage[1] = stage[2] = stage[3] = make_uint4(0u, 0u, 0u, 0u);
   if (X < g.c[0] && Y < g.c[1]) {
     const int x = warp, y = lane;
     const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
@@ -458,19 +466,21 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
       const int j = __ffs(left) - 1;
       left &= left - 1;
       const int code = code_at(cr, j);
-      if (codes) sh.code[warp][lane][j] = (uint8_t)code;
-      if (METHOD == MC)
+      if (METHOD == MC) {
         nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-      else
-        nf += dmc_npatch(dmc_case(dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g)));
+      } else {
+        const int rcode = dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g);
+        if (codes) sh.code[warp][lane][j] = (CellRec)(rcode | ((code & 1) << 8) | (nf << 9));
+        nf += dmc_npatch(dmc_case(rcode));
+      }
     }
     seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
-    // the Morton codes of a segment with non-trivial cells (0 for the trivial ones),
-    // read by the emit for the segments whose count is not zero
     if (codes && nt) {
       uint4* out = reinterpret_cast<uint4*>(codes + g.code(X, Y, Z0));
       out[0] = stage[0];
       out[1] = stage[1];
+      out[2] = stage[2];
+      out[3] = stage[3];
     }
   }
   // a cell can emit faces / patches without owning a crossing edge (its
@@ -557,7 +567,7 @@ __device__ __forceinline__ void count_chunk_empty(const Geom& g, uint64_t* __res
 template <class S, int METHOD>
 __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
-                                           uint8_t* __restrict__ codes, Stats* stats, int64_t unit, int tag,
+                                           CellRec* __restrict__ codes, Stats* stats, int64_t unit, int tag,
                                            int64_t& ck) {
   // a row of nzc chunks is cut into nbz near-equal runs of at most KZ chunks
   const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
@@ -612,7 +622,7 @@ __device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                             uint8_t* __restrict__ tile_flag,
-                                                            uint8_t* __restrict__ codes, Stats* stats,
+                                                            CellRec* __restrict__ codes, Stats* stats,
                                                             int* __restrict__ active) {
   __shared__ CountShared<S, METHOD> sh;
   if (threadIdx.x == 0) {
@@ -759,7 +769,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
                                                                 const __grid_constant__ CUtensorMap narrow,
                                                                 Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                                 uint8_t* __restrict__ tile_flag,
-                                                                uint8_t* __restrict__ codes, Stats* stats,
+                                                                CellRec* __restrict__ codes, Stats* stats,
                                                                 int* __restrict__ active) {
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   __shared__ CountShared<S, METHOD> sh;
@@ -858,7 +868,7 @@ struct BatchGrid {
   uint64_t* seg;        // this grid's first segment in the concatenated, globally scanned array
   uint64_t* seg_end;    // the next grid's first segment (or the total slot)
   uint8_t* tile_flag;   // this grid's tile bytes
-  uint8_t* codes;       // this grid's cell codes (count -> emit)
+  CellRec* codes;       // this grid's cell records (count -> emit), null for MC
   int64_t cblk0;        // first count unit of the grid in the flattened queue
   int64_t ptile0;       // first point tile (backward)
   S* gsdf;              // backward outputs
@@ -1131,22 +1141,21 @@ __host__ __device__ constexpr int epos_cap() {
 }
 
 // One active tile: its dual vertices and quads; patch ids written into quads are
-// reduced by vsub (as in mc_emit_tile).  The cells' Morton codes come from the codes
-// array the count filled (valid for the segments whose count is not zero; the
-// others hold trivial cells only), so the SDF is read only for the edge vertices.
+// reduced by vsub (as in mc_emit_tile).  The cells' codes (after the ambiguity test)
+// and in-segment patch offsets come from the cell records of the count (valid for the
+// segments whose count is not zero; the others hold trivial cells only), so the SDF is
+// read only for the edge vertices.
 template <class S>
 __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
-                                              const uint8_t* __restrict__ codes, int tile, S* __restrict__ verts,
+                                              const CellRec* __restrict__ codes, int tile, S* __restrict__ verts,
                                               int64_t* __restrict__ quads, int normalize, int64_t vsub,
                                               const EdgeRecord<S>& rec) {
-  constexpr int KX = TX + 2, KY = TY + 2;  // code window: cells [X0-1, X0+TX] x [Y0-1, Y0+TY], z index j+1 for Z0+j,
+  constexpr int KX = TX + 2, KY = TY + 2;  // window: cells [X0-1, X0+TX] x [Y0-1, Y0+TY], z index j+1 for Z0+j,
   constexpr int KZ2 = TZ + 2;              // j in [-1, TZ]
   constexpr int CX = TX + 1, CY = TY + 1;  // code rows: cells [X0-1, X0+TX) x [Y0-1, Y0+TY) (own + the -1 halo)
   constexpr int CAP = epos_cap<S>();
-  __shared__ uint8_t cw[KX][KY][KZ2];     // raw Morton codes of the window
+  __shared__ CellRec cw[KX][KY][KZ2];     // cell records of the window (0 where trivial)
   __shared__ uint8_t sact[KX][KY];        // bit 0/1/2: the row's segment tz-1 / tz / tz+1 has a non-zero count
-  __shared__ uint8_t rc[CX][CY][TZ + 1];  // resolved codes; z index j+1 for cell Z0+j, 0 for Z0-1
-  __shared__ int16_t pp[CX][CY][TZ + 1];  // first patch of the cell inside its segment
   __shared__ uint32_t pb[CX][CY];
   __shared__ uint32_t qb[TX][TY];
   __shared__ RowBits wb[TX + 1][TY + 1];  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
@@ -1181,65 +1190,36 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     }
   }
   __syncthreads();
-  // codes of the window, one warp per row; the edge rows' crossing bits from them
+  // records of the window, one warp per row; the edge rows' crossing bits from them
   for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
     const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
     const uint32_t act = sact[wx][wy];
     const int c = (act & 2) ? codes[g.code(X, Y, Z0 + lane)] : 0;
-    cw[wx][wy][lane + 1] = (uint8_t)c;
+    cw[wx][wy][lane + 1] = (CellRec)c;
     int e = 0;
     if (lane == 0 && (act & 1)) e = codes[g.code(X, Y, Z0 - 1)];
     if (lane == 31 && (act & 4)) e = codes[g.code(X, Y, Z0 + TZ)];
-    if (lane == 0) cw[wx][wy][0] = (uint8_t)e;
-    if (lane == 31) cw[wx][wy][TZ + 1] = (uint8_t)e;
+    if (lane == 0) cw[wx][wy][0] = (CellRec)e;
+    if (lane == 31) cw[wx][wy][TZ + 1] = (CellRec)e;
     if (wx >= 1 && wy >= 1) {
-      const int cf = cross_flags(c);
+      const int code = c & 0xff, cf = cross_flags(code);
       RowBits w;
       w.xc = __ballot_sync(0xffffffffu, cf & 1);
       w.yc = __ballot_sync(0xffffffffu, cf & 2);
       w.zc = __ballot_sync(0xffffffffu, cf & 4);
-      w.nt = __ballot_sync(0xffffffffu, c != 0 && c != 255);
+      w.nt = __ballot_sync(0xffffffffu, code != 0 && code != 255);
       if (lane == 0) wb[wx - 1][wy - 1] = w;
-      if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e);
+      if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e & 0xff);
     }
   }
   __syncthreads();
-  // resolved codes and in-segment patch prefixes of the tile's cells and their -1 halo
-  // (the ambiguity test, src/cudualmc.cu:815-839, with the neighbour's code from the
-  // window, or from the SDF outside it)
-  auto resolve = [&](int wx, int wy, int jj, int code) -> int {
-    const int dir = dmc_dir(dmc_case(code));
-    if (dir == 7) return code;
-    const int comp = dir >> 1, d = (dir & 1) ? 1 : -1;
-    const int X = X0 - 1 + wx, Y = Y0 - 1 + wy, Z = Z0 - 1 + jj;
-    const int nx = wx + (comp == 0 ? d : 0), ny = wy + (comp == 1 ? d : 0), nj = jj + (comp == 2 ? d : 0);
-    const int nc = comp == 0 ? X + d : (comp == 1 ? Y + d : Z + d);
-    if (nc < 0 || nc >= g.c[comp]) return code;
-    const int ncode = ((unsigned)nx < (unsigned)KX && (unsigned)ny < (unsigned)KY && (unsigned)nj < (unsigned)KZ2)
-                          ? cw[nx][ny][nj]
-                          : cell_code_far<S>(f, X + (comp == 0 ? d : 0), Y + (comp == 1 ? d : 0), Z + (comp == 2 ? d : 0));
-    return dmc_dir(dmc_case(ncode)) != 7 ? (code ^ 0xff) : code;
+  // code after the ambiguity test, and first patch relative to its row's base pb, of
+  // window cell (x, y) at z index jj (jj = 0: cell Z0-1, the last of the previous segment)
+  auto rcode = [&](int x, int y, int jj) -> int { return cw[x][y][jj] & 0xff; };
+  auto ppatch = [&](int x, int y, int jj) -> int {
+    const int r = cw[x][y][jj];
+    return jj ? (r >> 9) : -(int)dmc_npatch(dmc_case(r & 0xff));
   };
-  for (int r = warp; r < CX * CY; r += TY) {
-    const int x = r / CY, y = r % CY;
-    const int craw = cw[x][y][lane + 1];
-    const bool nontriv = craw != 0 && craw != 255;
-    const uint32_t nt = __ballot_sync(0xffffffffu, nontriv);
-    const int c0raw = cw[x][y][0];
-    // a row without non-trivial cells (Z0 - 1 included) is never read
-    if (nt == 0 && (c0raw == 0 || c0raw == 255)) continue;
-    const int code = nontriv ? resolve(x, y, lane + 1, craw) : 0;
-    const uint32_t np = dmc_npatch(dmc_case(code));
-    const uint32_t inc = nt ? warp_incl(np) : 0u;
-    rc[x][y][lane + 1] = (uint8_t)code;
-    pp[x][y][lane + 1] = (int16_t)(inc - np);
-    if (lane == 0) {
-      int c0 = c0raw;
-      if (c0 != 0 && c0 != 255) c0 = resolve(x, y, 0, c0);
-      rc[x][y][0] = (uint8_t)c0;
-      pp[x][y][0] = (int16_t)(-(int)dmc_npatch(dmc_case(c0)));  // last cell of the previous segment
-    }
-  }
   // edge rows: crossing edges (window items) and, for the own rows, the non-trivial
   // cells (dual vertex items); row bases by a block scan, then one warp per row
   // writes the row's items
@@ -1301,14 +1281,14 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int x = ix + 1, y = iy + 1;  // code row / mask row of the own row
     const RowBits& r = wb[ix][iy];
     const int64_t qid = (int64_t)qb[ix][iy] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
-    const int type = a + 3 * (cw[x][y][j + 1] & 1);  // corner 0 of the owner cell (Morton bit 0)
+    const int type = a + 3 * ((cw[x][y][j + 1] >> 8) & 1);  // raw corner 0 of the owner cell
     int4 rid = make_int4(0, 0, 0, 0);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int q = g_dmc_quad[4 * type + k];
       const int ox = (q & 3) - 1, oy = ((q >> 2) & 3) - 1, oz = ((q >> 4) & 3) - 1;
       const int nx = x + ox, ny = y + oy, nz = j + 1 + oz;
-      const int64_t id = (int64_t)pb[nx][ny] + pp[nx][ny][nz] + dmc_patch_of(dmc_case(rc[nx][ny][nz]), q >> 8) - vsub;
+      const int64_t id = (int64_t)pb[nx][ny] + ppatch(nx, ny, nz) + dmc_patch_of(dmc_case(rcode(nx, ny, nz)), q >> 8) - vsub;
       quads[4 * qid + k] = id;
       // the record orders the cells by their steps back (db, dc) along axes a+1, a+2
       const int db = -(a == 0 ? oy : (a == 1 ? oz : ox)), dc = -(a == 0 ? oz : (a == 1 ? ox : oy));
@@ -1338,10 +1318,10 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     int ix, iy, j, a;
     item_decode(citems[i], ix, iy, j, a);
     const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
-    const int code = rc[x][y][j + 1];
+    const int code = rcode(x, y, j + 1);
     const int np = dmc_npatch(dmc_case(code));
     const uint64_t pm = __ldg(&g_dmc_pmask.m[code]);
-    const int64_t p0 = (int64_t)pb[x][y] + pp[x][y][j + 1];
+    const int64_t p0 = (int64_t)pb[x][y] + ppatch(x, y, j + 1);
 #pragma unroll 1
     for (int q = 0; q < np; ++q) {
       uint32_t m = (uint32_t)(pm >> (12 * q)) & 0xfffu;
@@ -1375,7 +1355,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
 
 template <class S>
 __global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
-                                                               const uint8_t* __restrict__ codes,
+                                                               const CellRec* __restrict__ codes,
                                                                const int* __restrict__ active,
                                                                const unsigned long long* __restrict__ n_active,
                                                                S* __restrict__ verts, int64_t* __restrict__ quads,
