@@ -74,6 +74,16 @@ struct diso_extractor {
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_zero = nullptr;  // end of the last diso_zero_grads on the side stream
+  // gradient buffers of diso_zero_grads that the next count on `stream` zeroes
+  struct PendingZero {
+    void* p[2];
+    int64_t bytes[2];
+    cudaStream_t stream;
+    bool set;
+  } zpend = {};
+  ZeroJob zemit = {};            // the emit's part of the zeros of the last count
+  cudaStream_t zemit_stream = nullptr;
+  bool zemit_set = false;
   cudaEvent_t ev_counts = nullptr;  // the count's results are on the host
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
@@ -362,6 +372,14 @@ Field<S> make_field(const void* sdf, const void* deform, int nx, int ny, int nz,
   return f;
 }
 
+int flush_zero(diso_extractor* ex, cudaStream_t z);
+int take_zero_job(diso_extractor* ex, const Geom& g, int64_t units, unsigned grid, cudaStream_t s, ZeroJob* zj);
+ZeroJob take_emit_zero(diso_extractor* ex, unsigned grid, cudaStream_t s);
+int flush_emit_zero(diso_extractor* ex, cudaStream_t s);
+
+// share of a forward's gradient zeros that the count writes (the emit writes the rest)
+constexpr double ZERO_COUNT_SHARE = 0.35;
+
 template <class S>
 int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double iso, double padval,
                  uint64_t* seg, cudaStream_t s) {
@@ -376,20 +394,25 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
   CUtensorMap wide, narrow;
   const bool tma = count_tensor_maps<S>(sdf, nx, ny, nz, &wide, &narrow);
-  KernelTimer* kt = new (std::nothrow) KernelTimer(ex, K_COUNT, s);
   if (tma) {
     const int64_t units = count_tma_units(g);
     const int64_t want =
         std::max<int64_t>(ex->tma_ctas, (units * TMA_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     const size_t smem = count_tma_smem<S>();
+    ZeroJob zj;
+    if ((rc = take_zero_job(ex, g, units, grid, s, &zj)) != DISO_OK) return rc;
+    KernelTimer kt(ex, K_COUNT, s);
     if (ex->method == DISO_MC)
       count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
-                                                           ex->stats, ex->active);
+                                                           ex->stats, ex->active, zj);
     else
       count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
-                                                            ex->stats, ex->active);
+                                                            ex->stats, ex->active, zj);
   } else {
+    ex->zemit_set = false;
+    if ((rc = flush_zero(ex, ex->side)) != DISO_OK) return rc;
+    KernelTimer kt(ex, K_COUNT, s);
     const int64_t units = count_units(g);
     const int64_t want =
         std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
@@ -399,7 +422,6 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
     else
       count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
   }
-  delete kt;  // the count's end event
   CUDA_TRY(cudaGetLastError());
   return run_scan(ex, seg, g.nseg, s);
 }
@@ -421,7 +443,6 @@ int count_read(diso_extractor* ex, int nx, int ny, int nz, double iso, const uin
   Geom g;
   g.init(nx, ny, nz);
   (void)seg;
-  (void)s;
   CUDA_TRY(cudaEventSynchronize(ex->ev_counts));
   const Stats& h = *ex->stats_host;
   const uint64_t total = h.pad[0];
@@ -442,6 +463,8 @@ int count_read(diso_extractor* ex, int nx, int ny, int nz, double iso, const uin
   out->emitted = 0;
   out->n_active_tiles = (int64_t)h.n_active;
   ex->last_active = out->n_active_tiles;
+  // the emit's part of the zeros: no emit follows a count of an empty surface
+  if (out->empty) return flush_emit_zero(ex, s);
   return DISO_OK;
 }
 
@@ -466,13 +489,14 @@ int emit_launch(diso_extractor* ex, const void* sdf, const void* deform, int nx,
   g.init(nx, ny, nz);
   Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
   CUDA_TRY(cudaMemsetAsync(&ex->stats->emit_tile, 0, sizeof(unsigned long long), s));
+  const ZeroJob zj = take_emit_zero(ex, grid, s);
   KernelTimer kt(ex, K_EMIT, s);
   if (ex->method == DISO_MC)
     mc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->active, &ex->stats->n_active, (S*)verts, faces,
-                                                normalize, record, vcap, fcap, ex->stats);
+                                                normalize, record, vcap, fcap, ex->stats, zj);
   else
     dmc_emit_kernel<S><<<grid, NTHREADS, 0, s>>>(f, g, seg, ex->codes, ex->active, &ex->stats->n_active, (S*)verts,
-                                                 faces, normalize, record, vcap, fcap, ex->stats);
+                                                 faces, normalize, record, vcap, fcap, ex->stats, zj);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
@@ -481,7 +505,7 @@ template <class S>
 int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
                  double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, void* record,
                  cudaStream_t s) {
-  if (ex->last_active <= 0) return DISO_OK;
+  if (ex->last_active <= 0) return flush_emit_zero(ex, s);
   const unsigned grid = (unsigned)std::min<int64_t>(ex->last_active, ex->emit_ctas);
   return emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record, grid,
                         INT64_MAX, INT64_MAX, s);
@@ -572,8 +596,9 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   return zeroed ? DISO_OK : side_join(ex, s);
 }
 
-int zero_grads(diso_extractor* ex, void* gsdf, int64_t sb, void* gdef, int64_t db, cudaStream_t s,
-               cudaStream_t z) {
+// the zeros as memsets on stream z, after the work queued on s so far
+int zero_grads_side(diso_extractor* ex, void* gsdf, int64_t sb, void* gdef, int64_t db, cudaStream_t s,
+                    cudaStream_t z) {
   CUDA_TRY(cudaEventRecord(ex->ev_fork, s));
   CUDA_TRY(cudaStreamWaitEvent(z, ex->ev_fork, 0));
   {
@@ -582,6 +607,103 @@ int zero_grads(diso_extractor* ex, void* gsdf, int64_t sb, void* gdef, int64_t d
     if (db) CUDA_TRY(cudaMemsetAsync(gdef, 0, (size_t)db, z));
   }
   CUDA_TRY(cudaEventRecord(ex->ev_zero, z));
+  return DISO_OK;
+}
+
+// a pending zero goes to a side-stream memset (when no TMA count on its stream takes it)
+int flush_zero(diso_extractor* ex, cudaStream_t z) {
+  if (!ex->zpend.set) return DISO_OK;
+  const diso_extractor::PendingZero pz = ex->zpend;
+  ex->zpend.set = false;
+  return zero_grads_side(ex, pz.p[0], pz.bytes[0], pz.p[1], pz.bytes[1], pz.stream, z);
+}
+
+// Buffers whose zeros the next forward on stream s writes beside its count and emit
+// (they are 16-byte aligned); others are zeroed on stream z beside the work of s.
+// Zeros still pending from an earlier call are dropped, not written: that forward
+// never ran, and its buffers may be gone.
+int zero_grads(diso_extractor* ex, void* gsdf, int64_t sb, void* gdef, int64_t db, cudaStream_t s,
+               cudaStream_t z) {
+  ex->zpend.set = false;
+  ex->zemit_set = false;
+  const bool aligned = ((uintptr_t)gsdf & 15u) == 0 && ((uintptr_t)gdef & 15u) == 0;
+  if (!aligned) return zero_grads_side(ex, gsdf, sb, gdef, db, s, z);
+  ex->zpend.p[0] = gsdf;
+  ex->zpend.p[1] = gdef;
+  ex->zpend.bytes[0] = sb;
+  ex->zpend.bytes[1] = db;
+  ex->zpend.stream = s;
+  ex->zpend.set = true;
+  return DISO_OK;
+}
+
+// rounds of `bytes` over `grid` CTAs that take `steps` steps each at least
+void zero_rate(ZeroJob* zj, unsigned grid, int64_t steps) {
+  const int64_t bytes = zj->end - zj->begin;
+  const int64_t per_step = (bytes + (int64_t)grid * steps - 1) / ((int64_t)grid * steps);
+  zj->rbytes = std::max<int64_t>(ZBUF, (per_step + ZBUF - 1) / ZBUF * ZBUF);
+  zj->rounds = bytes > 0 ? (bytes + (int64_t)grid * zj->rbytes - 1) / ((int64_t)grid * zj->rbytes) : 0;
+}
+
+// The pending zero on stream s, split between the TMA count over `units` units in
+// `grid` CTAs (the first ZERO_COUNT_SHARE of the bytes, one round per box) and the
+// emit that follows (the rest, kept in ex->zemit).  The bytes past the last whole
+// 16-byte vector of each buffer are set here.
+int take_zero_job(diso_extractor* ex, const Geom& g, int64_t units, unsigned grid, cudaStream_t s, ZeroJob* zj) {
+  *zj = ZeroJob{};
+  ex->zemit_set = false;
+  if (!ex->zpend.set) return DISO_OK;
+  if (ex->zpend.stream != s) return flush_zero(ex, ex->side);
+  const diso_extractor::PendingZero pz = ex->zpend;
+  ex->zpend.set = false;
+  int64_t nv[2];
+  for (int i = 0; i < 2; ++i) {
+    nv[i] = pz.bytes[i] / 16;
+    const int64_t tail = pz.bytes[i] - nv[i] * 16;
+    if (tail) CUDA_TRY(cudaMemsetAsync((char*)pz.p[i] + nv[i] * 16, 0, (size_t)tail, s));
+  }
+  zj->p0 = (char*)pz.p[0];
+  zj->p1 = (char*)pz.p[1];
+  zj->n0 = nv[0] * 16;
+  const int64_t n = (nv[0] + nv[1]) * 16;
+  if (n == 0) return DISO_OK;
+  const int64_t split = (int64_t)((double)n * ZERO_COUNT_SHARE) / 16 * 16;
+  ex->zemit = *zj;
+  ex->zemit.begin = split;
+  ex->zemit.end = n;
+  ex->zemit_stream = s;
+  ex->zemit_set = split < n;
+  zj->begin = 0;
+  zj->end = split;
+  // the fewest boxes a CTA gets is its whole units times the boxes of the shortest
+  // unit (its chunks and the two 4-deep boxes)
+  const int64_t nbz = (g.nzc + KZT - 1) / KZT, kz = (g.nzc + nbz - 1) / nbz;
+  const int64_t kz_min = g.nzc - (nbz - 1) * kz;
+  zero_rate(zj, grid, std::max<int64_t>(1, (units / grid) * (kz_min + 2)));
+  return DISO_OK;
+}
+
+// the emit's part of the zeros, for an emit on stream s in `grid` CTAs (one round per
+// tile, at the tile count of the last count)
+ZeroJob take_emit_zero(diso_extractor* ex, unsigned grid, cudaStream_t s) {
+  ZeroJob zj{};
+  if (!ex->zemit_set || ex->zemit_stream != s) return zj;
+  ex->zemit_set = false;
+  zj = ex->zemit;
+  zero_rate(&zj, grid, std::max<int64_t>(1, ex->last_active / grid));
+  return zj;
+}
+
+// the emit's part of the zeros as memsets on stream s (when no emit follows the count)
+int flush_emit_zero(diso_extractor* ex, cudaStream_t s) {
+  if (!ex->zemit_set) return DISO_OK;
+  ex->zemit_set = false;
+  const ZeroJob& z = ex->zemit;
+  if (z.begin < z.n0) CUDA_TRY(cudaMemsetAsync(z.p0 + z.begin, 0, (size_t)(std::min(z.end, z.n0) - z.begin), s));
+  if (z.end > z.n0) {
+    const int64_t b = std::max(z.begin, z.n0);
+    CUDA_TRY(cudaMemsetAsync(z.p1 + (b - z.n0), 0, (size_t)(z.end - b), s));
+  }
   return DISO_OK;
 }
 

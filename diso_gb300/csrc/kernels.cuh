@@ -696,6 +696,56 @@ struct BoxCursor {
   __device__ int kind() const { return t == tz0 - 1 ? 1 : (t == tz1 ? 2 : 0); }
 };
 
+// Zeros written beside a forward's kernels (the gradient buffers of a forward whose
+// backward writes only the point tiles near the surface): the bytes [begin, end) of
+// two 16-byte aligned ranges seen as one, written by bulk copies of a zeroed block of
+// shared memory, so that the writes cost the warps neither issue slots nor load/store
+// bandwidth.  Round r of CTA b is the rbytes from begin + (r * gridDim.x + b) * rbytes;
+// a CTA issues one round per step of its work (a box of the count, a tile of the
+// emit) and the rounds left at its end.
+constexpr int ZBUF = 4096;  // bytes of the zero block
+
+struct ZeroJob {
+  char* p0;
+  char* p1;
+  int64_t n0;          // bytes of p0 (a multiple of 16)
+  int64_t begin, end;  // multiples of 16
+  int64_t rounds;      // ceil((end - begin) / (gridDim.x * rbytes)), 0: no job
+  int64_t rbytes;      // bytes per round (a multiple of ZBUF)
+};
+
+// zero the block (all threads; a barrier must follow before the first round)
+__device__ __forceinline__ void zero_block_init(uint4* zbuf) {
+  for (int i = threadIdx.x; i < ZBUF / 16; i += blockDim.x) zbuf[i] = make_uint4(0u, 0u, 0u, 0u);
+  fence_proxy_async();  // the zeros are read by the bulk copies
+}
+
+// round r of this CTA, one piece of up to ZBUF bytes per lane of the calling warp
+__device__ __forceinline__ void zero_round(const ZeroJob& z, const void* zbuf, int64_t r, int lane) {
+  if (r >= z.rounds) return;
+  const int64_t start = z.begin + (r * gridDim.x + blockIdx.x) * z.rbytes;
+  const int64_t end = min(start + z.rbytes, z.end);
+  bool any = false;
+  for (int64_t o = start + (int64_t)lane * ZBUF; o < end; o += 32 * ZBUF) {
+    const int64_t e = min(o + (int64_t)ZBUF, end);
+    if (o < z.n0) {  // the piece may run past the end of p0 into p1
+      const int64_t e0 = min(e, z.n0);
+      bulk_store(z.p0 + o, zbuf, (uint32_t)(e0 - o));
+      if (e > z.n0) bulk_store(z.p1, zbuf, (uint32_t)(e - z.n0));
+    } else {
+      bulk_store(z.p1 + (o - z.n0), zbuf, (uint32_t)(e - o));
+    }
+    any = true;
+  }
+  if (any) bulk_commit();
+}
+
+// the rounds from r on, then wait for all of the warp's copies
+__device__ __forceinline__ void zero_finish(const ZeroJob& z, const void* zbuf, int64_t r, int lane) {
+  for (; r < z.rounds; ++r) zero_round(z, zbuf, r, lane);
+  bulk_wait_all();
+}
+
 template <class S>
 __device__ __forceinline__ void issue_box(const CUtensorMap* wide, const CUtensorMap* narrow, void* dst,
                                           uint64_t* bar, const BoxCursor& c) {
@@ -770,13 +820,15 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
                                                                 Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                                 uint8_t* __restrict__ tile_flag,
                                                                 CellRec* __restrict__ codes, Stats* stats,
-                                                                int* __restrict__ active) {
+                                                                int* __restrict__ active, const ZeroJob zj) {
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   __shared__ CountShared<S, METHOD> sh;
   __shared__ __align__(8) uint64_t full[TMA_STAGES];
+  __shared__ __align__(128) uint4 zbuf[ZBUF / 16];
   unsigned char* stage_mem = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nunits = count_tma_units(g);
+  if (zj.rounds) zero_block_init(zbuf);
   if (threadIdx.x == 0) {
     sh.nlist = 0;
     sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
@@ -815,6 +867,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
         if (r < CROWS && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1) vrows |= 1ull << i;
       }
     }
+    if (warp == 1) zero_round(zj, zbuf, k, lane);
     const bool ok = mbar_wait_bounded(&full[st], (uint32_t)((k / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
     box_ballots<S, METHOD>(sh, f, reinterpret_cast<const S*>(stage_mem + st * tma_box_bytes<S>()), cc.t, cc.kind(),
                            vrows, mn, mx);
@@ -852,6 +905,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
     for (int64_t j = k; j < issued; ++j)
       mbar_wait_bounded(&full[j % TMA_STAGES], (uint32_t)((j / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
   }
+  if (warp == 1) zero_finish(zj, zbuf, k, lane);
   publish_minmax<S>(stats, mn, mx);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
@@ -1109,20 +1163,28 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
                                                            const unsigned long long* __restrict__ n_active,
                                                            S* __restrict__ verts, int64_t* __restrict__ faces,
                                                            int normalize, void* record, int64_t vcap, int64_t fcap,
-                                                           Stats* stats) {
-  if (!emit_fits<MC>(g, seg, vcap, fcap, stats)) return;
-  const EdgeRecord<S> rec = grid_record<S, MC>(record, g, seg);
-  const int64_t n = (int64_t)*n_active;
+                                                           Stats* stats, const ZeroJob zj) {
+  __shared__ __align__(128) uint4 zbuf[ZBUF / 16];
   __shared__ int64_t next;
+  if (zj.rounds) zero_block_init(zbuf);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t it = 0;  // tiles of this CTA, one zero round each
+  if (emit_fits<MC>(g, seg, vcap, fcap, stats)) {
+    const EdgeRecord<S> rec = grid_record<S, MC>(record, g, seg);
+    const int64_t n = (int64_t)*n_active;
 #pragma unroll 1
-  for (;;) {
-    if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
-    __syncthreads();
-    const int64_t t = next;
-    __syncthreads();
-    if (t >= n) break;
-    mc_emit_tile<S>(f, g, seg, active[t], verts, faces, normalize, 0, rec);
+    for (;; ++it) {
+      if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
+      __syncthreads();
+      const int64_t t = next;
+      __syncthreads();
+      if (t >= n) break;
+      if (warp == 1) zero_round(zj, zbuf, it, lane);
+      mc_emit_tile<S>(f, g, seg, active[t], verts, faces, normalize, 0, rec);
+    }
   }
+  __syncthreads();
+  if (warp == 1) zero_finish(zj, zbuf, it, lane);
 }
 
 // ------------------------------------------------------------------ DMC emit
@@ -1360,20 +1422,28 @@ __global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom 
                                                                const unsigned long long* __restrict__ n_active,
                                                                S* __restrict__ verts, int64_t* __restrict__ quads,
                                                                int normalize, void* record, int64_t vcap,
-                                                               int64_t fcap, Stats* stats) {
-  if (!emit_fits<DMC>(g, seg, vcap, fcap, stats)) return;
-  const EdgeRecord<S> rec = grid_record<S, DMC>(record, g, seg);
-  const int64_t n = (int64_t)*n_active;
+                                                               int64_t fcap, Stats* stats, const ZeroJob zj) {
+  __shared__ __align__(128) uint4 zbuf[ZBUF / 16];
   __shared__ int64_t next;
+  if (zj.rounds) zero_block_init(zbuf);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t it = 0;  // tiles of this CTA, one zero round each
+  if (emit_fits<DMC>(g, seg, vcap, fcap, stats)) {
+    const EdgeRecord<S> rec = grid_record<S, DMC>(record, g, seg);
+    const int64_t n = (int64_t)*n_active;
 #pragma unroll 1
-  for (;;) {
-    if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
-    __syncthreads();
-    const int64_t t = next;
-    __syncthreads();
-    if (t >= n) break;
-    dmc_emit_tile<S>(f, g, seg, codes, active[t], verts, quads, normalize, 0, rec);
+    for (;; ++it) {
+      if (threadIdx.x == 0) next = (int64_t)atomicAdd(&stats->emit_tile, 1ull);
+      __syncthreads();
+      const int64_t t = next;
+      __syncthreads();
+      if (t >= n) break;
+      if (warp == 1) zero_round(zj, zbuf, it, lane);
+      dmc_emit_tile<S>(f, g, seg, codes, active[t], verts, quads, normalize, 0, rec);
+    }
   }
+  __syncthreads();
+  if (warp == 1) zero_finish(zj, zbuf, it, lane);
 }
 
 // ------------------------------------------------------------------ backward

@@ -80,6 +80,8 @@ class _ExtractFunction(Function):
         ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg,
                               record if record is not None else seg.new_empty(0))
         ctx.mark_non_differentiable(faces)
+        # the faces never get a gradient; without this autograd would fill one with zeros
+        ctx.set_materialize_grads(False)
         return verts, faces
 
     @staticmethod

@@ -137,13 +137,19 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                   double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
                   const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
 
-/* Zero a forward's gradient buffers ahead of its backward, on `zero_stream` (after
- * the work already queued on `stream`), so that the writes overlap the forward's
- * kernels, which leave HBM bandwidth unused; the caller keeps the buffers alive until
- * that stream has passed them (e.g. torch's Tensor.record_stream).  A later
- * diso_backward on the same extractor with flags | DISO_GRAD_ZEROED waits for the
- * zeros and writes only the point tiles near the surface.  No counterpart in the
- * reference (its backward zero-fills the padded gradients, diso/__init__.py:35-37, 89-91). */
+/* Zero a forward's gradient buffers ahead of its backward, beside the forward's
+ * kernels, which leave HBM bandwidth unused.  Call it before diso_forward_count /
+ * diso_forward on `stream`; the zeros are complete once that forward's emit has run
+ * (or its count found no surface).  When both buffers are 16-byte aligned, the
+ * count and the emit write the zeros between their own loads; otherwise (or when the
+ * count runs on another stream, or the SDF's rows are not a multiple of 16 bytes)
+ * they are memsets on `zero_stream` after the work queued on `stream`, and the caller
+ * keeps the buffers alive until that stream has passed them (e.g. torch's
+ * Tensor.record_stream).  A second call before any forward replaces the first, whose
+ * buffers are then not written.  A later diso_backward on the same extractor with
+ * flags | DISO_GRAD_ZEROED waits for the zeros and writes only the point tiles near
+ * the surface.  No counterpart in the reference (its backward zero-fills the padded
+ * gradients, diso/__init__.py:35-37, 89-91). */
 int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void* grad_deform, int64_t deform_bytes,
                     void* stream, void* zero_stream);
 

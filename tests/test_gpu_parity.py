@@ -215,6 +215,67 @@ def test_second_backward_and_forward_without_backward(cuda_device):
         assert g1.abs().sum() > 0 and d1.abs().sum() > 0
 
 
+@pytest.mark.parametrize("nz", [36, 35])
+def test_gradient_zeroing_paths(cuda_device, nz):
+    # buffers given to diso_zero_grads are zero once the next forward on the same
+    # stream has run: written by its count and emit (rows of 36 floats: the TMA count;
+    # bytes past the last 16-byte vector included), by memsets when the count finds no
+    # surface, on the side stream otherwise (rows of 35 floats, a misaligned buffer, a
+    # count on another stream)
+    from diso_gb300 import _native as N
+
+    ex = N.Extractor(N.DMC, torch.float32)
+    rng = np.random.default_rng(5)
+    g = torch.tensor(rng.uniform(-1, 1, (21, 18, nz)).astype(np.float32), device=cuda_device)
+    iso, pad = N.iso_values(0.0, torch.float32)
+    seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=cuda_device)
+
+    def forward(grid):
+        c = ex.count(grid, iso, pad, seg)
+        if not c.empty:
+            verts = torch.empty((c.n_verts, 3), device=cuda_device)
+            quads = torch.empty((c.n_faces, 4), dtype=torch.int64, device=cuda_device)
+            ex.emit(grid, None, iso, pad, seg, True, verts, quads)
+        return c
+
+    def nans(n, offset=0):
+        return torch.full((n + offset,), float("nan"), device=cuda_device)[offset:]
+
+    def zeroed(*ts):
+        torch.cuda.synchronize()
+        return all(bool(torch.all(t == 0)) for t in ts if t is not None)
+
+    a, b = nans(g.numel() + 2), nans(3 * g.numel() + 1)
+    ex.zero_grads(a, b)
+    assert not forward(g).empty
+    assert zeroed(a, b)
+    a = nans(1000)
+    ex.zero_grads(a, None)
+    forward(g)
+    assert zeroed(a)
+    a, b = nans(g.numel()), nans(3 * g.numel())
+    ex.zero_grads(a, b)
+    assert forward(g + 2).empty
+    assert zeroed(a, b)
+    a, b = nans(999, offset=1), nans(77)
+    assert a.data_ptr() % 16 != 0
+    ex.zero_grads(a, b)
+    forward(g)
+    assert zeroed(a, b)
+    a1, a2 = nans(5000), nans(7000)
+    ex.zero_grads(a1, None)
+    ex.zero_grads(a2, None)  # replaces the first call's buffers
+    forward(g)
+    assert zeroed(a2)
+    a, b = nans(3000), nans(50)
+    ex.zero_grads(a, b)
+    other = torch.cuda.Stream(cuda_device)
+    other.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(other):
+        c = forward(g)
+    assert zeroed(a, b) and c.n_faces > 0
+
+
 @pytest.mark.parametrize("method", ["mc", "dmc"])
 def test_single_call_forward_and_capacity_fallback(cuda_device, method):
     # a module that has seen a grid of this shape runs the forward as one native call
