@@ -290,20 +290,23 @@ class PhaseEvents:
         return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in self.done.items()}
 
 
-def kernel_bytes(vol, nseg, nv, nq, s):
+def kernel_bytes(vol, nseg, nv, nq, s, zshare):
     """Algorithmic bytes of one launch of each kernel of the 512^3 DMC step: what the
     kernel's function must read and write at least (nq crossing edges = quads, nv
-    patches = vertices, s bytes per scalar)."""
+    patches = vertices, s bytes per scalar).  The zeros of the two gradient arrays are
+    written by the count (the share zshare) and the emit (the rest), or by memsets
+    ("zero_grads") when the buffers do not allow it."""
+    zeros = vol * 4 * s
     return {
-        # the SDF once; the scanned per-segment counts out
-        "count": vol * s + nseg * 8,
+        # the SDF once; the scanned per-segment counts out; its share of the zeros
+        "count": vol * s + nseg * 8 + zshare * zeros,
         # segment counts in and out
         "scan": 2 * nseg * 8,
         # both end points of every crossing edge (SDF + deform) in; vertices, quads and
-        # the edge record (cell + axis, four patch ids, a byte per vertex) out
-        "emit": 2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8 + nq * (8 + 16) + nv,
-        # the two gradient arrays
-        "zero_grads": vol * 4 * s,
+        # the edge record (cell + axis, four patch ids, a byte per vertex) out; the rest
+        # of the zeros
+        "emit": 2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8 + nq * (8 + 16) + nv + (1 - zshare) * zeros,
+        "zero_grads": zeros,
         # per edge: record (cell, 4 patch ids), 4 patch bytes and 4 dL/dverts in, end points
         # (SDF + deform) in, 2 x 4 adjoints out
         "edge": nq * (8 + 16 + 4 + 4 * 3 * s + 2 * 4 * s + 8 * s),
@@ -337,6 +340,7 @@ def measured_peaks():
 
 def run_ours(args, rank, world, device):
     from diso_gb300 import DiffDMC
+    from diso_gb300 import _native as N
     import diso_gb300.extraction as X
 
     n = args.n
@@ -425,7 +429,8 @@ def run_ours(args, rank, world, device):
     s_b = 4
     vol = n ** 3
     nseg = (n + 1) ** 2 * ((n + 1 + 31) // 32)
-    algo = kernel_bytes(vol, nseg, nv, nq, s_b)
+    zshare = 0.0 if "zero_grads" in kernels else float(N.lib().diso_zero_count_share())
+    algo = kernel_bytes(vol, nseg, nv, nq, s_b, zshare)
     per_launch = {k: ms / max(cnt, 1) for k, (cnt, ms) in kernels.items()}
     ours = {k: v for k, v in per_launch.items() if k in algo and k != "zero_grads"}
     dom = max(ours, key=lambda k: ours[k] * kernels[k][0])

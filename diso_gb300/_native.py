@@ -69,6 +69,7 @@ EXPORTS = {
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
     "diso_zero_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_zero_count_share": (ctypes.c_double, []),
     "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),

@@ -1075,6 +1075,8 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                                                   deform ? grad_deform : nullptr, s);
 }
 
+double diso_zero_count_share(void) { return ZERO_COUNT_SHARE; }
+
 int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void* grad_deform, int64_t deform_bytes,
                     void* stream, void* zero_stream) {
   if (!ex) return fail(DISO_ERR_ARG, "null extractor");

@@ -153,6 +153,10 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
 int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void* grad_deform, int64_t deform_bytes,
                     void* stream, void* zero_stream);
 
+/* Share of diso_zero_grads' bytes that the count writes (the first bytes of
+ * grad_sdf then grad_deform, laid end to end); the emit writes the rest. */
+double diso_zero_count_share(void);
+
 /* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
  * device memory: code running while a stream is being captured, where cudaMalloc
  * is not allowed, and serving processes that fix their device memory at start-up
