@@ -100,6 +100,34 @@ __device__ __forceinline__ void edge_vertex(const Field<S>& f, int X, int Y, int
   for (int k = 0; k < 3; ++k) out[k] = p0[k] + (p1[k] - p0[k]) * t;
 }
 
+// edge_vertex for an edge whose two points lie inside the caller's grid: no pad
+// tests, one index for both points
+template <class S>
+__device__ __forceinline__ void edge_vertex_in(const Field<S>& f, int X, int Y, int Z, int a, S out[3]) {
+  const int ex = a == 0, ey = a == 1, ez = a == 2;
+  const int64_t i0 = f.lin(X, Y, Z);
+  const int64_t i1 = i0 + (a == 0 ? (int64_t)f.n1 * f.n2 : (a == 1 ? (int64_t)f.n2 : (int64_t)1));
+  const S d0 = __ldg(f.sdf + i0), d1 = __ldg(f.sdf + i1);
+  S t = S(0.5);
+  if (d1 != d0) {
+    S r = (f.iso - d0) / (d1 - d0);
+    r = S(0) > r ? S(0) : r;
+    t = r < S(1) ? r : S(1);
+  }
+  S q0[3] = {S(0), S(0), S(0)}, q1[3] = {S(0), S(0), S(0)};
+  if (f.def) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      q0[k] = __ldg(f.def + 3 * i0 + k);
+      q1[k] = __ldg(f.def + 3 * i1 + k);
+    }
+  }
+  const S p0[3] = {S(X) + q0[0], S(Y) + q0[1], S(Z) + q0[2]};
+  const S p1[3] = {S(X + ex) + q1[0], S(Y + ey) + q1[1], S(Z + ez) + q1[2]};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[k] = p0[k] + (p1[k] - p0[k]) * t;
+}
+
 // verts - 1, then / (dim - 1) (diso/__init__.py:56-60)
 template <class S>
 __device__ __forceinline__ void store_vertex(S* __restrict__ verts, int64_t i, const S p[3], const Geom& g,
@@ -1196,6 +1224,7 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
 // most of their edges).  Tiles with more crossing edges compute them per patch.
 constexpr int EW_ROWS = (TX + 1) * (TY + 1);
 constexpr int EW_ITEMS = EW_ROWS * 3 * (TZ + 1);
+static_assert(EW_ITEMS < (1 << 13), "window slots and flags share 16 bits");
 constexpr int EPOS_BYTES = 24576;
 template <class S>
 __host__ __device__ constexpr int epos_cap() {
@@ -1223,6 +1252,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   __shared__ RowBits wb[TX + 1][TY + 1];  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint8_t w32[TX + 1][TY + 1];  // crossing flags of the row's cell Z0 + TZ
   __shared__ uint16_t wbase[TX + 1][TY + 1];
+  __shared__ uint16_t wcell[TX + 1][TY + 1][TZ + 1];  // per edge-row cell: first window slot | flags << 13
   __shared__ uint16_t cbase[TX][TY];
   __shared__ uint16_t witems[EW_ITEMS];
   __shared__ uint16_t citems[TX * TY * TZ];
@@ -1312,11 +1342,13 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int fl = row_flags(w, lane);
     const uint32_t before = row_prefix(w, lane);
     uint32_t o = wbase[ex_][ey] + before;
+    wcell[ex_][ey][lane] = (uint16_t)(o | (fl << 13));
 #pragma unroll
     for (int a = 0; a < 3; ++a)
       if (fl & (1 << a)) witems[o++] = item_code(ex_, ey, lane, a);
     if (lane == 31) {
       const int f32 = w32[ex_][ey];
+      wcell[ex_][ey][TZ] = (uint16_t)(o | (f32 << 13));
 #pragma unroll
       for (int a = 0; a < 3; ++a)
         if (f32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
@@ -1326,6 +1358,9 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   }
   __syncthreads();
   const bool cached = nwi <= (uint32_t)CAP;
+  // every end point of the window's edges lies inside the caller's grid
+  const bool inner = X0 >= 1 && Y0 >= 1 && Z0 >= 1 && X0 + TX + 1 <= f.n0 && Y0 + TY + 1 <= f.n1 &&
+                     Z0 + TZ + 1 <= f.n2;
   // window edges: lerp vertices into the cache; the tile's own edges also give its quads
   // (one per crossing edge owned by a tile cell, src/cudualmc.cu:753-794, 1019-1056);
   // the edge exits (value falls through iso) when its start point is >= iso
@@ -1334,7 +1369,10 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     item_decode(witems[i], ix, iy, j, a);
     if (cached) {
       S p[3];
-      edge_vertex<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+      if (inner)
+        edge_vertex_in<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+      else
+        edge_vertex<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
       epos[i][0] = p[0];
       epos[i][1] = p[1];
       epos[i][2] = p[2];
@@ -1368,10 +1406,8 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   __syncthreads();
   // window slot of the edge along a owned by edge-row cell (x, y, j), j in [0, TZ]
   auto wslot = [&](int x, int y, int j, int a) -> int {
-    const RowBits r = wb[x][y];
-    if (j == TZ)
-      return wbase[x][y] + __popc(r.xc) + __popc(r.yc) + __popc(r.zc) + __popc(w32[x][y] & ((1 << a) - 1));
-    return wbase[x][y] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
+    const int w = wcell[x][y][j];
+    return (w & 0x1fff) + __popc((w >> 13) & ((1 << a) - 1));
   };
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
   // (create_dmc_verts_kernel, src/cudualmc.cu:907-955); a patch's edges come from the
@@ -1650,9 +1686,9 @@ __device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, co
   constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
   constexpr int CX = TX + 1, CY = TY + 1;  // cell rows [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint64_t m[WX][WY];
-  __shared__ RowBits rb[CX][CY];
-  __shared__ uint8_t f32[CX][CY];           // crossing flags of cell Z0 + TZ (first of the next chunk)
   __shared__ uint32_t b0[CX][CY], b1[CX][CY];  // first edge of the cell row's chunks zc and zc + 1
+  __shared__ uint32_t eb[CX][CY][TZ + 1];      // first edge of each window cell
+  __shared__ uint8_t ef[CX][CY][TZ + 1];       // its crossing flags (bit a: the edge along a)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0;
   ptile_coords(ptile, g, X0, Y0, Z0);
@@ -1672,39 +1708,38 @@ __device__ __forceinline__ void gather_tile(const Field<S>& f, const Geom& g, co
     else b0[sx][sy] = Counts::lo(sv);
   }
   __syncthreads();
+  // per window cell: crossing flags and the index of its first crossing edge (one
+  // warp per cell row, lane j for cell j, lane 31 also for cell TZ)
   const uint32_t valid = zvalid(g, Z0);
-  if (threadIdx.x < CX * CY) {
-    const int x = threadIdx.x / CY, y = threadIdx.x % CY;
-    RowBits r = {0u, 0u, 0u, 0u};
-    int fl = 0;
+  for (int r = warp; r < CX * CY; r += NTHREADS / 32) {
+    const int x = r / CY, y = r % CY;
+    RowBits rw = {0u, 0u, 0u, 0u};
+    int f32 = 0;
     if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
-      r = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
-      if (Z0 + TZ < g.c[2]) fl = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
+      rw = row_bits(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], valid);
+      if (Z0 + TZ < g.c[2]) f32 = flags_at(m[x][y], m[x + 1][y], m[x][y + 1], TZ + 1);
     }
-    rb[x][y] = r;
-    f32[x][y] = (uint8_t)fl;
+    eb[x][y][lane] = b0[x][y] + (uint32_t)row_prefix(rw, lane);
+    ef[x][y][lane] = (uint8_t)row_flags(rw, lane);
+    if (lane == 31) {
+      eb[x][y][TZ] = b1[x][y];
+      ef[x][y][TZ] = (uint8_t)f32;
+    }
   }
   __syncthreads();
-  // edge along a owned by window cell (x, y, j): crossing?  and its index
-  auto crossing = [&](int x, int y, int j, int a) -> int {
-    return j == TZ ? (f32[x][y] >> a) & 1 : (row_flags(rb[x][y], j) >> a) & 1;
-  };
-  auto eid = [&](int x, int y, int j, int a) -> int64_t {
-    if (j == TZ) return (int64_t)b1[x][y] + __popc(f32[x][y] & ((1 << a) - 1));
-    const RowBits r = rb[x][y];
-    return (int64_t)b0[x][y] + row_prefix(r, j) + __popc(row_flags(r, j) & ((1 << a) - 1));
-  };
-#pragma unroll 1
+#pragma unroll
   for (int ix = 0; ix < TX; ++ix) {
     const int x = ix + 1, y = warp + 1, j = lane + 1;
     S acc[4] = {S(0), S(0), S(0), S(0)};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      // the edge from this point along a (first point), then the edge ending here
-      if (crossing(x, y, j, a)) add_adj<S>(adj, eid(x, y, j, a), 0, acc);
-      const int xb = x - (a == 0), yb = y - (a == 1), jb = j - (a == 2);
-      if (crossing(xb, yb, jb, a)) add_adj<S>(adj, eid(xb, yb, jb, a), 1, acc);
-    }
+    // per axis the edge from this point (first point), then the edge ending here
+    const int fo = ef[x][y][j], fx = ef[x - 1][y][j], fy = ef[x][y - 1][j], fz = ef[x][y][j - 1];
+    const uint32_t bo = eb[x][y][j];
+    if (fo & 1) add_adj<S>(adj, bo, 0, acc);
+    if (fx & 1) add_adj<S>(adj, eb[x - 1][y][j], 1, acc);
+    if (fo & 2) add_adj<S>(adj, bo + (fo & 1), 0, acc);
+    if (fy & 2) add_adj<S>(adj, eb[x][y - 1][j] + (fy & 1), 1, acc);
+    if (fo & 4) add_adj<S>(adj, bo + __popc(fo & 3), 0, acc);
+    if (fz & 4) add_adj<S>(adj, eb[x][y][j - 1] + __popc(fz & 3), 1, acc);
     const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
     if (f.inside(X, Y, Z)) {
       const int64_t i = f.lin(X, Y, Z);
@@ -1761,7 +1796,7 @@ __global__ void __launch_bounds__(256) active_ptiles_kernel(Geom g, const uint8_
 
 // gather of the active point tiles in the list (persistent)
 template <class S>
-__global__ void __launch_bounds__(NTHREADS) gather_list_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+__global__ void __launch_bounds__(NTHREADS, sizeof(S) == 4 ? 4 : 3) gather_list_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
                                                                const int* __restrict__ list,
                                                                const unsigned* __restrict__ count,
                                                                const void* __restrict__ record, S* __restrict__ gsdf,
