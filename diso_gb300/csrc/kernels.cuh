@@ -1225,6 +1225,7 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, c
 constexpr int EW_ROWS = (TX + 1) * (TY + 1);
 constexpr int EW_ITEMS = EW_ROWS * 3 * (TZ + 1);
 static_assert(EW_ITEMS < (1 << 13), "window slots and flags share 16 bits");
+static_assert(EW_ITEMS >= 4 * TX * TY * TZ, "the window item list also holds a tile's patches");
 constexpr int EPOS_BYTES = 24576;
 template <class S>
 __host__ __device__ constexpr int epos_cap() {
@@ -1255,7 +1256,7 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   __shared__ uint16_t wcell[TX + 1][TY + 1][TZ + 1];  // per edge-row cell: first window slot | flags << 13
   __shared__ uint16_t cbase[TX][TY];
   __shared__ uint16_t witems[EW_ITEMS];
-  __shared__ uint16_t citems[TX * TY * TZ];
+  __shared__ uint8_t prow[TX][TY];        // patches of the own rows' segments
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
   __shared__ uint32_t nwi, nci;
   __shared__ __align__(16) S epos[CAP][3];
@@ -1266,11 +1267,11 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   if (threadIdx.x < KX * KY) {
     const int wx = threadIdx.x / KY, wy = threadIdx.x % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
     uint32_t act = 0;
-    uint64_t s0 = 0;
+    uint64_t s0 = 0, s1 = 0;
     if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1]) {
       const int64_t i = g.seg(X, Y, tz);
       s0 = seg[i];
-      const uint64_t s1 = seg[i + 1];
+      s1 = seg[i + 1];
       if (s1 != s0) act |= 2;
       if (tz > 0 && seg[i - 1] != s0) act |= 1;
       if (tz + 1 < g.nzc && seg[i + 2] != s1) act |= 4;
@@ -1278,7 +1279,10 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     sact[wx][wy] = (uint8_t)act;
     if (wx < CX && wy < CY) {
       pb[wx][wy] = Counts::hi(s0);
-      if (wx >= 1 && wy >= 1) qb[wx - 1][wy - 1] = Counts::lo(s0);
+      if (wx >= 1 && wy >= 1) {
+        qb[wx - 1][wy - 1] = Counts::lo(s0);
+        prow[wx - 1][wy - 1] = (uint8_t)(Counts::hi(s1) - Counts::hi(s0));
+      }
     }
   }
   __syncthreads();
@@ -1312,16 +1316,16 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int r = cw[x][y][jj];
     return jj ? (r >> 9) : -(int)dmc_npatch(dmc_case(r & 0xff));
   };
-  // edge rows: crossing edges (window items) and, for the own rows, the non-trivial
-  // cells (dual vertex items); row bases by a block scan, then one warp per row
-  // writes the row's items
+  // edge rows: crossing edges (window items) and, for the own rows, the patches
+  // (dual vertex items); row bases by a block scan, then one warp per row writes the
+  // row's window items
   {
     uint32_t ce = 0, cc = 0;
     const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
     if (threadIdx.x < EW_ROWS) {
       const RowBits w = wb[ex_][ey];
       ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(w32[ex_][ey]);
-      if (ex_ < TX && ey < TY) cc = __popc(w.nt);
+      if (ex_ < TX && ey < TY) cc = prow[ex_][ey];
     }
     uint32_t tot;
     const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
@@ -1353,8 +1357,6 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
       for (int a = 0; a < 3; ++a)
         if (f32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
     }
-    if (ex_ < TX && ey < TY && ((w.nt >> lane) & 1))
-      citems[cbase[ex_][ey] + __popc(w.nt & ((1u << lane) - 1u))] = item_code(ex_, ey, lane, 0);
   }
   __syncthreads();
   const bool cached = nwi <= (uint32_t)CAP;
@@ -1409,44 +1411,54 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     const int w = wcell[x][y][j];
     return (w & 0x1fff) + __popc((w >> 13) & ((1 << a) - 1));
   };
+  // dual vertex items, one per patch in patch order, into the window item list (done
+  // with): the patches of a non-trivial cell run from its record's in-segment prefix
+  // to the next non-trivial cell's (the segment's total after the last one; trivial
+  // cells have no record)
+  for (int r = warp; r < TX * TY; r += NTHREADS / 32) {
+    const int ex_ = r / TY, ey = r % TY, x = ex_ + 1, y = ey + 1;
+    const uint32_t nt = wb[ex_][ey].nt;
+    if ((nt >> lane) & 1) {
+      const uint32_t later = nt & ~((2u << lane) - 1u);
+      const int p0 = cw[x][y][lane + 1] >> 9;
+      const int p1 = later ? cw[x][y][__ffs(later)] >> 9 : (int)prow[ex_][ey];
+      for (int q = 0; q < p1 - p0; ++q) witems[cbase[ex_][ey] + p0 + q] = item_code(ex_, ey, lane, q);
+    }
+  }
+  __syncthreads();
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
   // (create_dmc_verts_kernel, src/cudualmc.cu:907-955); a patch's edges come from the
   // per-code patch masks
   for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
-    int ix, iy, j, a;
-    item_decode(citems[i], ix, iy, j, a);
+    int ix, iy, j, q;
+    item_decode(witems[i], ix, iy, j, q);
     const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
-    const int code = rcode(x, y, j + 1);
-    const int np = dmc_npatch(dmc_case(code));
-    const uint64_t pm = __ldg(&g_dmc_pmask.m[code]);
-    const int64_t p0 = (int64_t)pb[x][y] + ppatch(x, y, j + 1);
-#pragma unroll 1
-    for (int q = 0; q < np; ++q) {
-      uint32_t m = (uint32_t)(pm >> (12 * q)) & 0xfffu;
-      const int cnt = __popc(m);
-      S acc[3] = {S(0), S(0), S(0)};
-      while (m) {
-        const int e = __ffs(m) - 1;
-        m &= m - 1;
-        const int ge = edge_desc(e), s = ge & 7, ax = ge >> 3;
-        S v[3];
-        if (cached) {
-          const int k = wslot(ix + (s & 1), iy + ((s >> 1) & 1), j + ((s >> 2) & 1), ax);
-          v[0] = epos[k][0];
-          v[1] = epos[k][1];
-          v[2] = epos[k][2];
-        } else {
-          edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
-        }
-        acc[0] += v[0];
-        acc[1] += v[1];
-        acc[2] += v[2];
+    const int rc = cw[x][y][j + 1];
+    uint32_t m = (uint32_t)(__ldg(&g_dmc_pmask.m[rc & 0xff]) >> (12 * q)) & 0xfffu;
+    const int64_t p = (int64_t)pb[x][y] + (rc >> 9) + q;
+    const int cnt = __popc(m);
+    S acc[3] = {S(0), S(0), S(0)};
+    while (m) {
+      const int e = __ffs(m) - 1;
+      m &= m - 1;
+      const int ge = edge_desc(e), s = ge & 7, ax = ge >> 3;
+      S v[3];
+      if (cached) {
+        const int k = wslot(ix + (s & 1), iy + ((s >> 1) & 1), j + ((s >> 2) & 1), ax);
+        v[0] = epos[k][0];
+        v[1] = epos[k][1];
+        v[2] = epos[k][2];
+      } else {
+        edge_vertex<S>(f, X + (s & 1), Y + ((s >> 1) & 1), Z + ((s >> 2) & 1), ax, v);
       }
-      const S inv = recip<S>(cnt);  // S(1) / S(cnt)
-      const S v[3] = {acc[0] * inv, acc[1] * inv, acc[2] * inv};
-      store_vertex<S>(verts, p0 + q, v, g, normalize);
-      if (rec.aux) rec.aux[p0 + q] = (uint8_t)(cnt | (q << 4));
+      acc[0] += v[0];
+      acc[1] += v[1];
+      acc[2] += v[2];
     }
+    const S inv = recip<S>(cnt);  // S(1) / S(cnt)
+    const S v[3] = {acc[0] * inv, acc[1] * inv, acc[2] * inv};
+    store_vertex<S>(verts, p, v, g, normalize);
+    if (rec.aux) rec.aux[p] = (uint8_t)(cnt | (q << 4));
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
