@@ -15,8 +15,8 @@
 
 namespace diso {
 
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 16;  // a thread's elements: 128 contiguous bytes
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr unsigned SCAN_SPIN_LIMIT = 1u << 22;
 
@@ -46,14 +46,27 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* _
   const int64_t tile = tile_id_s;
   const int64_t base = tile * SCAN_TILE + (int64_t)tid * SCAN_ITEMS;
 
+  // whole tiles of a 16-byte aligned array move as 16-byte vectors
+  const bool whole = (tile + 1) * SCAN_TILE <= n && ((uintptr_t)a & 15u) == 0;
   uint64_t v[SCAN_ITEMS];
+  if (whole) {
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(a + base);
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS / 2; ++i) {
+      const ulonglong2 w = p[i];
+      v[2 * i] = w.x;
+      v[2 * i + 1] = w.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      const int64_t k = base + i;
+      v[i] = (k < n) ? a[k] : 0ull;
+    }
+  }
   uint64_t sum = 0;
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) {
-    int64_t k = base + i;
-    v[i] = (k < n) ? a[k] : 0ull;
-    sum += v[i];
-  }
+  for (int i = 0; i < SCAN_ITEMS; ++i) sum += v[i];
   // block exclusive scan of the thread sums
   uint64_t incl = warp_incl64(sum);
   if (lane == 31) warp_tot[warp] = incl;
@@ -116,11 +129,24 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* _
   }
   __syncthreads();
   uint64_t run = tile_excl + texcl;
+  if (whole) {
+    ulonglong2* p = reinterpret_cast<ulonglong2*>(a + base);
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) {
-    int64_t k = base + i;
-    if (k <= n) a[k] = run;
-    run += v[i];
+    for (int i = 0; i < SCAN_ITEMS / 2; ++i) {
+      ulonglong2 w;
+      w.x = run;
+      run += v[2 * i];
+      w.y = run;
+      run += v[2 * i + 1];
+      p[i] = w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      const int64_t k = base + i;
+      if (k <= n) a[k] = run;
+      run += v[i];
+    }
   }
 }
 

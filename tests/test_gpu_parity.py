@@ -79,6 +79,10 @@ ORACLE_CASES = [
     ("dmc", "float32", "uniform", (2, 1, 64), 0.45, 0.0, True, True),
     ("mc", "float32", "spheres", (128, 128, 128), 0.45, 0.0, True, False),
     ("dmc", "float32", "spheres", (128, 128, 128), 0.45, 0.0, True, True),
+    # 64 x 128 rows of one and of two 32-cell segments: 8192 and 16384 segments, whole
+    # tiles of the segment scan
+    ("mc", "float32", "uniform", (63, 127, 31), None, 0.0, True, False),
+    ("dmc", "float32", "spheres", (63, 127, 63), 0.3, 0.0, True, True),
 ]
 
 
