@@ -70,6 +70,18 @@ EXPORTS = {
     "diso_zero_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_zero_count_share": (ctypes.c_double, []),
+    "diso_mesh_normals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                         ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_mesh_weld": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                      ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.c_void_p]),
+    "diso_mesh_obj": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
+                                     ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p]),
+    "diso_mesh_ply_bytes": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]),
+    "diso_mesh_ply": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),
@@ -210,6 +222,29 @@ class Extractor:
         grad_sdf.record_stream(side)
         if grad_deform is not None:
             grad_deform.record_stream(side)
+
+    # mesh consumers (diso_mesh_*): the extractor supplies the dtype and the scratch
+    def mesh_normals(self, verts, faces, out):
+        check(lib().diso_mesh_normals(self._h, ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], faces.shape[1],
+                                      ptr(out), stream_of(verts.device)), "vertex normals")
+
+    def mesh_weld(self, verts, faces, tol, out_verts, out_faces):
+        nv, nf = ctypes.c_int64(0), ctypes.c_int64(0)
+        check(lib().diso_mesh_weld(self._h, ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], faces.shape[1],
+                                   float(tol), ptr(out_verts), ptr(out_faces), ctypes.byref(nv), ctypes.byref(nf),
+                                   stream_of(verts.device)), "weld")
+        return int(nv.value), int(nf.value)
+
+    def mesh_obj(self, verts, normals, faces, text=None):
+        n = ctypes.c_int64(0)
+        check(lib().diso_mesh_obj(self._h, ptr(verts), ptr(normals), verts.shape[0], ptr(faces), faces.shape[0],
+                                  faces.shape[1], ptr(text), text.numel() if text is not None else 0,
+                                  ctypes.byref(n), stream_of(verts.device)), "OBJ text")
+        return int(n.value)
+
+    def mesh_ply(self, verts, normals, faces, body):
+        check(lib().diso_mesh_ply(self._h, ptr(verts), ptr(normals), verts.shape[0], ptr(faces), faces.shape[0],
+                                  faces.shape[1], ptr(body), stream_of(verts.device)), "PLY body")
 
     def backward(self, sdf, deform, iso, pad, seg, record, normalize, grad_verts, grad_sdf, grad_deform,
                  exact=False, zeroed=False):

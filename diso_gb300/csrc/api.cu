@@ -12,6 +12,7 @@
 
 #include "../../include/diso_gb300.h"
 #include "kernels.cuh"
+#include "mesh.cuh"
 #include "scan.cuh"
 
 using namespace diso;
@@ -65,6 +66,8 @@ struct diso_extractor {
   int64_t codes_cap = 0;
   uint64_t* split = nullptr;     // split counts (n_quads + 1)
   int64_t split_cap = 0;
+  uint8_t* mesh = nullptr;       // mesh consumers' scratch (normals, weld, OBJ), bytes
+  int64_t mesh_cap = 0;
   int64_t last_active = 0;       // from the last forward count
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
   int tma_ctas = 0;              // the same for the TMA count kernel
@@ -145,6 +148,9 @@ struct diso_extractor {
     codes = nullptr;
     codes_cap = 0;
     cudaFree(split);
+    cudaFree(mesh);
+    mesh = nullptr;
+    mesh_cap = 0;
     cudaFree(plist);
     cudaFree(plist_n);
     if (side) cudaStreamDestroy(side);
@@ -962,6 +968,141 @@ int batch_results(diso_extractor* ex, diso_counts* out, int64_t* voff, int64_t* 
 
 }  // namespace
 
+
+// ------------------------------------------------------------------ mesh consumers
+
+constexpr unsigned long long MESH_ERR_INDEX = 8ull;  // Stats::error bit 3: a face index out of range
+
+inline unsigned mesh_ctas(const diso_extractor* ex, int64_t n) { return stride_ctas(n, (unsigned)ex->sms * 8u); }
+
+// the extractor's mesh scratch as consecutive 256-byte aligned pieces
+struct MeshCarve {
+  uint8_t* base;
+  int64_t used = 0;
+  template <class T>
+  T* take(int64_t count) {
+    T* p = (T*)(base + used);
+    used += (count * (int64_t)sizeof(T) + 255) / 256 * 256;
+    return p;
+  }
+};
+
+int mesh_scratch(diso_extractor* ex, int64_t bytes) { return grow(ex->mesh, ex->mesh_cap, bytes); }
+
+// waits for the stream; an out-of-range face index is an argument error
+int mesh_finish(diso_extractor* ex, cudaStream_t s, const char* what) {
+  CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (ex->stats_host->error & 1ull) return fail(DISO_ERR_SCAN, "%s: scan look-back wait gave up", what);
+  if (ex->stats_host->error & MESH_ERR_INDEX) return fail(DISO_ERR_ARG, "%s: a face index is out of range", what);
+  return DISO_OK;
+}
+
+template <class S>
+int mesh_normals(diso_extractor* ex, const S* v, int64_t nv, const int64_t* faces, int64_t nf, int k, S* out,
+                 cudaStream_t s) {
+  int rc;
+  if ((rc = mesh_scratch(ex, nv * 24 + 512)) != DISO_OK) return rc;
+  MeshCarve c{ex->mesh};
+  unsigned long long* maxbits = c.take<unsigned long long>(1);
+  unsigned long long* acc = c.take<unsigned long long>(3 * nv);
+  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), s));
+  CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)(3 * nv) * sizeof(unsigned long long), s));
+  if (nf > 0) {
+    normals_max_kernel<S><<<mesh_ctas(ex, nf), 256, 0, s>>>(v, faces, nf, k, nv, maxbits, &ex->stats->error);
+    normals_acc_kernel<S><<<mesh_ctas(ex, nf), 256, 0, s>>>(v, faces, nf, k, nv, maxbits, acc);
+  }
+  normals_out_kernel<S><<<mesh_ctas(ex, nv), 256, 0, s>>>(acc, nv, out);
+  CUDA_TRY(cudaGetLastError());
+  return mesh_finish(ex, s, "vertex normals");
+}
+
+template <class S>
+int mesh_weld(diso_extractor* ex, const S* v, int64_t nv, const int64_t* faces, int64_t nf, int k, double tol,
+              S* out_v, int64_t* out_f, int64_t* nv_out, int64_t* nf_out, cudaStream_t s) {
+  uint32_t slots = 1024;
+  while ((int64_t)slots < 2 * nv) slots <<= 1;
+  int rc;
+  if ((rc = mesh_scratch(ex, (int64_t)slots * 4 + nv * 4 + (nv + 1) * 8 + (nf + 1) * 8 + nf * k * 8 + 1280)) !=
+      DISO_OK)
+    return rc;
+  MeshCarve c{ex->mesh};
+  int* table = c.take<int>(slots);
+  int* rep = c.take<int>(nv);
+  uint64_t* keep = c.take<uint64_t>(nv + 1);
+  uint64_t* keepf = c.take<uint64_t>(nf + 1);
+  int64_t* mapped = c.take<int64_t>(nf * k);
+  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(table, 0xff, (size_t)slots * sizeof(int), s));
+  weld_insert_kernel<S><<<mesh_ctas(ex, nv), 256, 0, s>>>(v, nv, tol, table, slots - 1);
+  weld_rep_kernel<S><<<mesh_ctas(ex, nv), 256, 0, s>>>(v, nv, tol, table, slots - 1, rep, keep);
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = run_scan(ex, keep, nv, s)) != DISO_OK) return rc;
+  if (nf > 0) {
+    weld_faces_kernel<<<mesh_ctas(ex, nf), 256, 0, s>>>(faces, nf, k, nv, rep, keep, mapped, keepf,
+                                                       &ex->stats->error);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if ((rc = run_scan(ex, keepf, nf, s)) != DISO_OK) return rc;
+  weld_compact_verts_kernel<S><<<mesh_ctas(ex, nv), 256, 0, s>>>(v, nv, rep, keep, out_v);
+  if (nf > 0) weld_compact_faces_kernel<<<mesh_ctas(ex, nf), 256, 0, s>>>(mapped, nf, k, keepf, out_f);
+  CUDA_TRY(cudaGetLastError());
+  uint64_t tot[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(&tot[0], keep + nv, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(&tot[1], keepf + nf, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if ((rc = mesh_finish(ex, s, "weld")) != DISO_OK) return rc;
+  *nv_out = (int64_t)tot[0];
+  *nf_out = (int64_t)tot[1];
+  return DISO_OK;
+}
+
+template <class S>
+int mesh_obj(diso_extractor* ex, const S* v, const S* nrm, int64_t nv, const int64_t* faces, int64_t nf, int k,
+             char* text, int64_t cap, int64_t* bytes, cudaStream_t s) {
+  const int64_t lines = (nrm ? 2 * nv : nv) + nf;
+  int rc;
+  if ((rc = mesh_scratch(ex, (lines + 1) * 8 + 256)) != DISO_OK) return rc;
+  MeshCarve c{ex->mesh};
+  uint64_t* off = c.take<uint64_t>(lines + 1);
+  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  if (lines > 0) obj_len_kernel<S><<<mesh_ctas(ex, lines), 256, 0, s>>>(v, nrm, nv, faces, nf, k, off);
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = run_scan(ex, off, lines, s)) != DISO_OK) return rc;
+  uint64_t total = 0;
+  CUDA_TRY(cudaMemcpyAsync(&total, off + lines, sizeof total, cudaMemcpyDeviceToHost, s));
+  if ((rc = mesh_finish(ex, s, "OBJ text")) != DISO_OK) return rc;
+  *bytes = (int64_t)total;
+  if (!text || (int64_t)total > cap) return DISO_OK;  // the size only
+  if (lines > 0) obj_write_kernel<S><<<mesh_ctas(ex, lines), 256, 0, s>>>(v, nrm, nv, faces, nf, k, off, text);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+template <class S>
+int mesh_ply(diso_extractor* ex, const S* v, const S* nrm, int64_t nv, const int64_t* faces, int64_t nf, int k,
+             uint8_t* body, cudaStream_t s) {
+  const int64_t vbytes = nv * 3 * (int64_t)sizeof(S) * (nrm ? 2 : 1);
+  if (nrm) {
+    if (nv > 0) ply_vertex_kernel<S><<<mesh_ctas(ex, nv), 256, 0, s>>>(v, nrm, nv, (S*)body);
+  } else if (vbytes > 0) {
+    CUDA_TRY(cudaMemcpyAsync(body, v, (size_t)vbytes, cudaMemcpyDeviceToDevice, s));
+  }
+  if (nf > 0) ply_face_kernel<<<mesh_ctas(ex, nf), 256, 0, s>>>(faces, nf, k, body + vbytes);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+// common checks of the mesh entry points
+int mesh_args(diso_extractor* ex, const void* verts, int64_t nv, const int64_t* faces, int64_t nf, int k) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (k != 3 && k != 4) return fail(DISO_ERR_ARG, "faces must have 3 or 4 corners (got %d)", k);
+  if (nv < 0 || nf < 0) return fail(DISO_ERR_ARG, "negative vertex or face count");
+  if (nv >= (1ll << 31)) return fail(DISO_ERR_ARG, "too many vertices for 32-bit indices: %lld", (long long)nv);
+  if ((nv && !verts) || (nf && !faces)) return fail(DISO_ERR_ARG, "null vertices or faces");
+  return bind_device(ex);
+}
+
 extern "C" {
 
 int diso_create(int method, int dtype, diso_extractor** out) {
@@ -1192,6 +1333,67 @@ int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n)
 const char* diso_last_error(void) { return g_err; }
 
 const char* diso_version(void) { return "diso_gb300 0.1.0 (sm_103a)"; }
+
+
+int diso_mesh_normals(diso_extractor* ex, const void* verts, int64_t n_verts, const int64_t* faces, int64_t n_faces,
+                      int corners, void* normals, void* stream) {
+  int rc = mesh_args(ex, verts, n_verts, faces, n_faces, corners);
+  if (rc) return rc;
+  if (n_verts && !normals) return fail(DISO_ERR_ARG, "null normals");
+  if (n_verts == 0) return DISO_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32
+             ? mesh_normals<float>(ex, (const float*)verts, n_verts, faces, n_faces, corners, (float*)normals, s)
+             : mesh_normals<double>(ex, (const double*)verts, n_verts, faces, n_faces, corners, (double*)normals, s);
+}
+
+int diso_mesh_weld(diso_extractor* ex, const void* verts, int64_t n_verts, const int64_t* faces, int64_t n_faces,
+                   int corners, double tol, void* out_verts, int64_t* out_faces, int64_t* n_verts_out,
+                   int64_t* n_faces_out, void* stream) {
+  int rc = mesh_args(ex, verts, n_verts, faces, n_faces, corners);
+  if (rc) return rc;
+  if (!n_verts_out || !n_faces_out) return fail(DISO_ERR_ARG, "null output counts");
+  if (!(tol >= 0.0)) return fail(DISO_ERR_ARG, "tolerance must be >= 0");
+  if ((n_verts && !out_verts) || (n_faces && !out_faces)) return fail(DISO_ERR_ARG, "null output vertices or faces");
+  *n_verts_out = *n_faces_out = 0;
+  if (n_verts == 0) return n_faces ? fail(DISO_ERR_ARG, "weld: faces without vertices") : DISO_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? mesh_weld<float>(ex, (const float*)verts, n_verts, faces, n_faces, corners, tol,
+                                                  (float*)out_verts, out_faces, n_verts_out, n_faces_out, s)
+                               : mesh_weld<double>(ex, (const double*)verts, n_verts, faces, n_faces, corners, tol,
+                                                   (double*)out_verts, out_faces, n_verts_out, n_faces_out, s);
+}
+
+int diso_mesh_obj(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
+                  int64_t n_faces, int corners, char* text, int64_t text_cap, int64_t* text_bytes, void* stream) {
+  int rc = mesh_args(ex, verts, n_verts, faces, n_faces, corners);
+  if (rc) return rc;
+  if (!text_bytes || text_cap < 0) return fail(DISO_ERR_ARG, "null text size or negative capacity");
+  *text_bytes = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? mesh_obj<float>(ex, (const float*)verts, (const float*)normals, n_verts, faces,
+                                                 n_faces, corners, text, text_cap, text_bytes, s)
+                               : mesh_obj<double>(ex, (const double*)verts, (const double*)normals, n_verts, faces,
+                                                  n_faces, corners, text, text_cap, text_bytes, s);
+}
+
+int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int corners, int with_normals) {
+  if ((dtype != DISO_F32 && dtype != DISO_F64) || (corners != 3 && corners != 4) || n_verts < 0 || n_faces < 0)
+    return -1;
+  return n_verts * 3 * (dtype == DISO_F32 ? 4 : 8) * (with_normals ? 2 : 1) + n_faces * (1 + 4 * corners);
+}
+
+int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
+                  int64_t n_faces, int corners, void* body, void* stream) {
+  int rc = mesh_args(ex, verts, n_verts, faces, n_faces, corners);
+  if (rc) return rc;
+  if (!body && (n_verts || n_faces)) return fail(DISO_ERR_ARG, "null body buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  return ex->dtype == DISO_F32 ? mesh_ply<float>(ex, (const float*)verts, (const float*)normals, n_verts, faces,
+                                                 n_faces, corners, (uint8_t*)body, s)
+                               : mesh_ply<double>(ex, (const double*)verts, (const double*)normals, n_verts, faces,
+                                                  n_faces, corners, (uint8_t*)body, s);
+}
 
 }  // extern "C"
 

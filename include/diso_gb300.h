@@ -243,6 +243,52 @@ int diso_timing(diso_extractor* ex, int enable);
  * end events), at most `max` entries, *n = entries written; then starts over. */
 int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n);
 
+/* ---- Mesh consumers on the device ----
+ * For the meshes the extractor returns: vertices [n_verts][3] in the extractor's
+ * dtype, faces [n_faces][corners] int64 (corners 3 or 4).  Each call runs on
+ * `stream` and synchronises it at the end; a face index outside [0, n_verts) is
+ * DISO_ERR_ARG.  The reference writes its meshes through trimesh on the host
+ * (test/example.py:71-73, trimesh.Trimesh(...).export to OBJ); these replace that
+ * step for meshes in device memory.  The extractor only supplies the dtype and
+ * grow-only scratch. */
+
+/* Area-weighted vertex normals: per vertex the sum of the normals of its faces
+ * (triangles (p1-p0) x (p2-p0), quads (p2-p0) x (p3-p1), i.e. twice the vector
+ * area, in double), normalised; [0, 0, 0] for a vertex without area.  The sums are
+ * exact 64-bit fixed point (2^50 over the largest face normal component), so the
+ * result does not depend on the order of the GPU's atomics.  normals: [n_verts][3]. */
+int diso_mesh_normals(diso_extractor* ex, const void* verts, int64_t n_verts, const int64_t* faces, int64_t n_faces,
+                      int corners, void* normals, void* stream);
+
+/* Weld: vertices with equal positions (tol = 0: equal coordinates, -0 = +0;
+ * tol > 0: equal floor(x / tol + 0.5) per coordinate) become one, the lowest index
+ * of each group; kept vertices and faces keep their order, faces whose corners are
+ * no longer distinct are dropped.  out_verts holds up to n_verts rows, out_faces up to
+ * n_faces; *n_verts_out / *n_faces_out receive the counts. */
+int diso_mesh_weld(diso_extractor* ex, const void* verts, int64_t n_verts, const int64_t* faces, int64_t n_faces,
+                   int corners, double tol, void* out_verts, int64_t* out_faces, int64_t* n_verts_out,
+                   int64_t* n_faces_out, void* stream);
+
+/* OBJ text into a device buffer: "v x y z" lines with every coordinate as "%.8f"
+ * (correctly rounded, ties to even; nan / inf / -inf spelled so), then, when normals
+ * is not NULL, "vn" lines, then "f a b c[ d]" lines with 1-based indices ("a//a"
+ * with normals); every line ends in "\n".  *text_bytes receives the length; the text
+ * is written only when text is not NULL and the length fits text_cap (call with
+ * text = NULL for the size).  Coordinates must have |x| < 1.8e11. */
+int diso_mesh_obj(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
+                  int64_t n_faces, int corners, char* text, int64_t text_cap, int64_t* text_bytes, void* stream);
+
+/* Bytes of a binary little-endian PLY body (-1 for bad arguments): the vertex block
+ * (x y z, then nx ny nz when with_normals, in the dtype) and the face block (one
+ * byte count, then `corners` int32 indices per face). */
+int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int corners, int with_normals);
+
+/* The PLY body into a device buffer of diso_mesh_ply_bytes bytes; the header
+ * ("ply", "format binary_little_endian 1.0", the element and property lines,
+ * "end_header") is the caller's. */
+int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
+                  int64_t n_faces, int corners, void* body, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* diso_last_error(void);
 
