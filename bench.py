@@ -188,6 +188,75 @@ def run_batched(device, method, steps=10, warmup=3, ngrids=64):
             "ms_loop": ms_loop, "ms_graph": ms_graph}
 
 
+def run_mesh(device, n=512, steps=5, warmup=2, cpu_sample=100000):
+    """The mesh consumers on the benchmark's DMC mesh (quads): device times of vertex
+    normals, weld, OBJ text and PLY body (CUDA events), the files written through the
+    public calls (host wall time: device work, copy to pinned memory, file write), and
+    the CPU oracle on a sample of the mesh, scaled to the whole."""
+    import tempfile
+
+    from diso_gb300 import DiffDMC, mesh
+
+    sdf = spheres_field(n, device)
+    deform = deform_field(n, device)
+    with torch.no_grad():
+        v, f = DiffDMC(torch.float32)(sdf, deform, return_quads=True)
+    del sdf, deform
+    nv, nf = v.shape[0], f.shape[0]
+    nrm = mesh.vertex_normals(v, f)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, out
+
+    res = {"mesh": f"DMC quads of the {n}^3 benchmark grid", "verts": nv, "quads": nf}
+    ms, _ = timed(lambda: mesh.vertex_normals(v, f))
+    # faces twice (max pass, sum pass) with their corners' vertices, 24 B of sums per
+    # corner (read + write), normals out
+    by = 2 * nf * (4 * 8 + 4 * 12) + nf * 4 * 24 + nv * 12
+    res["normals_ms"] = ms
+    res["normals_gbs"] = by / (ms * 1e-3) / 1e9
+    ms, (wv, wf) = timed(lambda: mesh.weld(v, f))
+    res["weld_ms"], res["weld_verts"], res["weld_quads"] = ms, wv.shape[0], wf.shape[0]
+    ms, text = timed(lambda: mesh.obj_text(v, f, nrm))
+    res["obj_ms"], res["obj_bytes"] = ms, text.numel()
+    res["obj_gbs"] = text.numel() / (ms * 1e-3) / 1e9
+    ms, body = timed(lambda: mesh.ply_body(v, f, nrm))
+    res["ply_ms"], res["ply_bytes"] = ms, body.numel()
+    del text, body
+    with tempfile.TemporaryDirectory() as tmp:
+        for kind, fn in (("obj", mesh.write_obj), ("ply", mesh.write_ply)):
+            path = os.path.join(tmp, "mesh." + kind)
+            fn(path, v, f, nrm)
+            t0 = time.perf_counter()
+            fn(path, v, f, nrm)
+            res[f"write_{kind}_ms"] = (time.perf_counter() - t0) * 1e3
+    # the CPU oracle (numpy normals, Python OBJ formatting) on the first cpu_sample
+    # vertices and the faces among them, scaled by the vertex count
+    from oracle import mesh as M
+
+    k = min(cpu_sample, nv)
+    hv, hf = v[:k].cpu().numpy(), f.cpu().numpy()
+    hf = hf[(hf < k).all(axis=1)]
+    hn = M.vertex_normals(hv, hf)
+    t0 = time.perf_counter()
+    M.vertex_normals(hv, hf)
+    t1 = time.perf_counter()
+    M.obj_text(hv, hf, hn)
+    t2 = time.perf_counter()
+    res["cpu_baseline"] = {"normals_ms": (t1 - t0) * 1e3 * nv / k, "obj_ms": (t2 - t1) * 1e3 * nv / k, "cores": 1,
+                           "kind": "port", "sample": f"first {k} vertices and their {hf.shape[0]} quads, scaled"}
+    return res
+
+
 def run_served(device, nreq=2000, rate=2000.0):
     """p50 / p99 latency and grids/s of the continuous-batching server against the
     plain per-request call on the same arrival trace."""
@@ -554,7 +623,8 @@ def main():
     res = run_ours(args, rank, world, device)
     if rank == 0 and world == 1 and not args.no_batched:
         for name, fn in (("batched_mc", lambda: run_batched(device, 0)), ("batched_dmc", lambda: run_batched(device, 1)),
-                         ("served", lambda: run_served(device, args.requests))):
+                         ("served", lambda: run_served(device, args.requests)),
+                         ("mesh_consumers", lambda: run_mesh(device, args.n))):
             try:
                 res[name] = fn()
             except Exception as e:  # report, but keep the headline line
