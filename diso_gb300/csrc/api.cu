@@ -227,11 +227,11 @@ EncodeTiledFn encode_tiled() {
   return fn;
 }
 
-// Tensor maps of the SDF for the TMA count: full boxes (32 x 33 x 9 points, z
-// innermost) and the 4-deep boxes below / above a unit.  False when the SDF cannot
-// be described (address not 16-byte aligned, rows not a multiple of 16 bytes).
+// The tensor map of the SDF for the TMA count: boxes of 32 x 33 x 9 points (z
+// innermost).  False when the SDF cannot be described (address not 16-byte aligned,
+// rows not a multiple of 16 bytes).
 template <class S>
-bool count_tensor_maps(const void* sdf, int nx, int ny, int nz, CUtensorMap* wide, CUtensorMap* narrow) {
+bool count_tensor_map(const void* sdf, int nx, int ny, int nz, CUtensorMap* wide) {
   if (((uintptr_t)sdf & 15u) != 0 || ((int64_t)nz * (int64_t)sizeof(S)) % 16 != 0) return false;
   EncodeTiledFn enc = encode_tiled();
   if (!enc) return false;
@@ -240,12 +240,7 @@ bool count_tensor_maps(const void* sdf, int nx, int ny, int nz, CUtensorMap* wid
   const cuuint64_t strides[2] = {(cuuint64_t)nz * sizeof(S), (cuuint64_t)nz * ny * sizeof(S)};
   const cuuint32_t estr[3] = {1, 1, 1};
   const cuuint32_t wbox[3] = {32, (cuuint32_t)(CR + 1), (cuuint32_t)(CP + 1)};
-  const cuuint32_t nbox[3] = {(cuuint32_t)TBN, (cuuint32_t)(CR + 1), (cuuint32_t)(CP + 1)};
-  if (enc(wide, dt, 3, const_cast<void*>(sdf), dims, strides, wbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
-      CUDA_SUCCESS)
-    return false;
-  return enc(narrow, dt, 3, const_cast<void*>(sdf), dims, strides, nbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  return enc(wide, dt, 3, const_cast<void*>(sdf), dims, strides, wbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -398,8 +393,8 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
-  CUtensorMap wide, narrow;
-  const bool tma = count_tensor_maps<S>(sdf, nx, ny, nz, &wide, &narrow);
+  CUtensorMap wide;
+  const bool tma = count_tensor_map<S>(sdf, nx, ny, nz, &wide);
   if (tma) {
     const int64_t units = count_tma_units(g);
     const int64_t want =
@@ -410,10 +405,10 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
     if ((rc = take_zero_job(ex, g, units, grid, s, &zj)) != DISO_OK) return rc;
     KernelTimer kt(ex, K_COUNT, s);
     if (ex->method == DISO_MC)
-      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
+      count_tma_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(wide, f, g, seg, tile_flags(seg, g), codes,
                                                            ex->stats, ex->active, zj);
     else
-      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, narrow, f, g, seg, tile_flags(seg, g), codes,
+      count_tma_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(wide, f, g, seg, tile_flags(seg, g), codes,
                                                             ex->stats, ex->active, zj);
   } else {
     ex->zemit_set = false;
@@ -681,11 +676,11 @@ int take_zero_job(diso_extractor* ex, const Geom& g, int64_t units, unsigned gri
   ex->zemit_set = split < n;
   zj->begin = 0;
   zj->end = split;
-  // the fewest boxes a CTA gets is its whole units times the boxes of the shortest
-  // unit (its chunks and the two 4-deep boxes)
+  // the fewest boxes a CTA gets is its whole units times the boxes (chunks) of the
+  // shortest unit
   const int64_t nbz = (g.nzc + KZT - 1) / KZT, kz = (g.nzc + nbz - 1) / nbz;
   const int64_t kz_min = g.nzc - (nbz - 1) * kz;
-  zero_rate(zj, grid, std::max<int64_t>(1, (units / grid) * (kz_min + 2)));
+  zero_rate(zj, grid, std::max<int64_t>(1, (units / grid) * kz_min));
   return DISO_OK;
 }
 

@@ -550,8 +550,8 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Fi
 // vrows: bit i = the warp's point row i lies in the grid (used rows only)
 // (written masks only) bit 0: one of them is not all ones, bit 1: one is not all zeros
 template <class S, int METHOD>
-__device__ __forceinline__ uint32_t count_combine(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
-                                                  uint32_t (&p2)[2]) {
+__device__ __forceinline__ uint32_t count_combine_cur(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
+                                                      uint32_t (&p2)[2], const uint32_t (&curk)[2]) {
   constexpr uint64_t ALL = (1ull << (MASK_TOP + 1)) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t mixed = 0;
@@ -559,7 +559,7 @@ __device__ __forceinline__ uint32_t count_combine(CountShared<S, METHOD>& sh, bo
   for (int k = 0; k < 2; ++k) {
     const int i = lane + 32 * k, r = warp + 8 * i;
     if (i < CRPW && r < CROWS) {
-      const uint32_t cur = sh.bal[r];
+      const uint32_t cur = curk[k];
       if (write) {
         const uint64_t m = (uint64_t)(p2[k] >> 30) | ((uint64_t)p1[k] << 2) | ((uint64_t)(cur & 1u) << 34);
         (&sh.m[0][0])[r] = m;
@@ -570,6 +570,37 @@ __device__ __forceinline__ uint32_t count_combine(CountShared<S, METHOD>& sh, bo
     }
   }
   return mixed;
+}
+
+template <class S, int METHOD>
+__device__ __forceinline__ uint32_t count_combine(CountShared<S, METHOD>& sh, bool write, uint32_t (&p1)[2],
+                                                  uint32_t (&p2)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t cur[2] = {0u, 0u};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int i = lane + 32 * k, r = warp + 8 * i;
+    if (i < CRPW && r < CROWS) cur[k] = sh.bal[r];
+  }
+  return count_combine_cur<S, METHOD>(sh, write, p1, p2, cur);
+}
+
+// bits (value >= iso) of the points at unpadded z0 .. z0 + cnt - 1 of the lane's
+// point rows (i = lane, lane + 32 of this warp; rows from padded (X0, Y0)), each at
+// bit z mod 32 as in that chunk's ballot; the pad value outside the grid
+template <class S>
+__device__ __forceinline__ void point_bits(const Field<S>& f, int X0, int Y0, int z0, int cnt, uint32_t (&out)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int i = lane + 32 * k, r = warp + 8 * i;
+    uint32_t b = 0;
+    if (i < CRPW && r < CROWS) {
+      const int X = X0 + r / (CR + 1), Y = Y0 + r % (CR + 1);
+      for (int c = 0; c < cnt; ++c) b |= (f.at(X, Y, z0 + c + 1) >= f.iso ? 1u : 0u) << ((z0 + c) & 31);
+    }
+    out[k] = b;
+  }
 }
 
 // A chunk whose masks are all ones or all zeros has no non-trivial cell: its
@@ -669,13 +700,15 @@ __global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, 
 
 // The count pass with the SDF brought into shared memory by the TMA unit: for every
 // chunk of a unit one bulk tensor copy of the box of 9 x 33 point rows x 32 points
-// (out-of-grid points arrive as zeros and are replaced by the pad value), the chunks
-// below and above a unit as boxes 4 points deep.  A ring of TMA_STAGES boxes per CTA
-// keeps copies in flight while the warps turn the previous box into ballots; the
-// counting itself is count_chunk.  Needs a 16-byte aligned SDF whose rows are a
-// multiple of 16 bytes (the tensor map's strides); otherwise count_kernel runs.
+// (out-of-grid points arrive as zeros and are replaced by the pad value).  The three
+// points of each row that a unit's masks take from the chunks below and above it
+// (two below its first chunk, one above its last) are plain loads by the lanes that
+// keep those rows' ballot history, so every pipeline step is a full box.  A ring of
+// TMA_STAGES boxes per CTA keeps copies in flight while the warps turn the previous
+// box into ballots; the counting itself is count_chunk.  Needs a 16-byte aligned SDF
+// whose rows are a multiple of 16 bytes (the tensor map's strides); otherwise
+// count_kernel runs.
 constexpr int KZT = 8;                        // chunks per unit (at most)
-constexpr int TBN = 4;                        // depth of the boxes below / above a unit
 constexpr int TMA_STAGES = 2;
 constexpr int TMA_TILES_PER_UNIT = (CP / TX) * (CR / TY) * KZT;
 constexpr long long TMA_WAIT_CYCLES = 1ll << 32;  // about two seconds
@@ -683,10 +716,6 @@ constexpr long long TMA_WAIT_CYCLES = 1ll << 32;  // about two seconds
 template <class S>
 __host__ __device__ constexpr int tma_box_bytes() {
   return CROWS * 32 * (int)sizeof(S);
-}
-template <class S>
-__host__ __device__ constexpr int tma_narrow_bytes() {
-  return CROWS * TBN * (int)sizeof(S);
 }
 // dynamic shared memory of count_tma_kernel: the stages, plus room to align them to 128 bytes
 template <class S>
@@ -699,7 +728,7 @@ __host__ __device__ inline int64_t count_tma_units(const Geom& g) {
 }
 
 // a position in a CTA's stream of boxes: the unit (rows from (X0, Y0), chunks
-// [tz0, tz1)) and the box's chunk t in [tz0 - 1, tz1]
+// [tz0, tz1)) and the box's chunk t in [tz0, tz1)
 struct BoxCursor {
   int64_t unit;
   int X0, Y0, tz0, tz1, t;
@@ -711,17 +740,15 @@ struct BoxCursor {
     X0 = (int)(col / nby) * CP;
     Y0 = (int)(col % nby) * CR;
     tz1 = min(tz0 + kz, g.nzc);
-    t = tz0 - 1;
+    t = tz0;
   }
   __device__ void next(const Geom& g, int64_t nunits) {
-    if (++t > tz1) {
+    if (++t >= tz1) {
       unit += gridDim.x;
       if (unit < nunits) start(g, unit);
     }
   }
   __device__ bool valid(int64_t nunits) const { return unit < nunits; }
-  // 0: a full chunk; 1: the 4 points below the unit (lanes 28..31); 2: the 4 above (lanes 0..3)
-  __device__ int kind() const { return t == tz0 - 1 ? 1 : (t == tz1 ? 2 : 0); }
 };
 
 // Zeros written beside a forward's kernels (the gradient buffers of a forward whose
@@ -775,28 +802,20 @@ __device__ __forceinline__ void zero_finish(const ZeroJob& z, const void* zbuf, 
 }
 
 template <class S>
-__device__ __forceinline__ void issue_box(const CUtensorMap* wide, const CUtensorMap* narrow, void* dst,
-                                          uint64_t* bar, const BoxCursor& c) {
-  const int k = c.kind();
-  if (k == 0) {
-    mbar_expect_tx(bar, (uint32_t)tma_box_bytes<S>());
-    tma_load_3d(dst, wide, bar, 32 * c.t, c.Y0 - 1, c.X0 - 1);
-  } else {
-    mbar_expect_tx(bar, (uint32_t)tma_narrow_bytes<S>());
-    tma_load_3d(dst, narrow, bar, 32 * c.t + (k == 1 ? 32 - TBN : 0), c.Y0 - 1, c.X0 - 1);
-  }
+__device__ __forceinline__ void issue_box(const CUtensorMap* wide, void* dst, uint64_t* bar, const BoxCursor& c) {
+  mbar_expect_tx(bar, (uint32_t)tma_box_bytes<S>());
+  tma_load_3d(dst, wide, bar, 32 * c.t, c.Y0 - 1, c.X0 - 1);
 }
 
-// ballots of chunk t from a box in shared memory (row r at box + r * width); the
-// 4-deep boxes contribute bits only (their points are counted by the unit that owns
-// their chunk), full boxes also the min / max
+// ballots of chunk t from its box in shared memory (row r at box + 32 r), and the
+// min / max of the values in the grid
 template <class S, int METHOD>
 __device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Field<S>& f, const S* box, int t,
-                                            int kind, uint64_t vrows, S& mn, S& mx) {
+                                            uint64_t vrows, S& mn, S& mx) {
   constexpr int NB = 4, HALF = (CRPW + NB - 1) / NB;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint64_t used = warp + 8 * (CRPW - 1) < CROWS ? (1ull << CRPW) - 1 : (1ull << (CRPW - 1)) - 1;
-  if (kind == 0 && vrows == used && t >= 0 && 32 * t + 32 <= f.n2) {
+  if (vrows == used && 32 * t + 32 <= f.n2) {
     // every point of the warp's rows lies in the grid: one load, compare and ballot per row
     const S* p = box + warp * 32 + lane;
 #pragma unroll
@@ -811,10 +830,7 @@ __device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Fi
     __syncwarp();
     return;
   }
-  const int l0 = kind == 1 ? 32 - TBN : 0, width = kind == 0 ? 32 : TBN;
-  const int e = lane - l0;
-  const bool zin = (unsigned)e < (unsigned)width && (unsigned)(32 * t + lane) < (unsigned)f.n2;
-  const bool track = kind == 0;
+  const bool zin = 32 * t + lane < f.n2;
 #pragma unroll
   for (int h = 0; h < NB; ++h) {
     S v[HALF];
@@ -823,7 +839,7 @@ __device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Fi
     for (int k = 0; k < HALF; ++k) {
       const int i = h * HALF + k, r = warp + 8 * i;
       in[k] = zin && i < CRPW && ((vrows >> i) & 1ull);
-      const S b = box[in[k] ? r * width + e : 0];  // every read stays inside the box
+      const S b = box[in[k] ? r * 32 + lane : 0];  // every read stays inside the box
       v[k] = in[k] ? b : f.pad;
     }
 #pragma unroll
@@ -833,7 +849,7 @@ __device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Fi
         const uint32_t b = __ballot_sync(0xffffffffu, v[k] >= f.iso);
         if (lane == 0) sh.bal[r] = b;
       }
-      if (track && in[k]) {
+      if (in[k]) {
         mn = smin(mn, v[k]);
         mx = smax(mx, v[k]);
       }
@@ -844,7 +860,6 @@ __device__ __forceinline__ void box_ballots(CountShared<S, METHOD>& sh, const Fi
 
 template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_constant__ CUtensorMap wide,
-                                                                const __grid_constant__ CUtensorMap narrow,
                                                                 Field<S> f, Geom g, uint64_t* __restrict__ seg,
                                                                 uint8_t* __restrict__ tile_flag,
                                                                 CellRec* __restrict__ codes, Stats* stats,
@@ -874,7 +889,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   int64_t issued = 0;
   if (threadIdx.x == 0) {
     for (int st = 0; st < TMA_STAGES && pc.valid(nunits); ++st, ++issued) {
-      issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
+      issue_box<S>(&wide, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
       pc.next(g, nunits);
     }
   }
@@ -885,8 +900,9 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   int64_t k = 0;
   for (; cc.valid(nunits); ++k) {
     const int st = (int)(k % TMA_STAGES);
-    if (cc.t == cc.tz0 - 1) {
-      // a new unit: which of the warp's point rows lie in the grid
+    if (cc.t == cc.tz0) {
+      // a new unit: which of the warp's point rows lie in the grid, and the ballot
+      // history of the lane's rows: the two points below the unit's first chunk
       vrows = 0;
 #pragma unroll
       for (int i = 0; i < CRPW; ++i) {
@@ -894,11 +910,16 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
         const int X = cc.X0 + r / (CR + 1), Y = cc.Y0 + r % (CR + 1);
         if (r < CROWS && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1) vrows |= 1ull << i;
       }
+      point_bits<S>(f, cc.X0, cc.Y0, 32 * cc.tz0 - 2, 2, p1);
+      p2[0] = p2[1] = 0u;
     }
+    // at the unit's last chunk, the point above it (read before the wait)
+    uint32_t above[2] = {0u, 0u};
+    if (cc.t == cc.tz1 - 1) point_bits<S>(f, cc.X0, cc.Y0, 32 * cc.tz1, 1, above);
     if (warp == 1) zero_round(zj, zbuf, k, lane);
     const bool ok = mbar_wait_bounded(&full[st], (uint32_t)((k / TMA_STAGES) & 1), TMA_WAIT_CYCLES);
-    box_ballots<S, METHOD>(sh, f, reinterpret_cast<const S*>(stage_mem + st * tma_box_bytes<S>()), cc.t, cc.kind(),
-                           vrows, mn, mx);
+    box_ballots<S, METHOD>(sh, f, reinterpret_cast<const S*>(stage_mem + st * tma_box_bytes<S>()), cc.t, vrows, mn,
+                           mx);
     const uint32_t mixed = count_combine<S, METHOD>(sh, cc.t >= cc.tz0 + 1, p1, p2);
     // slots rotate over the CTA's boxes: slot (k+2)%3 was last read before the
     // previous barrier and is next written after the next one
@@ -914,7 +935,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
       sh.mixed[(k + 2) % 3] = 0;
       if (pc.valid(nunits)) {
         fence_proxy_async();
-        issue_box<S>(&wide, &narrow, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
+        issue_box<S>(&wide, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
         pc.next(g, nunits);
         ++issued;
       }
@@ -924,6 +945,17 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
         count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, cc.X0, cc.Y0, cc.t - 1, 0);
       else
         count_chunk_empty<S, METHOD>(g, seg, tile_flag, cc.X0, cc.Y0, cc.t - 1);
+    }
+    if (cc.t == cc.tz1 - 1) {
+      // the unit's last chunk, its masks completed by the points above it
+      __syncthreads();  // the chunk just counted is done with sh.m and sh.act
+      const uint32_t m = count_combine_cur<S, METHOD>(sh, true, p1, p2, above);
+      // a mask with a zero bit and a mask with a one bit: the chunk has crossings
+      const bool some0 = __syncthreads_or(m & 1u), some1 = __syncthreads_or(m & 2u);
+      if (some0 && some1)
+        count_chunk<S, METHOD>(sh, f, g, seg, tile_flag, codes, cc.X0, cc.Y0, cc.t, 0);
+      else
+        count_chunk_empty<S, METHOD>(g, seg, tile_flag, cc.X0, cc.Y0, cc.t);
     }
     cc.next(g, nunits);
   }
