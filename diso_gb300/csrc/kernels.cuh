@@ -1318,26 +1318,42 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     }
   }
   __syncthreads();
-  // records of the window, one warp per row; the edge rows' crossing bits from them
-  for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
-    const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
-    const uint32_t act = sact[wx][wy];
-    const int c = (act & 2) ? codes[g.code(X, Y, Z0 + lane)] : 0;
-    cw[wx][wy][lane + 1] = (CellRec)c;
-    int e = 0;
-    if (lane == 0 && (act & 1)) e = codes[g.code(X, Y, Z0 - 1)];
-    if (lane == 31 && (act & 4)) e = codes[g.code(X, Y, Z0 + TZ)];
-    if (lane == 0) cw[wx][wy][0] = (CellRec)e;
-    if (lane == 31) cw[wx][wy][TZ + 1] = (CellRec)e;
-    if (wx >= 1 && wy >= 1) {
-      const int code = c & 0xff, cf = cross_flags(code);
-      RowBits w;
-      w.xc = __ballot_sync(0xffffffffu, cf & 1);
-      w.yc = __ballot_sync(0xffffffffu, cf & 2);
-      w.zc = __ballot_sync(0xffffffffu, cf & 4);
-      w.nt = __ballot_sync(0xffffffffu, code != 0 && code != 255);
-      if (lane == 0) wb[wx - 1][wy - 1] = w;
-      if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e & 0xff);
+  // records of the window, one warp per row (the records of RB rows in flight
+  // together); the edge rows' crossing bits from them
+  constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32), RB = 4;
+#pragma unroll 1
+  for (int i0 = 0; i0 < RPW; i0 += RB) {
+    int c[RB], e[RB];
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+      const int r = warp + (NTHREADS / 32) * (i0 + k);
+      c[k] = e[k] = 0;
+      if (r < KX * KY) {
+        const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+        const uint32_t act = sact[wx][wy];
+        if (act & 2) c[k] = codes[g.code(X, Y, Z0 + lane)];
+        if (lane == 0 && (act & 1)) e[k] = codes[g.code(X, Y, Z0 - 1)];
+        if (lane == 31 && (act & 4)) e[k] = codes[g.code(X, Y, Z0 + TZ)];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RB; ++k) {
+      const int r = warp + (NTHREADS / 32) * (i0 + k);
+      if (r >= KX * KY) break;
+      const int wx = r / KY, wy = r % KY;
+      cw[wx][wy][lane + 1] = (CellRec)c[k];
+      if (lane == 0) cw[wx][wy][0] = (CellRec)e[k];
+      if (lane == 31) cw[wx][wy][TZ + 1] = (CellRec)e[k];
+      if (wx >= 1 && wy >= 1) {
+        const int code = c[k] & 0xff, cf = cross_flags(code);
+        RowBits w;
+        w.xc = __ballot_sync(0xffffffffu, cf & 1);
+        w.yc = __ballot_sync(0xffffffffu, cf & 2);
+        w.zc = __ballot_sync(0xffffffffu, cf & 4);
+        w.nt = __ballot_sync(0xffffffffu, code != 0 && code != 255);
+        if (lane == 0) wb[wx - 1][wy - 1] = w;
+        if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e[k] & 0xff);
+      }
     }
   }
   __syncthreads();
