@@ -320,8 +320,8 @@ int reset_stats(diso_extractor* ex, cudaStream_t s) {
   return DISO_OK;
 }
 
-// exclusive look-back scan of a[0..n) in place, a[n] = total
-int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s) {
+// look-back state for a scan of n elements; returns its tiles (0 on failure)
+int64_t scan_reserve(diso_extractor* ex, int64_t n) {
   const int64_t tiles = (n + 1 + SCAN_TILE - 1) / SCAN_TILE;
   if (tiles > ex->scan_cap) {
     cudaFree(ex->scan_flag);
@@ -331,17 +331,31 @@ int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s) {
     ex->scan_agg = ex->scan_incl = nullptr;
     ex->scan_cap = 0;
     const int64_t cap = tiles + tiles / 4 + 64;
-    CUDA_TRY(cudaMalloc((void**)&ex->scan_flag, (size_t)cap * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc((void**)&ex->scan_agg, (size_t)cap * sizeof(uint64_t)));
-    CUDA_TRY(cudaMalloc((void**)&ex->scan_incl, (size_t)cap * sizeof(uint64_t)));
+    if (cudaMalloc((void**)&ex->scan_flag, (size_t)cap * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&ex->scan_agg, (size_t)cap * sizeof(uint64_t)) != cudaSuccess ||
+        cudaMalloc((void**)&ex->scan_incl, (size_t)cap * sizeof(uint64_t)) != cudaSuccess) {
+      fail(DISO_ERR_CUDA, "scan state allocation of %lld tiles failed", (long long)cap);
+      return 0;
+    }
     ex->scan_cap = cap;
   }
-  CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
-  CUDA_TRY(cudaMemsetAsync(&ex->stats->scan_tile, 0, sizeof(unsigned long long), s));
+  return tiles;
+}
+
+// exclusive look-back scan of a[0..n) in place, a[n] = total (also into *total_out
+// when given).  `prepared`: its flags and tile counter were zeroed by count_prep_kernel.
+int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s, bool prepared = false,
+             uint64_t* total_out = nullptr) {
+  const int64_t tiles = scan_reserve(ex, n);
+  if (tiles == 0) return DISO_ERR_CUDA;
+  if (!prepared) {
+    CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
+    CUDA_TRY(cudaMemsetAsync(&ex->stats->scan_tile, 0, sizeof(unsigned long long), s));
+  }
   ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
   {
     KernelTimer kt(ex, K_SCAN, s);
-    scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats);
+    scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats, total_out);
   }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
@@ -389,7 +403,11 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   int rc;
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
   if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
-  if ((rc = reset_stats(ex, s)) != DISO_OK) return rc;
+  // status words and the scan's look-back flags in one launch
+  const int64_t scan_tiles = scan_reserve(ex, g.nseg);
+  if (scan_tiles == 0) return DISO_ERR_CUDA;
+  count_prep_kernel<<<1, 256, 0, s>>>(ex->stats, ex->scan_flag, scan_tiles);
+  CUDA_TRY(cudaGetLastError());
   CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
@@ -424,15 +442,16 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
       count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
   }
   CUDA_TRY(cudaGetLastError());
-  return run_scan(ex, seg, g.nseg, s);
+  return run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->pad[0]));
 }
 
-// the count's results to the host (into the pinned stats mirror; its pad[0] takes the
-// scanned total), then an event
+// the count's results to the host (into the pinned stats mirror; its pad[0] holds
+// the scanned total), then an event
 template <class S>
 int count_copy(diso_extractor* ex, const Geom& g, const uint64_t* seg, cudaStream_t s) {
+  (void)g;
+  (void)seg;
   CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaMemcpyAsync(&ex->stats_host->pad[0], seg + g.nseg, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaEventRecord(ex->ev_counts, s));
   return DISO_OK;
 }
@@ -865,7 +884,7 @@ int batch_count(diso_extractor* ex, cudaStream_t s) {
   const int64_t tiles = (ex->bseg_total + 1 + SCAN_TILE - 1) / SCAN_TILE;
   CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
   ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
-  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(ex->brecord, ex->bseg_total, st, ex->stats);
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(ex->brecord, ex->bseg_total, st, ex->stats, nullptr);
   CUDA_TRY(cudaGetLastError());
   const int64_t* doffs = (const int64_t*)((char*)ex->bbound + sizeof(uint64_t) * (MAX_BATCH + 1));
   gather_bounds_kernel<<<1, 256, 0, s>>>(ex->brecord, doffs, n, ex->bbound);
@@ -1461,7 +1480,7 @@ int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sd
   const int64_t tiles = (g.nseg + 1 + SCAN_TILE - 1) / SCAN_TILE;
   CUDA_TRY(cudaMemsetAsync(sc->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
   ScanState st{sc->scan_flag, sc->scan_agg, sc->scan_incl};
-  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(seg, g.nseg, st, &sc->stats);
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(seg, g.nseg, st, &sc->stats, nullptr);
   CUDA_TRY(cudaGetLastError());
   Stats h;
   uint64_t total = 0;

@@ -35,8 +35,10 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// total_out (may be null) also receives the total a[n]
 __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* __restrict__ a, int64_t n,
-                                                                     ScanState st, Stats* stats) {
+                                                                     ScanState st, Stats* stats,
+                                                                     uint64_t* total_out) {
   __shared__ uint64_t warp_tot[SCAN_THREADS / 32];
   __shared__ uint64_t tile_excl;
   __shared__ int64_t tile_id_s;
@@ -145,9 +147,22 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* _
     for (int i = 0; i < SCAN_ITEMS; ++i) {
       const int64_t k = base + i;
       if (k <= n) a[k] = run;
+      if (k == n && total_out) *total_out = run;
       run += v[i];
     }
   }
+}
+
+// the status words of a forward (min key at its maximum, everything else zero) and
+// the look-back flags of its segment scan, in one launch
+__global__ void __launch_bounds__(256) count_prep_kernel(Stats* stats, uint32_t* __restrict__ scan_flag,
+                                                         int64_t tiles) {
+  if (threadIdx.x == 0) {
+    Stats z = {};
+    z.min_key = ~0ull;
+    *stats = z;
+  }
+  for (int64_t i = threadIdx.x; i < tiles; i += blockDim.x) scan_flag[i] = 0u;
 }
 
 }  // namespace diso
