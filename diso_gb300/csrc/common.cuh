@@ -96,7 +96,6 @@ struct Field {
 
 __device__ const uint64_t g_mc_tri[256] = DISO_MC_TRIANGLES;
 __device__ const uint64_t g_dmc_case[256] = DISO_DMC_CASES;
-__device__ const uint8_t g_edge[12] = DISO_EDGE_TABLE;
 __device__ const int g_dmc_quad[24] = DISO_DMC_QUADS;
 
 __device__ __forceinline__ uint64_t mc_tri(int code) { return __ldg(g_mc_tri + code); }
@@ -104,7 +103,6 @@ __device__ __forceinline__ uint64_t dmc_case(int code) { return __ldg(g_dmc_case
 __device__ __forceinline__ int dmc_dir(uint64_t w) { return (int)((w >> 28) & 7); }
 __device__ __forceinline__ int dmc_npatch(uint64_t w) { return (int)((w >> 24) & 7); }
 __device__ __forceinline__ int dmc_patch_of(uint64_t w, int e) { return (int)((w >> (2 * e)) & 3); }
-__device__ __forceinline__ int dmc_patch_size(uint64_t w, int p) { return (int)((w >> (32 + 4 * p)) & 15); }
 
 // MC case code (corner order of src/cumc.cu:107) from the Morton code: swap corners 2<->3, 6<->7
 __device__ __forceinline__ int mc_from_morton(int m) {
@@ -130,20 +128,8 @@ constexpr uint64_t pack_edges(int i) {
 constexpr uint64_t kEdgePack = detail::pack_edges(0);
 __device__ __forceinline__ int edge_desc(int e) { return (int)((kEdgePack >> (5 * e)) & 31); }
 
-// Bit (s + 8 a) set when the cell edge from corner s along axis a crosses (its two
-// corner bits in the Morton code differ); with desc = s | a << 3 the bit of edge e
-// is bit edge_desc(e).
-__device__ __forceinline__ uint32_t cross_bits(int m) {
-  return (uint32_t)(((m ^ (m >> 1)) & 0x55) | (((m ^ (m >> 2)) & 0x33) << 8) | (((m ^ (m >> 4)) & 0x0f) << 16));
-}
-
 // ----------------------------------------------------------------- reductions
 
-__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
-#pragma unroll
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 __device__ __forceinline__ uint64_t warp_sum64(uint64_t v) {
 #pragma unroll
   for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

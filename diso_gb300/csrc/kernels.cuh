@@ -2,14 +2,20 @@
 //
 //   count_kernel /    all tiles: per-segment crossing / face (MC) or crossing / patch
 //   count_tma_kernel  (DMC) counts, the min/max of the SDF for the empty-surface
-//                     guard, two activity bytes per tile and the list of active tiles
-//   scan              scan.cuh
+//                     guard, two activity bytes per tile, the list of active tiles,
+//                     the DMC cell records, and a share of the gradient zeros
+//   scan              scan.cuh (and the forward's reset kernel)
 //   mc_emit_kernel    active tiles: MC vertices and triangles (and the edge record)
-//   dmc_emit_kernel   active tiles: DMC dual vertices and quads (and the edge record)
+//   dmc_emit_kernel   active tiles: DMC dual vertices and quads (and the edge record),
+//                     the rest of the gradient zeros
 //   edge_adjoint_kernel  backward, every crossing edge: its adjoint at both ends
-//   zero_tiles_kernel /  backward, every point tile: dL/dsdf and dL/ddeform, written
-//   gather_list_kernel   once (zeros away from the surface, sums of edge adjoints near it)
+//   active_ptiles_kernel backward: the list of point tiles near the surface
+//   gather_list_kernel   backward, those point tiles: dL/dsdf and dL/ddeform as sums
+//                        of edge adjoints (the rest of the gradients are the zeros
+//                        of the forward, or zero_tiles_kernel's)
 //   split_*           DMC quad -> triangle split (return_quads=False)
+//   batch_*           the same phases over a batch of grids
+// Mesh consumers (normals, weld, OBJ, PLY) are in mesh.cuh.
 //
 // Row masks.  Every kernel first turns the SDF rows its tile needs into bit masks:
 // a warp reads 32 (+3) consecutive points of a row (X, Y) along z, coalesced, and
