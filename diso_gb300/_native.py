@@ -41,6 +41,16 @@ class Counts(ctypes.Structure):
     ]
 
 
+class SphereFieldDesc(ctypes.Structure):
+    """diso_sphere_field: spheres [count][4] (x, y, z, r) in device memory, grid bounds."""
+    _fields_ = [
+        ("spheres", ctypes.c_void_p),
+        ("count", ctypes.c_int),
+        ("lo", ctypes.c_double * 3),
+        ("hi", ctypes.c_double * 3),
+    ]
+
+
 EXPORTS = {
     # name: (restype, argtypes)
     "diso_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
@@ -70,6 +80,12 @@ EXPORTS = {
     "diso_zero_grads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_zero_count_share": (ctypes.c_double, []),
+    "diso_forward_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SphereFieldDesc), ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.POINTER(Counts)]),
+    "diso_field_materialize": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(SphereFieldDesc), ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_mesh_normals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                          ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_mesh_weld": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
@@ -222,6 +238,14 @@ class Extractor:
         grad_sdf.record_stream(side)
         if grad_deform is not None:
             grad_deform.record_stream(side)
+
+    def forward_field(self, desc, shape, iso, pad, seg, normalize, verts, faces) -> Counts:
+        """The forward of an evaluated field in one call (see diso_forward_field)."""
+        c = Counts()
+        check(lib().diso_forward_field(self._h, ctypes.byref(desc), *shape, iso, pad, ptr(seg), int(bool(normalize)),
+                                       ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], stream_of(verts.device),
+                                       ctypes.byref(c)), "forward of a field")
+        return c
 
     # mesh consumers (diso_mesh_*): the extractor supplies the dtype and the scratch
     def mesh_normals(self, verts, faces, out):

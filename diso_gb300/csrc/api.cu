@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/diso_gb300.h"
+#include "fields.cuh"
 #include "kernels.cuh"
 #include "mesh.cuh"
 #include "scan.cuh"
@@ -983,6 +984,89 @@ int batch_results(diso_extractor* ex, diso_counts* out, int64_t* voff, int64_t* 
 }  // namespace
 
 
+// ------------------------------------------------------------------ evaluated fields
+
+template <class S>
+SphereField<S> make_sphere_field(const diso_sphere_field* d, int nx, int ny, int nz, double iso, double padval) {
+  SphereField<S> f;
+  f.sph = (const S*)d->spheres;
+  f.K = d->count;
+  const int n[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a) {
+    f.lo[a] = (S)d->lo[a];
+    f.step[a] = n[a] > 1 ? (S)((d->hi[a] - d->lo[a]) / (double)(n[a] - 1)) : S(0);
+  }
+  f.n0 = nx;
+  f.n1 = ny;
+  f.n2 = nz;
+  f.iso = (S)iso;
+  f.pad = (S)padval;
+  return f;
+}
+
+// The forward of an evaluated field in one call, as forward_all without deform or
+// edge record: the count evaluates the chunks near the surface (the others it
+// classifies whole), the emit evaluates the end points of the crossing edges.
+template <class S>
+int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint64_t* seg, int normalize,
+                  void* verts, int64_t vcap, int64_t* faces, int64_t fcap, cudaStream_t s, diso_counts* out) {
+  Geom g;
+  g.init(f.n0, f.n1, f.n2);
+  int rc;
+  if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
+  if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
+  const int64_t scan_tiles = scan_reserve(ex, g.nseg);
+  if (scan_tiles == 0) return DISO_ERR_CUDA;
+  ex->zpend.set = ex->zemit_set = false;  // gradient zeros belong to a dense forward
+  count_prep_kernel<<<1, 256, 0, s>>>(ex->stats, ex->scan_flag, scan_tiles);
+  CUDA_TRY(cudaGetLastError());
+  CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
+  {
+    const int64_t units = count_units(g);
+    const int64_t want =
+        std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+    const unsigned grid = (unsigned)std::min<int64_t>(want, units);
+    KernelTimer kt(ex, K_COUNT, s);
+    if (ex->method == DISO_MC)
+      count_kernel<S, MC, SphereField<S>><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
+                                                                    ex->active);
+    else
+      count_kernel<S, DMC, SphereField<S>><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
+                                                                     ex->active);
+  }
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->pad[0]))) != DISO_OK)
+    return rc;
+  if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(&ex->stats->emit_tile, 0, sizeof(unsigned long long), s));
+  {
+    const ZeroJob zj{};
+    KernelTimer kt(ex, K_EMIT, s);
+    if (ex->method == DISO_MC)
+      mc_emit_kernel<S, SphereField<S>><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
+          f, g, seg, ex->active, &ex->stats->n_active, (S*)verts, faces, normalize, nullptr, vcap, fcap, ex->stats, zj);
+    else
+      dmc_emit_kernel<S, SphereField<S>><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
+          f, g, seg, codes, ex->active, &ex->stats->n_active, (S*)verts, faces, normalize, nullptr, vcap, fcap,
+          ex->stats, zj);
+  }
+  CUDA_TRY(cudaGetLastError());
+  if ((rc = count_read<S>(ex, f.n0, f.n1, f.n2, iso, seg, s, out)) != DISO_OK) return rc;
+  out->emitted = (out->n_verts <= vcap && out->n_faces <= fcap) ? 1 : 0;
+  return DISO_OK;
+}
+
+int check_field(const diso_sphere_field* field, int nx, int ny, int nz) {
+  if (!field || !field->spheres) return fail(DISO_ERR_ARG, "null field or spheres");
+  if (field->count < 1 || field->count > 65536) return fail(DISO_ERR_ARG, "sphere count %d (1..65536)", field->count);
+  if (nx < 1 || ny < 1 || nz < 1) return fail(DISO_ERR_ARG, "grid dims must be >= 1 (got %d x %d x %d)", nx, ny, nz);
+  const double cells = (double)(nx + 1) * (ny + 1) * (nz + 1);
+  if (3.0 * cells >= 2147483647.0) return fail(DISO_ERR_ARG, "grid too large: %d x %d x %d", nx, ny, nz);
+  for (int a = 0; a < 3; ++a)
+    if (!std::isfinite(field->lo[a]) || !std::isfinite(field->hi[a])) return fail(DISO_ERR_ARG, "non-finite bounds");
+  return DISO_OK;
+}
+
 // ------------------------------------------------------------------ mesh consumers
 
 constexpr unsigned long long MESH_ERR_INDEX = 8ull;  // Stats::error bit 3: a face index out of range
@@ -1407,6 +1491,43 @@ int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, in
                                                  n_faces, corners, (uint8_t*)body, s)
                                : mesh_ply<double>(ex, (const double*)verts, (const double*)normals, n_verts, faces,
                                                   n_faces, corners, (uint8_t*)body, s);
+}
+
+
+int diso_forward_field(diso_extractor* ex, const diso_sphere_field* field, int nx, int ny, int nz, double isovalue,
+                       double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces,
+                       int64_t fcap, void* stream, diso_counts* out) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  int rc = check_field(field, nx, ny, nz);
+  if (rc) return rc;
+  if (!seg || !out) return fail(DISO_ERR_ARG, "null seg or counts");
+  if (vcap < 0 || fcap < 0 || (vcap && !verts) || (fcap && !faces)) return fail(DISO_ERR_ARG, "bad output buffers");
+  if ((rc = bind_device(ex)) != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ex->dtype == DISO_F32)
+    return forward_field<float>(ex, make_sphere_field<float>(field, nx, ny, nz, isovalue, padval), isovalue, seg,
+                                normalize, verts, vcap, faces, fcap, s, out);
+  return forward_field<double>(ex, make_sphere_field<double>(field, nx, ny, nz, isovalue, padval), isovalue, seg,
+                               normalize, verts, vcap, faces, fcap, s, out);
+}
+
+int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, int ny, int nz, void* sdf,
+                           void* stream) {
+  if (dtype != DISO_F32 && dtype != DISO_F64) return fail(DISO_ERR_ARG, "unknown dtype %d", dtype);
+  int rc = check_field(field, nx, ny, nz);
+  if (rc) return rc;
+  if (!sdf) return fail(DISO_ERR_ARG, "null output grid");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = (int64_t)nx * ny * nz;
+  const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 65536);
+  if (dtype == DISO_F32)
+    field_materialize_kernel<float><<<blocks, 256, 0, s>>>(make_sphere_field<float>(field, nx, ny, nz, 0.0, 1.0),
+                                                          (float*)sdf);
+  else
+    field_materialize_kernel<double><<<blocks, 256, 0, s>>>(make_sphere_field<double>(field, nx, ny, nz, 0.0, 1.0),
+                                                           (double*)sdf);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
 }
 
 }  // extern "C"

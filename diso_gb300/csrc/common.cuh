@@ -65,6 +65,7 @@ struct Geom {
 
 template <class S>
 struct Field {
+  static constexpr bool kDense = true;  // a grid in memory (fields.cuh has evaluated ones)
   const S* __restrict__ sdf;
   const S* __restrict__ def;  // [N0][N1][N2][3] or null
   int n0, n1, n2;
@@ -81,6 +82,8 @@ struct Field {
   __device__ __forceinline__ int64_t lin(int X, int Y, int Z) const {
     return ((int64_t)(X - 1) * n1 + (Y - 1)) * n2 + (Z - 1);
   }
+  // unpadded point (x, y, z) of a row in the grid whose first point is at `off`
+  __device__ __forceinline__ S point(int64_t off, int, int, int z) const { return __ldg(sdf + off + z); }
   // deform at padded point (zero in the pad)
   __device__ __forceinline__ void deform(int X, int Y, int Z, S d[3]) const {
     if (def && inside(X, Y, Z)) {

@@ -87,8 +87,8 @@ __device__ const detail::PatchMasks g_dmc_pmask = detail::make_patch_masks();
 
 // lerp vertex of the edge from padded point (X,Y,Z) along axis a, in padded
 // coordinates with deform (computeMcVert, src/cumc.cu:343-368)
-template <class S>
-__device__ __forceinline__ void edge_vertex(const Field<S>& f, int X, int Y, int Z, int a, S out[3]) {
+template <class S, class F = Field<S>>
+__device__ __forceinline__ void edge_vertex(const F& f, int X, int Y, int Z, int a, S out[3]) {
   const int ex = a == 0, ey = a == 1, ez = a == 2;
   const S d0 = f.at(X, Y, Z), d1 = f.at(X + ex, Y + ey, Z + ez);
   S t = S(0.5);
@@ -220,9 +220,9 @@ __device__ __forceinline__ void unpack_loc(int64_t l, int& X, int& Y, int& Z, in
 // Warp w takes rows w, w + NW, ...; it issues the loads of BATCH rows before their
 // ballots, so each warp keeps BATCH row loads in flight.  Tracks min / max of the
 // caller's (interior) values when TRACK.  Needs blockDim.x == NTHREADS.
-template <class S, int WX, int WY, bool TRACK>
-__device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
-                                           S& mn, S& mx, bool& seen) {
+template <class S, int WX, int WY, bool TRACK, class F = Field<S>>
+__device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const F& f, int WX0, int WY0, int Z0, S& mn,
+                                           S& mx, bool& seen) {
   constexpr int NW = NTHREADS / 32, NR = WX * WY, BATCH = 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z = Z0 - 1 + lane, Ze = Z0 + 31 + lane;
@@ -237,10 +237,10 @@ __device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const Field<S>
       const int r = r0 + k * NW;
       const int x = r / WY, y = r % WY, X = WX0 + x, Y = WY0 + y;
       const bool row = r < NR && (unsigned)(X - 1) < (unsigned)f.n0 && (unsigned)(Y - 1) < (unsigned)f.n1;
-      const int64_t base = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 - 1;
+      const int64_t off = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2;
       in[k] = row && zin;
-      v[k] = in[k] ? __ldg(f.sdf + base + Z) : f.pad;
-      e[k] = (row && ein) ? __ldg(f.sdf + base + Ze) : f.pad;
+      v[k] = in[k] ? f.point(off, X - 1, Y - 1, Z - 1) : f.pad;
+      e[k] = (row && ein) ? f.point(off, X - 1, Y - 1, Ze - 1) : f.pad;
     }
 #pragma unroll
     for (int k = 0; k < BATCH; ++k) {
@@ -293,8 +293,8 @@ __device__ __forceinline__ int code_at(const CodeRow& r, int j) {
 }
 
 // Morton code of cell (X, Y, Z) from global memory
-template <class S>
-__device__ __forceinline__ int cell_code_far(const Field<S>& f, int X, int Y, int Z) {
+template <class S, class F = Field<S>>
+__device__ __forceinline__ int cell_code_far(const F& f, int X, int Y, int Z) {
   int c = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) c |= (f.at(X + (i & 1), Y + ((i >> 1) & 1), Z + ((i >> 2) & 1)) >= f.iso) << i;
@@ -303,8 +303,8 @@ __device__ __forceinline__ int cell_code_far(const Field<S>& f, int X, int Y, in
 
 // Morton code of cell (X, Y, Z) from the masks when its corners are in the
 // window, otherwise from global memory
-template <class S, int WX, int WY>
-__device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+template <class S, int WX, int WY, class F = Field<S>>
+__device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const F& f, int WX0, int WY0, int Z0,
                                          int X, int Y, int Z) {
   // rows x and x + 1 must both lie in the window (x is unsigned: a row below the
   // window wraps to a huge value and fails the test)
@@ -318,8 +318,8 @@ __device__ __forceinline__ int cell_code(const uint64_t (&m)[WX][WY], const Fiel
 // DMC code after the face-neighbour ambiguity test (src/cudualmc.cu:815-839):
 // a "problematic" code looks at the cell across its ambiguous face; when that
 // (raw) code is problematic too, the code is complemented.
-template <class S, int WX, int WY>
-__device__ __forceinline__ int dmc_resolve_m(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+template <class S, int WX, int WY, class F = Field<S>>
+__device__ __forceinline__ int dmc_resolve_m(const uint64_t (&m)[WX][WY], const F& f, int WX0, int WY0, int Z0,
                                              int code, int X, int Y, int Z, const Geom& g) {
   const int dir = dmc_dir(dmc_case(code));
   if (dir == 7) return code;
@@ -432,13 +432,57 @@ __device__ __forceinline__ void publish_minmax(Stats* stats, S mn, S mx) {
 // ballots of chunk t (unpadded z in [32t, 32t + 32)) of the warp's point rows into
 // sh.bal; min / max of the values read.  Only the lanes in `lanes` read (the chunks
 // below and above a unit contribute two bits and one bit to its masks).
-template <class S, int METHOD>
-__device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const Field<S>& f, int t, uint32_t lanes,
-                                              S& mn, S& mx) {
+template <class S, int METHOD, class F = Field<S>>
+__device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const F& f, int t, uint32_t lanes, S& mn,
+                                              S& mx, int X0, int Y0) {
   constexpr int NB = 4, HALF = (CRPW + NB - 1) / NB;  // NB batches of HALF row loads in flight
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int z = 32 * t + lane;
   const bool zin = (unsigned)z < (unsigned)f.n2 && ((lanes >> lane) & 1u);
+  if constexpr (!F::kDense) {
+    // an evaluated field: a chunk that is wholly on one side of iso is not evaluated;
+    // its rows' ballots are uniform, and its bound (a value on that side of iso)
+    // stands in for its min and max: the guard's tests (min >= iso, max <= iso) only
+    // need to know on which sides the values lie
+    const int l0 = __ffs(lanes) - 1, l1 = 31 - __clz(lanes);
+    const int xa = max(X0 - 1, 0), xb = min(X0 + CP - 1, f.n0 - 1);
+    const int ya = max(Y0 - 1, 0), yb = min(Y0 + CR - 1, f.n1 - 1);
+    const int za = max(32 * t + l0, 0), zb = min(32 * t + l1, f.n2 - 1);
+    const bool pads = X0 - 1 < 0 || X0 + CP - 1 >= f.n0 || Y0 - 1 < 0 || Y0 + CR - 1 >= f.n1 || 32 * t + l0 < 0 ||
+                      32 * t + l1 >= f.n2;
+    double bound = 0.0;
+    const int cls = f.classify(xa, xb, ya, yb, za, zb, pads, bound);
+    if (cls >= 0) {
+      const uint32_t b = cls ? 0xffffffffu : 0u;
+#pragma unroll
+      for (int i = 0; i < CRPW; ++i) {
+        const int r = warp + 8 * i;
+        if (r < CROWS && lane == 0) sh.bal[r] = b;
+      }
+      if (xa <= xb && ya <= yb && za <= zb) {
+        mn = smin(mn, (S)bound);
+        mx = smax(mx, (S)bound);
+      }
+      __syncwarp();
+      return;
+    }
+    // evaluated one row at a time (compute, not loads, is what takes the time)
+#pragma unroll 1
+    for (int i = 0; i < CRPW; ++i) {
+      const int r = warp + 8 * i;
+      if (r >= CROWS) break;
+      const bool in = zin && sh.rowoff[r] >= 0;
+      const S v = in ? f.point(0, X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z) : f.pad;
+      const uint32_t b = __ballot_sync(0xffffffffu, v >= f.iso);
+      if (lane == 0) sh.bal[r] = b;
+      if (in) {
+        mn = smin(mn, v);
+        mx = smax(mx, v);
+      }
+    }
+    __syncwarp();
+    return;
+  }
 #pragma unroll
   for (int h = 0; h < NB; ++h) {
     S v[HALF];
@@ -448,7 +492,7 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
       const int r = warp + 8 * (h * HALF + k);
       const int64_t off = r < CROWS ? sh.rowoff[r] : -1;
       in[k] = zin && off >= 0;
-      v[k] = in[k] ? __ldg(f.sdf + off + z) : f.pad;
+      v[k] = in[k] ? f.point(off, X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z) : f.pad;
     }
 #pragma unroll
     for (int k = 0; k < HALF; ++k) {
@@ -477,8 +521,8 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
 // the first y row when dy, the first z cell when dz: the cells of this tile whose
 // edges can touch the point tile one step back by (dx, dy, dz) (the backward's
 // activity test).
-template <class S, int METHOD>
-__device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+template <class S, int METHOD, class F = Field<S>>
+__device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F& f, const Geom& g,
                                             uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
                                             CellRec* __restrict__ codes, int X0, int Y0, int tz, int tag) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -629,8 +673,8 @@ __device__ __forceinline__ void count_chunk_empty(const Geom& g, uint64_t* __res
 
 // One unit: per-segment counts, activity bytes of its tiles, the grid's min / max;
 // active tiles are appended (as tile | tag) to sh.list.
-template <class S, int METHOD>
-__device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+template <class S, int METHOD, class F = Field<S>>
+__device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const F& f, const Geom& g,
                                            uint64_t* __restrict__ seg, uint8_t* __restrict__ tile_flag,
                                            CellRec* __restrict__ codes, Stats* stats, int64_t unit, int tag,
                                            int64_t& ck) {
@@ -655,7 +699,7 @@ __device__ __forceinline__ void count_unit(CountShared<S, METHOD>& sh, const Fie
   // unpadded z in [32tz - 2, 32tz + 33)
 #pragma unroll 1
   for (int t = tz0 - 1; t <= tz1; ++t) {
-    count_ballots<S, METHOD>(sh, f, t, t < tz0 ? 0xc0000000u : (t == tz1 ? 1u : 0xffffffffu), mn, mx);
+    count_ballots<S, METHOD>(sh, f, t, t < tz0 ? 0xc0000000u : (t == tz1 ? 1u : 0xffffffffu), mn, mx, X0, Y0);
     const uint32_t mixed = count_combine<S, METHOD>(sh, t >= tz0 + 1, p1, p2);
     if (t < tz0 + 1) continue;
     // slots rotate over the CTA's chunks: slot (ck+2)%3 was last read before the
@@ -684,8 +728,8 @@ __device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned
   for (int i = threadIdx.x; i < sh.nlist; i += blockDim.x) active[sh.base + i] = sh.list[i];
 }
 
-template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS, 3) count_kernel(Field<S> f, Geom g, uint64_t* __restrict__ seg,
+template <class S, int METHOD, class F = Field<S>>
+__global__ void __launch_bounds__(NTHREADS, F::kDense ? 3 : 2) count_kernel(F f, Geom g, uint64_t* __restrict__ seg,
                                                             uint8_t* __restrict__ tile_flag,
                                                             CellRec* __restrict__ codes, Stats* stats,
                                                             int* __restrict__ active) {
@@ -1085,8 +1129,8 @@ constexpr int EMIT_ITEMS = 3 * TX * TY * TZ;  // every own edge crossing
 
 // One active tile: its vertices and triangles.  Vertex ids written into faces are
 // reduced by vsub (the grid's first vertex, for batches whose vertices are concatenated).
-template <class S>
-__device__ __forceinline__ void mc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+template <class S, class F = Field<S>>
+__device__ __forceinline__ void mc_emit_tile(const F& f, const Geom& g, const uint64_t* __restrict__ seg,
                                              int tile, S* __restrict__ verts, int64_t* __restrict__ faces,
                                              int normalize, int64_t vsub, const EdgeRecord<S>& rec) {
   constexpr int WX = TX + 2, WY = TY + 2;  // point rows [X0, X0+TX+1] x [Y0, Y0+TY+1]
@@ -1223,8 +1267,8 @@ __device__ __forceinline__ bool emit_fits(const Geom& g, const uint64_t* __restr
 
 // persistent over the *n_active active tiles of the count, taken in turn from a
 // counter (tiles differ much in cost)
-template <class S>
-__global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+template <class S, class F = Field<S>>
+__global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(F f, Geom g, const uint64_t* __restrict__ seg,
                                                            const int* __restrict__ active,
                                                            const unsigned long long* __restrict__ n_active,
                                                            S* __restrict__ verts, int64_t* __restrict__ faces,
@@ -1275,8 +1319,8 @@ __host__ __device__ constexpr int epos_cap() {
 // and in-segment patch offsets come from the cell records of the count (valid for the
 // segments whose count is not zero; the others hold trivial cells only), so the SDF is
 // read only for the edge vertices.
-template <class S>
-__device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, const uint64_t* __restrict__ seg,
+template <class S, class F = Field<S>>
+__device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const uint64_t* __restrict__ seg,
                                               const CellRec* __restrict__ codes, int tile, S* __restrict__ verts,
                                               int64_t* __restrict__ quads, int normalize, int64_t vsub,
                                               const EdgeRecord<S>& rec) {
@@ -1425,10 +1469,14 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
     item_decode(witems[i], ix, iy, j, a);
     if (cached) {
       S p[3];
-      if (inner)
-        edge_vertex_in<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
-      else
+      if constexpr (F::kDense) {
+        if (inner)
+          edge_vertex_in<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+        else
+          edge_vertex<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+      } else {
         edge_vertex<S>(f, X0 + ix, Y0 + iy, Z0 + j, a, p);
+      }
       epos[i][0] = p[0];
       epos[i][1] = p[1];
       epos[i][2] = p[2];
@@ -1517,8 +1565,8 @@ __device__ __forceinline__ void dmc_emit_tile(const Field<S>& f, const Geom& g, 
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
-template <class S>
-__global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg,
+template <class S, class F = Field<S>>
+__global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(F f, Geom g, const uint64_t* __restrict__ seg,
                                                                const CellRec* __restrict__ codes,
                                                                const int* __restrict__ active,
                                                                const unsigned long long* __restrict__ n_active,

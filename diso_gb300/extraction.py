@@ -132,9 +132,10 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
         d = deform.detach().contiguous() if deform is not None else None
         seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=dev)
         wants_grad = torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad))
-        # When a gradient can be asked for, its buffers are allocated now and zeroed on
-        # a second stream while the count runs (the count reads HBM far below its
-        # bandwidth); the backward then writes only the point tiles near the surface.
+        # When a gradient can be asked for, its buffers are allocated now; the forward's
+        # count and emit write their zeros between their own loads (they leave HBM
+        # bandwidth unused), and the backward writes only the point tiles near the
+        # surface.
         grads = None
         if wants_grad:
             grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=dev)
@@ -184,6 +185,13 @@ class DiffMC(nn.Module):
     def forward(self, grid, deform=None, isovalue=0.0, normalize=True):
         return extract(self._ex, grid, deform, isovalue, normalize)
 
+    def forward_field(self, field, shape, isovalue=0.0, normalize=True):
+        """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,
+        without a dense grid in memory; forward only."""
+        from .fields import extract_field
+
+        return extract_field(self._ex, field, shape, isovalue, normalize)
+
 
 class DiffDMC(nn.Module):
     """Differentiable dual marching cubes (diso/__init__.py:63-147).
@@ -200,3 +208,10 @@ class DiffDMC(nn.Module):
 
     def forward(self, grid, deform=None, isovalue=0.0, return_quads=False, normalize=True):
         return extract(self._ex, grid, deform, isovalue, normalize, return_quads, self.exact_grad)
+
+    def forward_field(self, field, shape, isovalue=0.0, return_quads=False, normalize=True):
+        """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,
+        without a dense grid in memory; forward only."""
+        from .fields import extract_field
+
+        return extract_field(self._ex, field, shape, isovalue, normalize, return_quads)

@@ -243,6 +243,36 @@ int diso_timing(diso_extractor* ex, int enable);
  * end events), at most `max` entries, *n = entries written; then starts over. */
 int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n);
 
+/* ---- Evaluated fields ----
+ * The caller side of the extraction without the dense grid: the reference's caller
+ * evaluates its SDF on a full meshgrid in PyTorch and passes the [N, N, N] tensor
+ * (test/example.py:8-16, 33-53).  Here the extractor evaluates the field where it
+ * needs values: the count classifies each chunk of 8 x 32 x 32 cells from bounds of
+ * the field over it and evaluates only the chunks that may hold the surface, the
+ * emit evaluates the end points of the crossing edges.  The field: a union of spheres,
+ * value(p) = min_k (|p - c_k| - r_k) at grid point p = lo + (hi - lo) * i / (n - 1)
+ * (per axis; step computed in double, then in the dtype), spheres [count][4] (x, y,
+ * z, r) in device memory in the extractor's dtype.  Forward only (no deform, no
+ * gradients). */
+typedef struct diso_sphere_field {
+  const void* spheres;
+  int count;
+  double lo[3];
+  double hi[3];
+} diso_sphere_field;
+
+/* As diso_forward for an evaluated field: count, scan and emit in one call into
+ * outputs of capacities vcap / fcap; counts->emitted says whether they fitted (if not,
+ * call again with larger outputs).  counts->sdf_min / sdf_max are bounds on the side
+ * of the isovalue that decide the empty-surface guard, not the grid's extremes. */
+int diso_forward_field(diso_extractor* ex, const diso_sphere_field* field, int nx, int ny, int nz, double isovalue,
+                       double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces,
+                       int64_t fcap, void* stream, diso_counts* counts);
+
+/* The field's dense grid [nx][ny][nz] (the same values the fused forward evaluates). */
+int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, int ny, int nz, void* sdf,
+                           void* stream);
+
 /* ---- Mesh consumers on the device ----
  * For the meshes the extractor returns: vertices [n_verts][3] in the extractor's
  * dtype, faces [n_faces][corners] int64 (corners 3 or 4).  Each call runs on

@@ -104,3 +104,16 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "nope.so"))
     with pytest.raises(RuntimeError, match="missing"):
         _native.lib()
+
+
+def test_field_entry_points_check_their_arguments(lib):
+    import ctypes
+
+    from diso_gb300 import _native as N
+
+    c = N.Counts()
+    d = N.SphereFieldDesc()
+    assert lib.diso_forward_field(None, None, 4, 4, 4, 0.0, 1.0, None, 1, None, 0, None, 0, None, ctypes.byref(c)) == 1
+    assert lib.diso_field_materialize(7, ctypes.byref(d), 4, 4, 4, None, None) == 1
+    d.count = 0
+    assert lib.diso_field_materialize(0, ctypes.byref(d), 4, 4, 4, None, None) == 1

@@ -1,0 +1,72 @@
+"""The fused forward of an evaluated field (DiffMC / DiffDMC.forward_field over
+diso_forward_field) against the dense forward on the same field's grid
+(field.materialize), which the other parity tests tie to the reference: vertices and
+faces must be identical, bit for bit, including where the count classified whole
+chunks without evaluating them."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DT = {"float32": torch.float32, "float64": torch.float64}
+
+
+def _field(kind, device, dtype):
+    from diso_gb300 import SphereUnion
+
+    rng = np.random.default_rng(7)
+    if kind == "example":  # the reference example's sphere and bounding box (test/example.py:20-53)
+        m = 0.5 + 1 / 64
+        return SphereUnion(torch.zeros(1, 3, device=device, dtype=dtype), torch.full((1,), 0.5, device=device,
+                                                                                        dtype=dtype), (-m,) * 3, (m,) * 3)
+    if kind == "spheres":
+        c = rng.uniform(-0.8, 0.8, (16, 3))
+        r = rng.uniform(0.05, 0.3, 16)
+    elif kind == "faces":  # spheres through the grid's faces
+        c = np.array([[1.0, 0.0, 0.0], [-0.2, -1.0, 0.3], [0.1, 0.2, 0.95]])
+        r = np.array([0.5, 0.4, 0.3])
+    elif kind == "inside":  # one sphere holding the whole grid: every value below iso, so the guard
+        c, r = np.zeros((1, 3)), np.array([3.0])
+    elif kind == "far":  # no surface: the empty-surface guard
+        c, r = np.array([[5.0, 5.0, 5.0]]), np.array([0.5])
+    elif kind == "small":  # few small spheres on a large grid: most chunks classified whole
+        c = rng.uniform(-0.6, 0.6, (4, 3))
+        r = rng.uniform(0.05, 0.12, 4)
+    return SphereUnion(torch.tensor(c, device=device, dtype=dtype), torch.tensor(r, device=device, dtype=dtype))
+
+
+CASES = [
+    # (field, shape, iso, normalize)
+    ("example", (64, 64, 64), 0.0, True),
+    ("spheres", (96, 80, 112), 0.0, True),
+    ("faces", (70, 65, 33), 0.0, True),
+    ("spheres", (57, 40, 77), 0.1, False),
+    ("inside", (40, 37, 50), 0.0, True),
+    ("far", (48, 48, 48), 0.0, True),
+    ("small", (160, 160, 160), 0.0, True),
+]
+
+
+@pytest.mark.parametrize("method", ["mc", "dmc"])
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("kind,shape,iso,normalize", CASES)
+def test_fused_field_matches_dense(cuda_device, method, dtype, kind, shape, iso, normalize):
+    from diso_gb300 import DiffDMC, DiffMC
+
+    dt = DT[dtype]
+    field = _field(kind, cuda_device, dt)
+    grid = field.materialize(shape, dt)
+    mod = DiffMC(dt) if method == "mc" else DiffDMC(dt)
+    variants = [{}] if method == "mc" else [{"return_quads": True}, {"return_quads": False}]
+    for kw in variants:
+        for _ in range(2):  # the second call uses the capacities the first one learned
+            v, f = mod.forward_field(field, shape, isovalue=iso, normalize=normalize, **kw)
+            with torch.no_grad():
+                vd, fd = mod(grid, isovalue=iso, normalize=normalize, **kw)
+            assert v.shape == vd.shape and f.shape == fd.shape and f.dtype == fd.dtype, (kw, v.shape, vd.shape)
+            assert torch.equal(v, vd) and torch.equal(f, fd), kw
+    if kind in ("far", "inside"):  # the empty-surface guard (all values above / below iso)
+        assert v.shape[0] == 0 and f.dtype == torch.int32
+    else:
+        assert v.shape[0] > 0
