@@ -258,6 +258,45 @@ def run_mesh(device, n=512, steps=5, warmup=2, cpu_sample=100000):
     return res
 
 
+def run_field(device, n=512, steps=10, warmup=3):
+    """The benchmark's 16 spheres (without the noise, which no closed form has) as an
+    evaluated field on [-1, 1]^3 at n^3: the fused forward (no dense grid) against
+    materialising the grid and running the dense forward, DiffDMC with quads, no
+    gradients.  Both give the same mesh (tests/test_gpu_fields.py)."""
+    from diso_gb300 import DiffDMC, SphereUnion
+
+    g = torch.Generator().manual_seed(SEED)
+    c = torch.rand(16, 3, generator=g, dtype=torch.float64) * 1.6 - 0.8
+    r = torch.rand(16, generator=g, dtype=torch.float64) * 0.25 + 0.05
+    field = SphereUnion(c.to(device, torch.float32), r.to(device, torch.float32))
+    mod = DiffDMC(torch.float32)
+
+    def dense():
+        with torch.no_grad():
+            return mod(field.materialize((n, n, n)), return_quads=True)
+
+    def fused():
+        return mod.forward_field(field, (n, n, n), return_quads=True)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, out
+
+    ms_d, (vd, qd) = timed(dense)
+    ms_f, (vf, qf) = timed(fused)
+    return {"field": f"16 spheres on [-1,1]^3 at {n}^3, DiffDMC quads, forward", "verts": vf.shape[0],
+            "quads": qf.shape[0], "same_mesh": bool(torch.equal(vd, vf) and torch.equal(qd, qf)),
+            "dense_ms": ms_d, "fused_ms": ms_f, "speedup": ms_d / ms_f}
+
+
 def run_served(device, nreq=2000, rate=2000.0):
     """p50 / p99 latency and grids/s of the continuous-batching server against the
     plain per-request call on the same arrival trace."""
@@ -641,7 +680,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_batched:
         for name, fn in (("batched_mc", lambda: run_batched(device, 0)), ("batched_dmc", lambda: run_batched(device, 1)),
                          ("served", lambda: run_served(device, args.requests)),
-                         ("mesh_consumers", lambda: run_mesh(device, args.n))):
+                         ("mesh_consumers", lambda: run_mesh(device, args.n)),
+                         ("fused_field", lambda: run_field(device, args.n))):
             try:
                 res[name] = fn()
             except Exception as e:  # report, but keep the headline line

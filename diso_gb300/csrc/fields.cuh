@@ -42,50 +42,86 @@ struct SphereField {
   __device__ __forceinline__ S point(int64_t, int x, int y, int z) const { return value(x, y, z); }
   __device__ __forceinline__ void deform(int, int, int, S d[3]) const { d[0] = d[1] = d[2] = S(0); }
 
+  // value() over the spheres in `cand` only (bit k: sphere k; all of them when
+  // `all`): the same value when the others cannot be the minimum (classify_warp)
+  __device__ __forceinline__ S value_of(int x, int y, int z, uint64_t cand, bool all) const {
+    if (all) return value(x, y, z);
+    const S px = lo[0] + step[0] * (S)x, py = lo[1] + step[1] * (S)y, pz = lo[2] + step[2] * (S)z;
+    S m = S(INFINITY);
+    while (cand) {
+      const int k = __ffsll((long long)cand) - 1;
+      cand &= cand - 1;
+      const S dx = px - __ldg(sph + 4 * k), dy = py - __ldg(sph + 4 * k + 1), dz = pz - __ldg(sph + 4 * k + 2);
+      const S d = sqrt(dx * dx + dy * dy + dz * dz) - __ldg(sph + 4 * k + 3);
+      m = d < m ? d : m;
+    }
+    return m;
+  }
+
   // The points with unpadded indices in [x0, x1] x [y0, y1] x [z0, z1] (the part in
-  // the grid; `pads`: some of the box lies outside it): 1 when every value is >= iso
-  // (the pad value is), 0 when every value is < iso and none is a pad, -1 otherwise.
-  // From bounds of each sphere's distance over the box in double, with a margin far
-  // above the rounding of value(); `bound` receives a value on the box's side of iso
-  // (a lower bound of its values for 1, an upper bound for 0).
-  __device__ __forceinline__ int classify(int x0, int x1, int y0, int y1, int z0, int z1, bool pads,
-                                          double& bound) const {
+  // the grid; `pads`: some of the box lies outside it), by the calling warp (one
+  // sphere per lane): cls = 1 when every value is >= iso (the pad value is), 0 when
+  // every value is < iso and none is a pad, -1 otherwise; `bound` a value on the
+  // box's side of iso for 1 and 0; `cand` the spheres that can be the minimum
+  // somewhere in the box (`all`: every sphere, for more than 64).  From bounds of
+  // each sphere's distance over the box with a margin (1e-4 of the coordinates'
+  // scale) far above the rounding of value().
+  __device__ __forceinline__ int classify_warp(int x0, int x1, int y0, int y1, int z0, int z1, bool pads, S& bound,
+                                               uint64_t& cand, bool& all) const {
+    const int lane = threadIdx.x & 31;
+    all = K > 64;
+    cand = 0;
     if (x0 > x1 || y0 > y1 || z0 > z1) return 1;  // only pad points
-    double bmin[3], bmax[3];
+    S bmin[3], bmax[3];
     const int i0[3] = {x0, y0, z0}, i1[3] = {x1, y1, z1};
-    double scale = fabs((double)iso) + 1.0;
+    S scale = fabs(iso) + S(1);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      const double u = (double)lo[a] + (double)step[a] * i0[a], v = (double)lo[a] + (double)step[a] * i1[a];
-      bmin[a] = fmin(u, v);
-      bmax[a] = fmax(u, v);
+      const S u = lo[a] + step[a] * (S)i0[a], v = lo[a] + step[a] * (S)i1[a];
+      bmin[a] = u < v ? u : v;
+      bmax[a] = u < v ? v : u;
       scale += fabs(bmin[a]) + fabs(bmax[a]);
     }
-    double fmin_lo = INFINITY, fmax_hi = INFINITY;  // min over spheres of each one's lower / upper bound
-    for (int k = 0; k < K; ++k) {
-      double dn = 0.0, df = 0.0;
+    S lo_k[2] = {S(INFINITY), S(INFINITY)};  // this lane's spheres lane, lane + 32 (the first 64)
+    S fmin_lo = S(INFINITY), fmax_hi = S(INFINITY), rmax = S(0);
+    for (int k = lane; k < K; k += 32) {
+      S dn = S(0), df = S(0);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const double c = (double)__ldg(sph + 4 * k + a);
-        const double near = c < bmin[a] ? bmin[a] - c : (c > bmax[a] ? c - bmax[a] : 0.0);
-        const double far = fmax(fabs(c - bmin[a]), fabs(c - bmax[a]));
+        const S c = __ldg(sph + 4 * k + a);
+        const S near = c < bmin[a] ? bmin[a] - c : (c > bmax[a] ? c - bmax[a] : S(0));
+        const S far = fabs(c - bmin[a]) > fabs(c - bmax[a]) ? fabs(c - bmin[a]) : fabs(c - bmax[a]);
         dn += near * near;
         df += far * far;
       }
-      const double r = (double)__ldg(sph + 4 * k + 3);
-      scale = fmax(scale, fabs(r));
-      fmin_lo = fmin(fmin_lo, sqrt(dn) - r);
-      fmax_hi = fmin(fmax_hi, sqrt(df) - r);
+      const S r = __ldg(sph + 4 * k + 3);
+      const S l = sqrt(dn) - r, h = sqrt(df) - r;
+      if (k < 64) lo_k[k >> 5] = l;
+      fmin_lo = l < fmin_lo ? l : fmin_lo;
+      fmax_hi = h < fmax_hi ? h : fmax_hi;
+      rmax = fabs(r) > rmax ? fabs(r) : rmax;
     }
-    const double margin = 1e-4 * scale;
-    if (fmin_lo >= (double)iso + margin) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const S a = __shfl_xor_sync(0xffffffffu, fmin_lo, o), b = __shfl_xor_sync(0xffffffffu, fmax_hi, o);
+      const S c = __shfl_xor_sync(0xffffffffu, rmax, o);
+      fmin_lo = a < fmin_lo ? a : fmin_lo;
+      fmax_hi = b < fmax_hi ? b : fmax_hi;
+      rmax = c > rmax ? c : rmax;
+    }
+    const S margin = S(1e-4) * (scale + rmax);
+    if (fmin_lo >= iso + margin) {
       bound = fmin_lo;
       return 1;
     }
-    if (!pads && fmax_hi < (double)iso - margin) {
+    if (!pads && fmax_hi < iso - margin) {
       bound = fmax_hi;
       return 0;
     }
+    // a sphere whose lower bound lies above the smallest upper bound is never the minimum
+    const uint32_t c0 = __ballot_sync(0xffffffffu, lane < K && lo_k[0] <= fmax_hi + margin);
+    const uint32_t c1 = __ballot_sync(0xffffffffu, lane + 32 < K && lo_k[1] <= fmax_hi + margin);
+    cand = (uint64_t)c0 | ((uint64_t)c1 << 32);
     return -1;
   }
 };

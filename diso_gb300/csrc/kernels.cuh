@@ -450,8 +450,10 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
     const int za = max(32 * t + l0, 0), zb = min(32 * t + l1, f.n2 - 1);
     const bool pads = X0 - 1 < 0 || X0 + CP - 1 >= f.n0 || Y0 - 1 < 0 || Y0 + CR - 1 >= f.n1 || 32 * t + l0 < 0 ||
                       32 * t + l1 >= f.n2;
-    double bound = 0.0;
-    const int cls = f.classify(xa, xb, ya, yb, za, zb, pads, bound);
+    S bound = S(0);
+    uint64_t cand = 0;
+    bool all = true;
+    const int cls = f.classify_warp(xa, xb, ya, yb, za, zb, pads, bound, cand, all);
     if (cls >= 0) {
       const uint32_t b = cls ? 0xffffffffu : 0u;
 #pragma unroll
@@ -460,8 +462,8 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
         if (r < CROWS && lane == 0) sh.bal[r] = b;
       }
       if (xa <= xb && ya <= yb && za <= zb) {
-        mn = smin(mn, (S)bound);
-        mx = smax(mx, (S)bound);
+        mn = smin(mn, bound);
+        mx = smax(mx, bound);
       }
       __syncwarp();
       return;
@@ -472,7 +474,7 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
       const int r = warp + 8 * i;
       if (r >= CROWS) break;
       const bool in = zin && sh.rowoff[r] >= 0;
-      const S v = in ? f.point(0, X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z) : f.pad;
+      const S v = in ? f.value_of(X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z, cand, all) : f.pad;
       const uint32_t b = __ballot_sync(0xffffffffu, v >= f.iso);
       if (lane == 0) sh.bal[r] = b;
       if (in) {
@@ -482,32 +484,33 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
     }
     __syncwarp();
     return;
-  }
+  } else {
 #pragma unroll
-  for (int h = 0; h < NB; ++h) {
-    S v[HALF];
-    bool in[HALF];
+    for (int h = 0; h < NB; ++h) {
+      S v[HALF];
+      bool in[HALF];
 #pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      const int r = warp + 8 * (h * HALF + k);
-      const int64_t off = r < CROWS ? sh.rowoff[r] : -1;
-      in[k] = zin && off >= 0;
-      v[k] = in[k] ? f.point(off, X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z) : f.pad;
-    }
-#pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      const int r = warp + 8 * (h * HALF + k);
-      if (h * HALF + k < CRPW && r < CROWS) {
-        const uint32_t b = __ballot_sync(0xffffffffu, v[k] >= f.iso);
-        if (lane == 0) sh.bal[r] = b;
+      for (int k = 0; k < HALF; ++k) {
+        const int r = warp + 8 * (h * HALF + k);
+        const int64_t off = r < CROWS ? sh.rowoff[r] : -1;
+        in[k] = zin && off >= 0;
+        v[k] = in[k] ? f.point(off, X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z) : f.pad;
       }
-      if (in[k]) {
-        mn = smin(mn, v[k]);
-        mx = smax(mx, v[k]);
+#pragma unroll
+      for (int k = 0; k < HALF; ++k) {
+        const int r = warp + 8 * (h * HALF + k);
+        if (h * HALF + k < CRPW && r < CROWS) {
+          const uint32_t b = __ballot_sync(0xffffffffu, v[k] >= f.iso);
+          if (lane == 0) sh.bal[r] = b;
+        }
+        if (in[k]) {
+          mn = smin(mn, v[k]);
+          mx = smax(mx, v[k]);
+        }
       }
     }
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 // Counts of the unit's chunk tz from the masks in sh.m (complete: the caller
