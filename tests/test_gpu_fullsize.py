@@ -73,3 +73,26 @@ def test_benchmark_grid_identities(cuda_device, workload):
     used = torch.zeros(vq.shape[0], dtype=torch.bool, device=vq.device)
     used[q.reshape(-1)] = True
     assert bool(used.all())
+
+
+def test_near_maximum_grid(cuda_device):
+    # 860^3 (the C ABI accepts grids up to 3 (n+1)^3 < 2^31 cells, about 890^3): cell
+    # records and segment indices beyond 2^31 entries of a row-major grid; MC and DMC
+    # forwards agree on the crossing edges, every index is in range, every dual vertex
+    # is used, and a repeat is bit-identical
+    from diso_gb300 import DiffDMC, DiffMC
+
+    n = 860
+    sdf = bench.spheres_field(n, cuda_device)
+    with torch.no_grad():
+        vm, fm = DiffMC(torch.float32)(sdf)
+        mod = DiffDMC(torch.float32)
+        vq, q = mod(sdf, return_quads=True)
+        vq2, q2 = mod(sdf, return_quads=True)
+    assert vm.shape[0] == q.shape[0] > 0
+    assert int(q.min()) >= 0 and int(q.max()) < vq.shape[0] and int(fm.max()) < vm.shape[0]
+    used = torch.zeros(vq.shape[0], dtype=torch.bool, device=vq.device)
+    used[q.reshape(-1)] = True
+    assert bool(used.all())
+    assert torch.equal(vq, vq2) and torch.equal(q, q2)
+    assert float(vq.min()) >= -0.01 and float(vq.max()) <= 1.01  # normalised to the grid
