@@ -1,7 +1,7 @@
 """Shared test helpers: golden fixtures, the reference's tolerances and the
 comparisons used by both the oracle tests (CPU) and the CUDA parity tests (GPU).
 
-Tolerances (the bar the benchmark spec states for this path):
+Tolerances (the bar for this path):
 * case codes, face index lists and vertex counts: exact;
 * vertices: within 1e-6 of the grid extent in float32, 1e-12 in float64
   (extent = 1 with normalize, dim - 1 without);
