@@ -70,3 +70,21 @@ def test_fused_field_matches_dense(cuda_device, method, dtype, kind, shape, iso,
         assert v.shape[0] == 0 and f.dtype == torch.int32
     else:
         assert v.shape[0] > 0
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_materialize_matches_the_field_definition(cuda_device, dtype):
+    # value(p) = min_k (|p - c_k| - r_k) at p = lo + (hi - lo) * i / (n - 1), against a
+    # float64 numpy evaluation (within rounding: the device contracts lo + step * i)
+    dt = DT[dtype]
+    field = _field("spheres", cuda_device, dt)
+    shape = (23, 17, 31)
+    got = field.materialize(shape, dt).cpu().numpy().astype(np.float64)
+    sph = field.spheres.cpu().numpy().astype(np.float64)
+    axes = [np.asarray(field.lo[a]) + (field.hi[a] - field.lo[a]) / (shape[a] - 1) * np.arange(shape[a])
+            for a in range(3)]
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+    ref = np.full(shape, np.inf)
+    for cx, cy, cz, r in sph:
+        ref = np.minimum(ref, np.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2) - r)
+    assert np.abs(got - ref).max() <= (1e-5 if dtype == "float32" else 1e-12)
