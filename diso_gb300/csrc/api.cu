@@ -443,11 +443,11 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
       count_kernel<S, DMC><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
   }
   CUDA_TRY(cudaGetLastError());
-  return run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->pad[0]));
+  return run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->total));
 }
 
-// the count's results to the host (into the pinned stats mirror; its pad[0] holds
-// the scanned total), then an event
+// the count's results to the host (into the pinned stats mirror, the scanned total
+// included), then an event
 template <class S>
 int count_copy(diso_extractor* ex, const Geom& g, const uint64_t* seg, cudaStream_t s) {
   (void)g;
@@ -466,7 +466,7 @@ int count_read(diso_extractor* ex, int nx, int ny, int nz, double iso, const uin
   (void)seg;
   CUDA_TRY(cudaEventSynchronize(ex->ev_counts));
   const Stats& h = *ex->stats_host;
-  const uint64_t total = h.pad[0];
+  const uint64_t total = h.total;
   if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
   if (h.error & 4ull) return fail(DISO_ERR_SCAN, "count: wait for a TMA copy gave up");
   // the low half counts crossings, the high half triangles (MC) or patches (DMC)
@@ -1035,7 +1035,7 @@ int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint6
                                                                      ex->active);
   }
   CUDA_TRY(cudaGetLastError());
-  if ((rc = run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->pad[0]))) != DISO_OK)
+  if ((rc = run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->total))) != DISO_OK)
     return rc;
   if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
   CUDA_TRY(cudaMemsetAsync(&ex->stats->emit_tile, 0, sizeof(unsigned long long), s));

@@ -179,7 +179,8 @@ struct Stats {
                                 // bit 2: a TMA wait gave up
   unsigned long long scan_tile; // dynamic tile counter of the look-back scan
   unsigned long long emit_tile; // dynamic tile counter of the emit
-  unsigned long long pad[2];
+  unsigned long long total;      // the segment scan's total (the forward's counts)
+  unsigned long long units;      // next unit of the TMA count (a grid-wide counter)
 };
 
 }  // namespace diso

@@ -795,9 +795,11 @@ struct BoxCursor {
     tz1 = min(tz0 + kz, g.nzc);
     t = tz0;
   }
-  __device__ void next(const Geom& g, int64_t nunits) {
+  // the next box; after a unit's last one, the unit next_unit() returns
+  template <class NextUnit>
+  __device__ void next(const Geom& g, int64_t nunits, NextUnit next_unit) {
     if (++t >= tz1) {
-      unit += gridDim.x;
+      unit = next_unit();
       if (unit < nunits) start(g, unit);
     }
   }
@@ -921,6 +923,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   __shared__ CountShared<S, METHOD> sh;
   __shared__ __align__(8) uint64_t full[TMA_STAGES];
   __shared__ __align__(128) uint4 zbuf[ZBUF / 16];
+  __shared__ int64_t uq[4];  // units in the order the producer took them (a ring: it runs <= 2 boxes ahead)
   unsigned char* stage_mem = dyn_smem + ((128u - (smem_u32(dyn_smem) & 127u)) & 127u);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nunits = count_tma_units(g);
@@ -933,18 +936,34 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
     mbar_fence_init();
   }
   __syncthreads();
+  // Units are taken from a grid-wide counter (stats->units, zeroed by the forward's
+  // reset) by the producer (thread 0) as it reaches them, so CTAs that met cheap
+  // units take more; the consumers follow the producer's order through uq (each id
+  // is written at least one CTA barrier before it is read).
+  unsigned long long* const unit_ctr = &stats->units;
+  int pseq = 0, cseq = 0;
+  auto take_unit = [&]() -> int64_t {
+    const int64_t u = (int64_t)atomicAdd(unit_ctr, 1ull);
+    const int64_t v = u < nunits ? u : nunits;
+    uq[pseq++ & 3] = v;
+    return v;
+  };
   BoxCursor pc, cc;  // producer (thread 0) and consumer positions
   pc.unit = cc.unit = nunits;
-  if (blockIdx.x < nunits) {
-    pc.start(g, blockIdx.x);
-    cc = pc;
-  }
   int64_t issued = 0;
   if (threadIdx.x == 0) {
+    const int64_t u = take_unit();
+    if (u < nunits) pc.start(g, u);
     for (int st = 0; st < TMA_STAGES && pc.valid(nunits); ++st, ++issued) {
       issue_box<S>(&wide, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
-      pc.next(g, nunits);
+      pc.next(g, nunits, take_unit);
     }
+  }
+  __syncthreads();  // uq holds the first units
+  auto read_unit = [&]() -> int64_t { return uq[cseq++ & 3]; };
+  {
+    const int64_t u = read_unit();
+    if (u < nunits) cc.start(g, u);
   }
   S mn = S(INFINITY), mx = S(-INFINITY);
   uint32_t p1[2] = {0u, 0u}, p2[2] = {0u, 0u};
@@ -989,7 +1008,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
       if (pc.valid(nunits)) {
         fence_proxy_async();
         issue_box<S>(&wide, stage_mem + st * tma_box_bytes<S>(), &full[st], pc);
-        pc.next(g, nunits);
+        pc.next(g, nunits, take_unit);
         ++issued;
       }
     }
@@ -1010,7 +1029,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
       else
         count_chunk_empty<S, METHOD>(g, seg, tile_flag, cc.X0, cc.Y0, cc.t);
     }
-    cc.next(g, nunits);
+    cc.next(g, nunits, read_unit);
   }
   if (failed && threadIdx.x == 0) {
     atomicOr(&stats->error, 4ull);
