@@ -74,6 +74,8 @@ EXPORTS = {
                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_isovalue_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_forward_count_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Counts)]),
@@ -142,7 +144,7 @@ def iso_values(isovalue: float, dtype: torch.dtype):
     """(iso, padval) as the reference's kernels see them: the isovalue in the
     grid's dtype and the pad value isovalue + 1 computed in Python and then
     rounded to that dtype (diso/__init__.py:52)."""
-    iso = float(isovalue)
+    iso = float(isovalue.detach()) if isinstance(isovalue, torch.Tensor) else float(isovalue)
     if dtype == torch.float32:
         return float(np.float32(iso)), float(np.float32(iso + 1.0))
     return iso, iso + 1.0
@@ -276,3 +278,12 @@ class Extractor:
         check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg), ptr(record),
                                   int(bool(normalize)), flags, ptr(grad_verts), ptr(grad_sdf),
                                   ptr(grad_deform), stream_of(sdf.device)), "backward")
+
+    def isovalue_grad(self, grad_sdf, seg=None):
+        """dL/d(isovalue) = -(sum of dL/dsdf), as a 0-dim float64 tensor on the
+        gradient's device (diso_isovalue_grad); `seg`, the forward's record, limits
+        the reads to the point tiles near the surface."""
+        out = torch.empty((), dtype=torch.float64, device=grad_sdf.device)
+        check(lib().diso_isovalue_grad(self._h, ptr(grad_sdf), *grad_sdf.shape, ptr(seg), ptr(out),
+                                       stream_of(grad_sdf.device)), "isovalue gradient")
+        return out

@@ -138,9 +138,11 @@ def _guard(res, i, iso, dtype):
 
 class _BatchFunction(Function):
     @staticmethod
-    def forward(ctx, bx, n, has_def, isos, normalize, return_quads, exact_grad, *inputs):
+    def forward(ctx, bx, n, has_def, isos, normalize, return_quads, exact_grad, iso_grids, *inputs):
+        # inputs: the n grids, the n deforms (has_def), then the isovalue tensors of
+        # the grids listed in iso_grids (those whose isovalue requires grad)
         sdfs = [t.detach().contiguous() for t in inputs[:n]]
-        defs = [t.detach().contiguous() for t in inputs[n:]] if has_def else None
+        defs = [t.detach().contiguous() for t in inputs[n:2 * n]] if has_def else None
         dev = sdfs[0].device
         grids = _grids(sdfs, defs, isos, bx.dtype)
         record = torch.empty(record_slots(grids), dtype=torch.int64, device=dev)
@@ -152,12 +154,14 @@ class _BatchFunction(Function):
         width = 3 if bx.method == N.MC else 4
         verts = torch.empty((nv, 3), dtype=bx.dtype, device=dev)
         faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
-        wants_grad = any(ctx.needs_input_grad[7:])
+        wants_grad = any(ctx.needs_input_grad[8:])
         edges = bx.edge_record(nv, nf, dev) if wants_grad else None
         bx.emit(normalize, verts, faces, dev, edges)
         ctx.bx, ctx.n, ctx.has_def, ctx.isos, ctx.normalize, ctx.exact = bx, n, has_def, isos, normalize, exact_grad
         ctx.record, ctx.edges, ctx.caps = record, edges, (nv, nf)
-        ctx.save_for_backward(*inputs)
+        ctx.iso_grids = iso_grids
+        ctx.iso_like = [(t.dtype, t.device, t.shape) for t in inputs[(2 if has_def else 1) * n:]]
+        ctx.save_for_backward(*inputs[:(2 if has_def else 1) * n])
         meta = [(int(res.voff[i]), int(res.counts[i].n_verts), int(res.foff[i]), int(res.counts[i].n_faces),
                  _guard(res, i, isos[i], bx.dtype)) for i in range(n)]
         ctx.meta = meta
@@ -182,7 +186,7 @@ class _BatchFunction(Function):
         inputs = ctx.saved_tensors
         n = ctx.n
         sdfs = [t.detach().contiguous() for t in inputs[:n]]
-        defs = [t.detach().contiguous() for t in inputs[n:]] if ctx.has_def else None
+        defs = [t.detach().contiguous() for t in inputs[n:2 * n]] if ctx.has_def else None
         dev = sdfs[0].device
         gs = [torch.empty_like(s) for s in sdfs]
         gd = [torch.empty_like(d) for d in defs] if defs is not None else None
@@ -193,17 +197,26 @@ class _BatchFunction(Function):
         bx.prepare(grids, ctx.record, dev)
         gv = gverts.contiguous() if gverts is not None else torch.zeros(0, 3, dtype=bx.dtype, device=dev)
         bx.backward(ctx.normalize, ctx.exact, gv, ctx.edges, *ctx.caps, dev)
-        return (None,) * 7 + tuple(gs) + (tuple(gd) if gd is not None else ())
+        # dL/d(isovalue) per grid: minus the sum of the grid's dL/dsdf
+        giso = [bx.ex.isovalue_grad(gs[i]).to(device=device, dtype=dtype).reshape(shape)
+                for i, (dtype, device, shape) in zip(ctx.iso_grids, ctx.iso_like)]
+        return (None,) * 8 + tuple(gs) + (tuple(gd) if gd is not None else ()) + tuple(giso)
 
 
 def extract_batch(bx: _Batch, sdfs, deforms=None, isovalue=0.0, normalize=True, return_quads=False,
                   exact_grad=False):
     """Differentiable extraction of a list of grids; returns a list of (verts, faces),
-    each what DiffMC / DiffDMC returns for that grid alone."""
+    each what DiffMC / DiffDMC returns for that grid alone.  `isovalue`: one value
+    for all grids or one per grid; a tensor that requires grad receives
+    dL/d(isovalue)."""
     n = len(sdfs)
     if n == 0:
         return []
-    isos = list(isovalue) if isinstance(isovalue, (list, tuple)) else [float(isovalue)] * n
+    isos = list(isovalue) if isinstance(isovalue, (list, tuple)) else [isovalue] * n
+    if len(isos) != n:
+        raise RuntimeError(f"{len(isos)} isovalues for {n} grids")
+    iso_grids = [i for i, v in enumerate(isos)
+                 if isinstance(v, torch.Tensor) and v.requires_grad and torch.is_grad_enabled()]
     for s in sdfs:
         if not s.is_cuda or s.dim() != 3 or s.dtype != bx.dtype:
             raise RuntimeError("every grid must be a 3-d CUDA tensor of the extractor's dtype")
@@ -211,10 +224,11 @@ def extract_batch(bx: _Batch, sdfs, deforms=None, isovalue=0.0, normalize=True, 
         for s, d in zip(sdfs, deforms):
             if d is None or tuple(d.shape) != tuple(s.shape) + (3,) or d.dtype != bx.dtype:
                 raise RuntimeError("deforms must be [X, Y, Z, 3] tensors matching their grids")
-    inputs = list(sdfs) + (list(deforms) if deforms is not None else [])
+    inputs = list(sdfs) + (list(deforms) if deforms is not None else []) + [isos[i] for i in iso_grids]
+    values = [float(v.detach()) if isinstance(v, torch.Tensor) else float(v) for v in isos]
     with torch.cuda.device(sdfs[0].device):
-        verts, faces = _BatchFunction.apply(bx, n, deforms is not None, isos, bool(normalize), bool(return_quads),
-                                            bool(exact_grad), *inputs)
+        verts, faces = _BatchFunction.apply(bx, n, deforms is not None, values, bool(normalize), bool(return_quads),
+                                            bool(exact_grad), iso_grids, *inputs)
     out = []
     width = 3 if (bx.method == N.MC or not return_quads) else 4
     for i, (v0, nvi, f0, nfi, empty) in enumerate(bx.last_meta):

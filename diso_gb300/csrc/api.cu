@@ -92,6 +92,8 @@ struct diso_extractor {
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
   unsigned* plist_n = nullptr;
+  double* isog = nullptr;        // per-CTA partial sums of the isovalue gradient
+  int64_t isog_cap = 0;
 
   // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
   void* bdesc = nullptr;         // device BatchGrid<S>[MAX_BATCH]
@@ -154,6 +156,9 @@ struct diso_extractor {
     mesh_cap = 0;
     cudaFree(plist);
     cudaFree(plist_n);
+    cudaFree(isog);
+    isog = nullptr;
+    isog_cap = 0;
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -1312,6 +1317,26 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                                : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, edge_record,
                                                   normalize, flags, grad_verts, grad_sdf,
                                                   deform ? grad_deform : nullptr, s);
+}
+
+int diso_isovalue_grad(diso_extractor* ex, const void* grad_sdf, int nx, int ny, int nz, const uint64_t* seg,
+                       double* grad_iso, void* stream) {
+  if (!grad_iso) return fail(DISO_ERR_ARG, "null grad_iso");
+  int rc = check_common(ex, grad_sdf, nx, ny, nz);
+  if (rc) return rc;
+  Geom g;
+  g.init(nx, ny, nz);
+  if ((rc = grow(ex->isog, ex->isog_cap, ISO_GRAD_CTAS)) != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint8_t* flags = seg ? tile_flags(seg, g) : nullptr;
+  if (ex->dtype == DISO_F32)
+    iso_grad_partial_kernel<float><<<ISO_GRAD_CTAS, 256, 0, s>>>(g, flags, (const float*)grad_sdf, ex->isog);
+  else
+    iso_grad_partial_kernel<double><<<ISO_GRAD_CTAS, 256, 0, s>>>(g, flags, (const double*)grad_sdf, ex->isog);
+  CUDA_TRY(cudaGetLastError());
+  iso_grad_final_kernel<<<1, 256, 0, s>>>(ex->isog, ISO_GRAD_CTAS, grad_iso);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
 }
 
 double diso_zero_count_share(void) { return ZERO_COUNT_SHARE; }

@@ -13,6 +13,7 @@
 //   gather_list_kernel   backward, those point tiles: dL/dsdf and dL/ddeform as sums
 //                        of edge adjoints (the rest of the gradients are the zeros
 //                        of the forward, or zero_tiles_kernel's)
+//   iso_grad_*        dL/d(isovalue) from dL/dsdf (optional)
 //   split_*           DMC quad -> triangle split (return_quads=False)
 //   batch_*           the same phases over a batch of grids
 // Mesh consumers (normals, weld, OBJ, PLY) are in mesh.cuh.
@@ -1927,6 +1928,72 @@ __global__ void __launch_bounds__(256) active_ptiles_kernel(Geom g, const uint8_
     if (lane == 0 && m) at = atomicAdd(count, (unsigned)__popc(m));
     at = __shfl_sync(0xffffffffu, at, 0);
     if (act) list[at + __popc(m & ((1u << lane) - 1u))] = (int)p;
+  }
+}
+
+// dL/d(isovalue) of an extraction, which the reference does not give (its isovalue is
+// a plain scalar, diso/__init__.py:48, 102): minus the sum of dL/dsdf over the grid.
+// Moving the isovalue by e moves every crossing exactly as moving every grid value by
+// -e (the pad value isovalue + 1 moves with the isovalue), and the lerp's adjoints of
+// an edge's two ends, (iso - d1) / (d1 - d0)^2 adj_t and (d0 - iso) / (d1 - d0)^2 adj_t
+// (src/cumc.cu:412-453), sum to minus the isovalue's, adj_t / (d1 - d0).  A pad end's
+// adjoint, dropped from dL/dsdf, is that end's share of the pad value's own term, so
+// the grid's points alone give the isovalue's.
+//
+// Partial sums in double, one per CTA, over a static assignment of point tiles (warp
+// w of the grid takes tiles w, w + W, ...); with the forward's tile flags the tiles
+// with no crossing nearby (their gradients are zeros) are skipped.  The reductions
+// run in a fixed order, so the result repeats bit for bit.
+constexpr int ISO_GRAD_CTAS = 512;
+
+template <class S>
+__global__ void __launch_bounds__(256) iso_grad_partial_kernel(Geom g, const uint8_t* __restrict__ tile_flag,
+                                                               const S* __restrict__ gsdf,
+                                                               double* __restrict__ partial) {
+  __shared__ double wsum[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nw = (int64_t)gridDim.x * 8;
+  double acc = 0.0;
+  for (int64_t p = (int64_t)blockIdx.x * 8 + warp; p < g.nptiles(); p += nw) {
+    int x0, y0, z0;
+    ptile_coords(p, g, x0, y0, z0);
+    if (tile_flag) {
+      const int a = lane < 8 ? ptile_flag(g, tile_flag, x0, y0, z0, lane) : 0;
+      if (!__any_sync(0xffffffffu, a)) continue;
+    }
+    const int z = z0 + lane;
+    if (z >= g.n[2]) continue;
+    for (int q = 0; q < TX * TY; ++q) {
+      const int x = x0 + q / TY, y = y0 + q % TY;
+      if (x < g.n[0] && y < g.n[1]) acc += (double)gsdf[((int64_t)x * g.n[1] + y) * g.n[2] + z];
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) wsum[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += wsum[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// the partial sums in a fixed order; out = -(their sum)
+__global__ void __launch_bounds__(256) iso_grad_final_kernel(const double* __restrict__ partial, int n,
+                                                             double* __restrict__ out) {
+  __shared__ double wsum[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) wsum[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += wsum[w];
+    *out = -t;
   }
 }
 

@@ -15,7 +15,9 @@ Differences that are invisible to callers of the reference API:
   its count; the backward computes each edge's adjoint once and writes the
   gradients near the surface, deterministically (no atomics);
 * vertices are shifted and normalised, and faces written as int64, inside the
-  kernels; the DMC quad split runs on the GPU in one pass plus a scan.
+  kernels; the DMC quad split runs on the GPU in one pass plus a scan;
+* an isovalue given as a tensor that requires grad gets dL/d(isovalue), minus
+  the sum of dL/dsdf (the reference's isovalue is a plain scalar).
 
 The outputs are the reference's: the same vertex, face and quad order, the same
 dtypes, including the int32 empty faces of the guard.
@@ -62,7 +64,8 @@ class _ExtractFunction(Function):
     backward needs."""
 
     @staticmethod
-    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads, out):
+    def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads, out,
+                iso_tensor):
         verts_buf, faces_buf, record = out
         nv, nf = int(counts.n_verts), int(counts.n_faces)
         verts, faces = verts_buf[:nv], faces_buf[:nf]
@@ -72,7 +75,8 @@ class _ExtractFunction(Function):
             n = ex.split(verts, faces, tris)
             _mark("split", "end")
             faces = tris[:n]
-        wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        wants_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1] or ctx.needs_input_grad[12]
+        ctx.iso_like = (iso_tensor.dtype, iso_tensor.device, iso_tensor.shape) if iso_tensor is not None else None
         ctx.gs, ctx.gd = grads if (wants_grad and grads is not None) else (None, None)
         ctx.ex = ex
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
@@ -102,8 +106,12 @@ class _ExtractFunction(Function):
             _mark("backward", "start")
             ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
                             zeroed=zeroed)
+            giso = None
+            if ctx.needs_input_grad[12]:
+                dtype, device, shape = ctx.iso_like
+                giso = ctx.ex.isovalue_grad(gs, seg).to(device=device, dtype=dtype).reshape(shape)
             _mark("backward", "end")
-        return gs, gd, None, None, None, None, None, None, None, None, None, None
+        return gs, gd, None, None, None, None, None, None, None, None, None, None, giso
 
 
 def _capacity(n):
@@ -113,6 +121,9 @@ def _capacity(n):
 def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
             exact_grad=False):
     """One differentiable extraction with the reference's semantics.
+
+    An isovalue given as a tensor that requires grad (a one-element tensor, not in
+    the reference) receives dL/d(isovalue) in the backward.
 
     exact_grad (DMC only) replaces the reference's backward in cells with several
     patches, where every patch receives the first patch's gradient
@@ -131,7 +142,9 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
         g = grid.detach().contiguous()
         d = deform.detach().contiguous() if deform is not None else None
         seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=dev)
-        wants_grad = torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad))
+        iso_tensor = isovalue if isinstance(isovalue, torch.Tensor) and isovalue.requires_grad else None
+        wants_grad = torch.is_grad_enabled() and (grid.requires_grad or (deform is not None and deform.requires_grad)
+                                                  or iso_tensor is not None)
         # When a gradient can be asked for, its buffers are allocated now; the forward's
         # count and emit write their zeros between their own loads (they leave HBM
         # bandwidth unused), and the backward writes only the point tiles near the
@@ -171,7 +184,7 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
             out = (verts, faces, record)
         _mark("forward", "end")
         return _ExtractFunction.apply(grid, deform, ex, seg, counts, iso, pad, bool(normalize), bool(return_quads),
-                                      bool(exact_grad), grads, out)
+                                      bool(exact_grad), grads, out, iso_tensor)
 
 
 class DiffMC(nn.Module):

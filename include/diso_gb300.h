@@ -137,6 +137,19 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                   double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
                   const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
 
+/* dL/d(isovalue) of an extraction, from the dL/dsdf [nx][ny][nz] that
+ * diso_backward wrote: minus its sum (moving the isovalue by e moves every crossing
+ * as moving every grid value by -e; the pad value isovalue + 1 moves with it).  The
+ * result is written as one double to device memory at grad_iso on `stream`.  With
+ * the forward's `seg`, only the point tiles near the surface are read (the others
+ * hold zeros); with seg = NULL the whole grid.  Deterministic (a fixed reduction
+ * order).  The gradient is that of the backward's flags: exact with
+ * DISO_GRAD_EXACT (and for MC), the counterpart of the reference's DMC gradient
+ * otherwise.  No counterpart in the reference, whose isovalue is a plain scalar
+ * without a gradient (diso/__init__.py:48, 102). */
+int diso_isovalue_grad(diso_extractor* ex, const void* grad_sdf, int nx, int ny, int nz, const uint64_t* seg,
+                       double* grad_iso, void* stream);
+
 /* Zero a forward's gradient buffers ahead of its backward, beside the forward's
  * kernels, which leave HBM bandwidth unused.  Call it before diso_forward_count /
  * diso_forward on `stream`; the zeros are complete once that forward's emit has run

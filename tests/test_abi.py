@@ -117,3 +117,17 @@ def test_field_entry_points_check_their_arguments(lib):
     assert lib.diso_field_materialize(7, ctypes.byref(d), 4, 4, 4, None, None) == 1
     d.count = 0
     assert lib.diso_field_materialize(0, ctypes.byref(d), 4, 4, 4, None, None) == 1
+
+
+def test_isovalue_grad_checks_its_arguments(lib):
+    h = ctypes.c_void_p()
+    assert lib.diso_create(0, 0, ctypes.byref(h)) == 0 and h.value
+    out = ctypes.c_void_p(16)
+    # rejected before any CUDA call: no extractor, no gradient, no output, bad dims
+    assert lib.diso_isovalue_grad(None, ctypes.c_void_p(16), 4, 4, 4, None, out, None) == 1
+    assert lib.diso_isovalue_grad(h, None, 4, 4, 4, None, out, None) == 1
+    assert lib.diso_isovalue_grad(h, ctypes.c_void_p(16), 4, 4, 4, None, None, None) == 1
+    assert b"grad_iso" in lib.diso_last_error()
+    assert lib.diso_isovalue_grad(h, ctypes.c_void_p(16), 4, 0, 4, None, out, None) == 1
+    assert b"grid dims" in lib.diso_last_error()
+    lib.diso_destroy(h)

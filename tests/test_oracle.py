@@ -115,6 +115,31 @@ def test_oracle_backward_finite_differences(method):
     assert abs(fd - gd[j]) <= 1e-6 * max(1.0, abs(fd))
 
 
+@pytest.mark.parametrize("method", [O.MC, O.DMC])
+@pytest.mark.parametrize("field", ["sphere", "plane"])
+def test_isovalue_gradient_is_minus_the_sdf_gradient_sum(method, field):
+    """dL/d(isovalue) = -(sum of dL/dsdf over the grid), the identity behind the
+    native isovalue gradient: central differences in the isovalue (float64) against
+    the oracle's backward.  The plane crosses the grid's faces, so edges to the pad
+    (isovalue + 1, moving with the isovalue) carry vertices too."""
+    rng = np.random.default_rng(5)
+    n = 10
+    a = np.linspace(-1, 1, n)
+    X, Y, Z = np.meshgrid(a, a, a, indexing="ij")
+    base = _sphere(n) if field == "sphere" else 0.6 * X + 0.3 * Y - 0.2 * Z - 0.1
+    sdf = base + 0.03 * rng.standard_normal((n, n, n))
+    deform = rng.uniform(-0.3, 0.3, (n, n, n, 3))
+    iso, h = 0.02, 1e-6
+    v, f, _ = O.extract(method, sdf, deform, iso, True, True, "float64")
+    w = rng.standard_normal(v.shape)
+    gs, _ = O.backward(method, sdf, deform, w, iso, True, "float64", exact=True)
+    lp, fp, _ = O.extract(method, sdf, deform, iso + h, True, True, "float64")
+    lm, fm, _ = O.extract(method, sdf, deform, iso - h, True, True, "float64")
+    assert np.array_equal(fp, f) and np.array_equal(fm, f)  # the same crossings at both ends
+    fd = ((lp * w).sum() - (lm * w).sum()) / (2 * h)
+    assert abs(fd + gs.sum()) <= 1e-6 * max(1.0, abs(fd)), (fd, -gs.sum())
+
+
 def test_empty_guard_when_max_equals_iso():
     sdf = -np.ones((5, 5, 5))
     sdf[2, 2, 2] = 0.0
