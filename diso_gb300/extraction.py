@@ -19,6 +19,11 @@ Differences that are invisible to callers of the reference API:
 * an isovalue given as a tensor that requires grad gets dL/d(isovalue), minus
   the sum of dL/dsdf (the reference's isovalue is a plain scalar).
 
+With recompute=True the forward keeps nothing for the backward but the inputs
+(no edge record, no gradient buffers: the reference's memory profile), and the
+backward runs the forward again to rebuild the edge record; slower, and the
+same gradients bit for bit.
+
 The outputs are the reference's: the same vertex, face and quad order, the same
 dtypes, including the int32 empty faces of the guard.
 """
@@ -65,7 +70,7 @@ class _ExtractFunction(Function):
 
     @staticmethod
     def forward(ctx, grid, deform, ex, seg, counts, iso, pad, normalize, return_quads, exact_grad, grads, out,
-                iso_tensor):
+                iso_tensor, recompute):
         verts_buf, faces_buf, record = out
         nv, nf = int(counts.n_verts), int(counts.n_faces)
         verts, faces = verts_buf[:nv], faces_buf[:nf]
@@ -81,7 +86,9 @@ class _ExtractFunction(Function):
         ctx.ex = ex
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
         ctx.has_deform = deform is not None
-        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg,
+        ctx.recompute, ctx.counts = recompute, (nv, nf)
+        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0),
+                              seg if not recompute else seg.new_empty(0),
                               record if record is not None else seg.new_empty(0))
         ctx.mark_non_differentiable(faces)
         # the faces never get a gradient; without this autograd would fill one with zeros
@@ -97,13 +104,17 @@ class _ExtractFunction(Function):
             if grad_verts is None:
                 grad_verts = torch.zeros(0, 3, dtype=g.dtype, device=g.device)
             gv = grad_verts.contiguous()
-            gs, gd = ctx.gs, ctx.gd
-            zeroed = gs is not None
-            if not zeroed:  # a second backward of the same graph (retain_graph)
-                gs = torch.empty_like(g)
-                gd = torch.empty_like(d) if d is not None else None
-            ctx.gs = ctx.gd = None
             _mark("backward", "start")
+            if ctx.recompute:
+                seg, record, gs, gd = _recompute(ctx.ex, g, d, ctx.iso, ctx.pad, ctx.normalize, *ctx.counts)
+                zeroed = True
+            else:
+                gs, gd = ctx.gs, ctx.gd
+                zeroed = gs is not None
+                if not zeroed:  # a second backward of the same graph (retain_graph)
+                    gs = torch.empty_like(g)
+                    gd = torch.empty_like(d) if d is not None else None
+                ctx.gs = ctx.gd = None
             ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
                             zeroed=zeroed)
             giso = None
@@ -111,7 +122,28 @@ class _ExtractFunction(Function):
                 dtype, device, shape = ctx.iso_like
                 giso = ctx.ex.isovalue_grad(gs, seg).to(device=device, dtype=dtype).reshape(shape)
             _mark("backward", "end")
-        return gs, gd, None, None, None, None, None, None, None, None, None, None, giso
+        return gs, gd, None, None, None, None, None, None, None, None, None, None, giso, None
+
+
+def _recompute(ex, g, d, iso, pad, normalize, nv, nf):
+    """The forward once more, for a backward whose forward kept nothing: the
+    segment record, the edge record (the outputs are rebuilt into temporaries) and
+    gradient buffers that this forward zeroes.  The reference's backward re-runs its
+    forward in the same way (diso/__init__.py:32, 86)."""
+    dev = g.device
+    seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=dev)
+    gs = torch.empty_like(g)
+    gd = torch.empty_like(d) if d is not None else None
+    ex.zero_grads(gs, gd)
+    width = 3 if ex.method == N.MC else 4
+    verts = torch.empty((nv, 3), dtype=ex.dtype, device=dev)
+    faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
+    record = torch.empty(max(1, ex.record_slots(n_verts=nv, n_faces=nf)), dtype=torch.int64, device=dev)
+    counts = ex.forward(g, d, iso, pad, seg, normalize, verts, faces, record)
+    if not counts.emitted or int(counts.n_verts) != nv or int(counts.n_faces) != nf:
+        raise RuntimeError("the forward run again for the backward gave another mesh "
+                           "(was the grid changed in place?)")
+    return seg, record, gs, gd
 
 
 def _capacity(n):
@@ -119,11 +151,14 @@ def _capacity(n):
 
 
 def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
-            exact_grad=False):
+            exact_grad=False, recompute=False):
     """One differentiable extraction with the reference's semantics.
 
     An isovalue given as a tensor that requires grad (a one-element tensor, not in
     the reference) receives dL/d(isovalue) in the backward.
+
+    recompute=True keeps no edge record and no gradient buffers between the
+    forward and the backward; the backward runs the forward again instead.
 
     exact_grad (DMC only) replaces the reference's backward in cells with several
     patches, where every patch receives the first patch's gradient
@@ -149,8 +184,9 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
         # count and emit write their zeros between their own loads (they leave HBM
         # bandwidth unused), and the backward writes only the point tiles near the
         # surface.
+        keep = wants_grad and not recompute  # the edge record and the gradient buffers
         grads = None
-        if wants_grad:
+        if keep:
             grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=dev)
                      if d is not None else None)
             ex.zero_grads(*grads)
@@ -163,7 +199,7 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
             verts = torch.empty((vcap, 3), dtype=ex.dtype, device=dev)
             faces = torch.empty((fcap, width), dtype=torch.int64, device=dev)
             record = (torch.empty(max(1, ex.record_slots(n_verts=vcap, n_faces=fcap)), dtype=torch.int64, device=dev)
-                      if wants_grad else None)
+                      if keep else None)
             counts = ex.forward(g, d, iso, pad, seg, normalize, verts, faces, record)
             if counts.emitted:
                 out = (verts, faces, record)
@@ -179,24 +215,28 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
             verts = torch.empty((nv, 3), dtype=ex.dtype, device=dev)
             faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
             record = (torch.empty(max(1, ex.record_slots(counts)), dtype=torch.int64, device=dev)
-                      if wants_grad else None)
+                      if keep else None)
             ex.emit(g, d, iso, pad, seg, normalize, verts, faces, record)
             out = (verts, faces, record)
         _mark("forward", "end")
         return _ExtractFunction.apply(grid, deform, ex, seg, counts, iso, pad, bool(normalize), bool(return_quads),
-                                      bool(exact_grad), grads, out, iso_tensor)
+                                      bool(exact_grad), grads, out, iso_tensor, bool(recompute))
 
 
 class DiffMC(nn.Module):
-    """Differentiable marching cubes (diso/__init__.py:9-61)."""
+    """Differentiable marching cubes (diso/__init__.py:9-61).
 
-    def __init__(self, dtype=torch.float32):
+    ``recompute=True`` (keyword only, not in the reference) keeps nothing between
+    the forward and the backward but the inputs; the backward runs the forward again."""
+
+    def __init__(self, dtype=torch.float32, *, recompute=False):
         super().__init__()
         self.dtype = dtype
+        self.recompute = recompute
         self._ex = N.Extractor(N.MC, dtype)
 
     def forward(self, grid, deform=None, isovalue=0.0, normalize=True):
-        return extract(self._ex, grid, deform, isovalue, normalize)
+        return extract(self._ex, grid, deform, isovalue, normalize, recompute=self.recompute)
 
     def forward_field(self, field, shape, isovalue=0.0, normalize=True):
         """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,
@@ -211,16 +251,18 @@ class DiffDMC(nn.Module):
 
     ``exact_grad=True`` (keyword only, not in the reference) gives the true
     derivative in cells with several patches; the default reproduces the
-    reference's gradient there (every patch gets the first patch's gradient)."""
+    reference's gradient there (every patch gets the first patch's gradient).
+    ``recompute=True`` as for DiffMC."""
 
-    def __init__(self, dtype=torch.float32, *, exact_grad=False):
+    def __init__(self, dtype=torch.float32, *, exact_grad=False, recompute=False):
         super().__init__()
         self.dtype = dtype
         self.exact_grad = exact_grad
+        self.recompute = recompute
         self._ex = N.Extractor(N.DMC, dtype)
 
     def forward(self, grid, deform=None, isovalue=0.0, return_quads=False, normalize=True):
-        return extract(self._ex, grid, deform, isovalue, normalize, return_quads, self.exact_grad)
+        return extract(self._ex, grid, deform, isovalue, normalize, return_quads, self.exact_grad, self.recompute)
 
     def forward_field(self, field, shape, isovalue=0.0, return_quads=False, normalize=True):
         """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,

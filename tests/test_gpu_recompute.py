@@ -1,0 +1,89 @@
+"""recompute=True: the forward keeps no edge record and no gradient buffers (the
+reference's memory profile: its backward re-runs the forward, diso/__init__.py:32,
+86); the backward runs the forward again.  Outputs and gradients equal the default
+mode's bit for bit, and the forward holds less device memory."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(n, dtype, dev, seed):
+    rng = np.random.default_rng(seed)
+    a = np.linspace(-1, 1, n)
+    X, Y, Z = np.meshgrid(a, a, a, indexing="ij")
+    npdt = np.float32 if dtype == torch.float32 else np.float64
+    sdf = (np.sqrt(X * X + Y * Y + Z * Z) - 0.55 + 0.03 * rng.standard_normal((n, n, n))).astype(npdt)
+    deform = rng.uniform(-0.3, 0.3, (n, n, n, 3)).astype(npdt)
+    return torch.tensor(sdf, device=dev), torch.tensor(deform, device=dev)
+
+
+def _module(method, dtype, recompute):
+    from diso_gb300 import DiffDMC, DiffMC
+
+    return DiffMC(dtype, recompute=recompute) if method == "mc" else DiffDMC(dtype, recompute=recompute)
+
+
+def _step(mod, sdf, deform, kw, iso=0.0):
+    s = sdf.clone().requires_grad_(True)
+    d = deform.clone().requires_grad_(True) if deform is not None else None
+    v, f = mod(s, d, iso, **kw)
+    w = torch.randn(v.shape, dtype=v.dtype, device=v.device, generator=torch.Generator(v.device).manual_seed(3))
+    (v * w).sum().backward()
+    return v.detach(), f, s.grad, d.grad if d is not None else None
+
+
+@pytest.mark.parametrize("method,kw", [("mc", {}), ("dmc", {"return_quads": True}), ("dmc", {})])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("with_deform", [True, False])
+def test_recompute_equals_stored(cuda_device, method, kw, dtype, with_deform):
+    sdf, deform = _inputs(40, dtype, cuda_device, 1)
+    deform = deform if with_deform else None
+    for iso in (0.0, 0.02):
+        a = _step(_module(method, dtype, False), sdf, deform, kw, iso)
+        b = _step(_module(method, dtype, True), sdf, deform, kw, iso)
+        for x, y in zip(a, b):
+            assert (x is None and y is None) or torch.equal(x, y)
+
+
+def test_recompute_isovalue_grad(cuda_device):
+    sdf, deform = _inputs(32, torch.float64, cuda_device, 2)
+    out = []
+    for recompute in (False, True):
+        iso = torch.tensor(0.01, dtype=torch.float64, device=cuda_device, requires_grad=True)
+        v, _ = _module("dmc", torch.float64, recompute)(sdf, deform, iso)
+        (v * v).sum().backward()
+        out.append(iso.grad)
+    assert torch.equal(out[0], out[1])
+
+
+def test_recompute_holds_less_memory(cuda_device):
+    n = 96
+    sdf, deform = _inputs(n, torch.float32, cuda_device, 3)
+    held = {}
+    for recompute in (False, True):
+        mod = _module("dmc", torch.float32, recompute)
+        with torch.no_grad():
+            mod(sdf, deform)  # the size hint for this shape
+        s = sdf.clone().requires_grad_(True)
+        d = deform.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        m0 = torch.cuda.memory_allocated(cuda_device)
+        v, f = mod(s, d, return_quads=True)
+        torch.cuda.synchronize()
+        held[recompute] = torch.cuda.memory_allocated(cuda_device) - m0
+        v.sum().backward()
+        del v, f, s, d
+    # the default forward holds the gradient buffers (4 n^3 floats) and the edge record
+    assert held[True] + 4 * n ** 3 * 4 <= held[False], held
+
+
+def test_recompute_detects_a_changed_grid(cuda_device):
+    sdf, _ = _inputs(24, torch.float32, cuda_device, 4)
+    s = sdf.clone().requires_grad_(True)
+    v, _ = _module("mc", torch.float32, True)(s)
+    with torch.no_grad():
+        s.add_(0.5)  # in place, after the forward: autograd's version check refuses the backward
+    with pytest.raises(RuntimeError):
+        v.sum().backward()
