@@ -164,6 +164,10 @@ class Extractor:
     def __init__(self, method: int, dtype: torch.dtype):
         self.method = method
         self.dtype = dtype
+        # output capacities per grid shape from the last extraction of that shape
+        # (dense grids and evaluated fields), for the single-call forward
+        self.size_hints = {}
+        self.field_hints = {}
         self._h = ctypes.c_void_p()
         check(lib().diso_create(method, dtype_tag(dtype), ctypes.byref(self._h)), "create")
 

@@ -190,7 +190,7 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
             grads = (torch.empty_like(g), torch.empty(tuple(g.shape) + (3,), dtype=g.dtype, device=dev)
                      if d is not None else None)
             ex.zero_grads(*grads)
-        hints = ex.__dict__.setdefault("size_hints", {})
+        hints = ex.size_hints
         hint = hints.get(tuple(g.shape))
         counts, out = None, None
         _mark("forward", "start")

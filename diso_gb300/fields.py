@@ -77,7 +77,7 @@ def extract_field(ex: N.Extractor, field, shape, isovalue=0.0, normalize=True, r
     with torch.cuda.device(dev):
         desc = field.desc(ex.dtype)
         seg = torch.empty(N.Extractor.segment_slots(shape), dtype=torch.int64, device=dev)
-        hints = ex.__dict__.setdefault("field_hints", {})
+        hints = ex.field_hints
         vcap, fcap = hints.get(shape, (1 << 16, 1 << 16))
         while True:
             verts = torch.empty((vcap, 3), dtype=ex.dtype, device=dev)
