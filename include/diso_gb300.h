@@ -73,7 +73,10 @@ int diso_create(int method, int dtype, diso_extractor** out);
 /* Free the extractor's scratch (the reference's ~CUMC / ~CUDMC, src/pybind.cpp:27-39, 219-232). */
 void diso_destroy(diso_extractor* ex);
 
-/* Number of uint64 slots of the per-call `seg` array for an nx*ny*nz grid. */
+/* Number of uint64 slots of the per-call `seg` array for an nx*ny*nz grid.  The
+ * caller owns this per-call state; the reference keeps its per-cell scan buffers in
+ * the extension object and grows them there (ensure_* in src/cumc.cu:177-263,
+ * src/cudualmc.cu:515-603). */
 int64_t diso_segment_slots(int nx, int ny, int nz);
 
 /* Forward, phase 1: case codes, counts, scan and the empty-surface guard.
@@ -95,7 +98,9 @@ int diso_forward_emit(diso_extractor* ex, const void* sdf, const void* deform, i
                       double isovalue, double padval, const uint64_t* seg, int normalize, void* verts,
                       int64_t* faces, uint64_t* edge_record, void* stream);
 
-/* The whole forward in one call: count, scan and emit into verts [vcap][3] and faces
+/* The whole forward in one call (CuMC::forward / CUDualMC::forward entire,
+ * src/cumc.cu:652-732, src/cudualmc.cu:1059-1128, with the Python layer's guard, pad
+ * and normalisation): count, scan and emit into verts [vcap][3] and faces
  * [fcap][3|4] (and edge_record, laid out for the actual counts; NULL without a
  * backward), synchronising the stream once at the end, so that the emit follows the
  * count on the GPU without a host round trip.  out->emitted = 1 when the outputs fitted
@@ -167,7 +172,8 @@ int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void*
                     void* stream, void* zero_stream);
 
 /* Share of diso_zero_grads' bytes that the count writes (the first bytes of
- * grad_sdf then grad_deform, laid end to end); the emit writes the rest. */
+ * grad_sdf then grad_deform, laid end to end); the emit writes the rest.  No
+ * counterpart in the reference. */
 double diso_zero_count_share(void);
 
 /* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
@@ -242,7 +248,8 @@ int diso_batch_backward(diso_extractor* ex, int normalize, int flags, const void
 /* ---------------------------------------------------------------- timing
  *
  * Optional timing of every kernel an extractor launches, for benchmarks: with
- * timing on, each launch is bracketed by CUDA events on its own stream. */
+ * timing on, each launch is bracketed by CUDA events on its own stream.  No
+ * counterpart in the reference, which times nothing. */
 typedef struct {
   char name[32];     /* count, scan, emit, zero_grads, zero_tiles, active_list, edge, gather, split */
   int64_t launches;
@@ -332,10 +339,13 @@ int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int cor
 int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
                   int64_t n_faces, int corners, void* body, void* stream);
 
-/* Message of the last failed call on this thread ("" if none). */
+/* Message of the last failed call on this thread ("" if none).  Replaces the
+ * reference's error paths: AT_ASSERTM / TORCH_INTERNAL_ASSERT on the inputs
+ * (src/pybind.cpp:5-11), which raise in Python, and CUDA errors that are printed and
+ * ignored (src/cumc.cu:68-78); here every failure is a status code with this message. */
 const char* diso_last_error(void);
 
-/* Library version string. */
+/* Library version string (no counterpart in the reference). */
 const char* diso_version(void);
 
 #ifdef __cplusplus
