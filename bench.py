@@ -447,6 +447,21 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: every rank's `ms` reduced with MAX over the job's
+    ranks (replicas: the job ends when its last rank does); no collective for one."""
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, steps, ms):
+    """Grids per second of the whole job: each of the `world` replicas runs `steps`
+    grids (weak scaling) within `ms`, the slowest rank's time."""
+    return world * steps / (ms / 1e3)
+
+
 def run_ours(args, rank, world, device):
     from diso_gb300 import DiffDMC
     from diso_gb300 import _native as N
@@ -491,11 +506,7 @@ def run_ours(args, rank, world, device):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1)
-    ms_t = torch.tensor([ms], device=device, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = max_over_ranks(t0.elapsed_time(t1), world, device)
     phases = ph.mean_ms()
 
     # e2e: every step's inputs are copied from pinned host memory and its loss is read
@@ -545,10 +556,7 @@ def run_ours(args, rank, world, device):
     e2e_run(e2e_steps)
     e1.record()
     torch.cuda.synchronize()
-    e_ms = torch.tensor([e0.elapsed_time(e1)], device=device, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(e_ms, op=torch.distributed.ReduceOp.MAX)
-    e_ms = float(e_ms.item())
+    e_ms = max_over_ranks(e0.elapsed_time(e1), world, device)
 
     # roofline of the dominant kernel (per-launch event times of the timed region)
     s_b = 4
@@ -566,7 +574,7 @@ def run_ours(args, rank, world, device):
     ms_step = ms_max / args.steps
     res = {
         "metric": METRIC,
-        "value": world * args.steps / (ms_max / 1e3),
+        "value": job_throughput(world, args.steps, ms_max),
         "unit": "grids/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -589,7 +597,7 @@ def run_ours(args, rank, world, device):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes": algo[dom],
                      "ms_per_launch": per_launch[dom], "traffic": traffic},
-        "e2e": {"value": world * e2e_steps / (e_ms / 1e3), "unit": "grids/s",
+        "e2e": {"value": job_throughput(world, e2e_steps, e_ms), "unit": "grids/s",
                 "h2d_bytes_per_step": int(sdf.numel() * 4 + deform.numel() * 4), "d2h_bytes_per_step": 4},
         "gpu_launches": sum(cnt for k, (cnt, _) in kernels.items() if k != "zero_grads"),
         "clocks": clk.summary(),
