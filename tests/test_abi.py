@@ -131,3 +131,45 @@ def test_isovalue_grad_checks_its_arguments(lib):
     assert lib.diso_isovalue_grad(h, ctypes.c_void_p(16), 4, 0, 4, None, out, None) == 1
     assert b"grid dims" in lib.diso_last_error()
     lib.diso_destroy(h)
+
+
+def _declarations():
+    """{name: (return type, [parameter declarations])} from the header."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*([a-z_0-9 ]+?[ \*]+)(diso_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", src, flags=re.M):
+        ret, name, params = m.groups()
+        ps = [] if params.strip() in ("", "void") else [p.strip() for p in params.split(",")]
+        out[name] = (ret.strip(), ps)
+    return out
+
+
+def _c_kind(decl):
+    decl = re.sub(r"\b(const|struct)\b", " ", decl)
+    if "*" in decl:
+        return "pointer"
+    return {"int": "int", "int64_t": "int64", "uint64_t": "int64", "double": "double", "void": "void"}[decl.split()[0]]
+
+
+def _ctypes_kind(t):
+    if t is None:
+        return "void"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return "pointer"
+    return {ctypes.c_int: "int", ctypes.c_int64: "int64", ctypes.c_uint64: "int64", ctypes.c_double: "double"}[t]
+
+
+def test_bindings_match_the_header_signatures():
+    # a binding whose argument list differs from the C declaration would pass
+    # garbage silently: every parameter's kind (pointer, int, int64, double) and the
+    # return kind must agree
+    from diso_gb300 import _native
+
+    decls = _declarations()
+    assert set(decls) == set(declared_functions())
+    for name, (ret, params) in decls.items():
+        restype, argtypes = _native.EXPORTS[name]
+        assert _ctypes_kind(restype) == _c_kind(ret), (name, "return", ret, restype)
+        assert len(argtypes) == len(params), (name, len(argtypes), len(params))
+        for i, (p, t) in enumerate(zip(params, argtypes)):
+            assert _ctypes_kind(t) == _c_kind(p), (name, i, p, t)
