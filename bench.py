@@ -399,22 +399,26 @@ class PhaseEvents:
         return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in self.done.items()}
 
 
-def kernel_bytes(vol, nseg, nv, nq, s, zshare):
-    """Algorithmic bytes of one launch of each kernel of the 512^3 DMC step: what the
+def kernel_bytes(vol, nseg, nv, nq, s, zshare, kernels, steps):
+    """Algorithmic bytes per launch of each kernel of the 512^3 DMC step: what the
     kernel's function must read and write at least (nq crossing edges = quads, nv
-    patches = vertices, s bytes per scalar).  The zeros of the two gradient arrays are
-    written by the count (the share zshare) and the emit (the rest), or by memsets
-    ("zero_grads") when the buffers do not allow it."""
+    patches = vertices, s bytes per scalar), from its bytes per step divided by its
+    launches per step (in recompute mode the count, the scan and the emit run once in
+    the forward and once more in the backward).  The zeros of the two gradient arrays
+    are written once per step, by the count (the share zshare) and the emit (the
+    rest), or by memsets ("zero_grads") when the buffers do not allow it."""
     zeros = vol * 4 * s
-    return {
-        # the SDF once; the scanned per-segment counts out; its share of the zeros
-        "count": vol * s + nseg * 8 + zshare * zeros,
+    per = {k: max(1, round(cnt / steps)) for k, (cnt, _) in kernels.items()}
+    k_count, k_scan, k_emit = per.get("count", 1), per.get("scan", 1), per.get("emit", 1)
+    step = {
+        # the SDF once per launch; the per-segment counts out; the count's share of the zeros
+        "count": k_count * (vol * s + nseg * 8) + zshare * zeros,
         # segment counts in and out
-        "scan": 2 * nseg * 8,
-        # both end points of every crossing edge (SDF + deform) in; vertices, quads and
-        # the edge record (cell + axis, four patch ids, a byte per vertex) out; the rest
-        # of the zeros
-        "emit": 2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8 + nq * (8 + 16) + nv + (1 - zshare) * zeros,
+        "scan": k_scan * 2 * nseg * 8,
+        # per launch both end points of every crossing edge (SDF + deform) in, vertices and
+        # quads out; once per step the edge record (cell + axis, four patch ids, a byte per
+        # vertex) and the rest of the zeros
+        "emit": k_emit * (2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8) + nq * (8 + 16) + nv + (1 - zshare) * zeros,
         "zero_grads": zeros,
         # per edge: record (cell, 4 patch ids), 4 patch bytes and 4 dL/dverts in, end points
         # (SDF + deform) in, 2 x 4 adjoints out
@@ -422,6 +426,7 @@ def kernel_bytes(vol, nseg, nv, nq, s, zshare):
         # the adjoints of every edge, once from each end
         "gather": nq * 8 * s,
     }
+    return {k: v / per.get(k, 1) for k, v in step.items()}
 
 
 def read_profile_traffic(kernel):
@@ -462,30 +467,21 @@ def job_throughput(world, steps, ms):
     return world * steps / (ms / 1e3)
 
 
-def run_ours(args, rank, world, device):
-    from diso_gb300 import DiffDMC
-    from diso_gb300 import _native as N
+def time_steps(ext, s, d, w, steps, warmup, world, with_clocks=False):
+    """`steps` timed forward + backward steps of `ext` on the resident inputs (after
+    `warmup` untimed ones), bracketed by barrier + synchronize; CUDA events around
+    every launch of the extractor (its timing mode) and around the phases.  Returns
+    (ms over all steps, max over ranks; per-kernel totals; phase means; clocks)."""
     import diso_gb300.extraction as X
 
-    n = args.n
-    sdf = spheres_field(n, device)
-    deform = deform_field(n, device)
-    ext = DiffDMC(torch.float32)
-    s = sdf.clone().requires_grad_(True)
-    d = deform.clone().requires_grad_(True)
-    v, f = ext(s, d, return_quads=True)
-    nv, nq = v.shape[0], f.shape[0]
-    w = loss_weights(nv, device, torch.float32)
-    del v, f
-
-    def step(s_in, d_in):
-        s_in.grad = None
-        d_in.grad = None
-        v, _ = ext(s_in, d_in, return_quads=True)
+    def step():
+        s.grad = None
+        d.grad = None
+        v, _ = ext(s, d, return_quads=True)
         (v * w).sum().backward()
 
-    for _ in range(args.warmup):
-        step(s, d)
+    for _ in range(warmup):
+        step()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -494,32 +490,95 @@ def run_ours(args, rank, world, device):
     X.phase_timer = ph
     ext._ex.timing(True)  # CUDA events around every launch of the extractor, on its stream
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(smi_id(device)) as clk:
+    clk = ClockSampler(smi_id(s.device)) if with_clocks else None
+    if clk:
+        clk.__enter__()
+    try:
         t0.record()
-        for _ in range(args.steps):
-            step(s, d)
+        for _ in range(steps):
+            step()
         t1.record()
         torch.cuda.synchronize()
-    X.phase_timer = None
+    finally:
+        if clk:
+            clk.__exit__()
+        X.phase_timer = None
     kernels = ext._ex.timing_read()
     ext._ex.timing(False)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    ms_max = max_over_ranks(t0.elapsed_time(t1), world, device)
-    phases = ph.mean_ms()
+    ms = max_over_ranks(t0.elapsed_time(t1), world, s.device)
+    return ms, kernels, ph.mean_ms(), (clk.summary() if clk else None)
 
-    # e2e: every step's inputs are copied from pinned host memory and its loss is read
-    # back.  The inputs are double-buffered: step k+1's copy runs on a copy stream
-    # while step k computes (every copy lies inside the timed region; the first one
-    # overlaps nothing)
+
+def peak_memory(ext, s, d, w):
+    """Device memory of one forward + backward step: the peak of torch's allocator
+    over the step (inputs, outputs, gradients, per-call records) plus the
+    extractor's own scratch, and what the forward keeps alive until its backward
+    beyond the inputs and the returned mesh."""
+    s.grad = None
+    d.grad = None
+    torch.cuda.synchronize()
+    base = torch.cuda.memory_allocated(s.device)
+    torch.cuda.reset_peak_memory_stats(s.device)
+    v, f = ext(s, d, return_quads=True)
+    loss = (v * w).sum()
+    torch.cuda.synchronize()
+    held = torch.cuda.memory_allocated(s.device) - base - v.numel() * v.element_size() - f.numel() * f.element_size()
+    loss.backward()
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated(s.device) + ext._ex.scratch_bytes()
+    del v, f, loss
+    return {"peak_hbm_gb": round(peak / 1e9, 4), "held_fwd_to_bwd_gb": round(max(held, 0) / 1e9, 4),
+            "extractor_scratch_gb": round(ext._ex.scratch_bytes() / 1e9, 4)}
+
+
+def run_ours(args, rank, world, device):
+    from diso_gb300 import DiffDMC
+    from diso_gb300 import _native as N
+
+    n = args.n
+    sdf = spheres_field(n, device)
+    deform = deform_field(n, device)
+    # the large configuration: the backward recomputes the crossing lists
+    ext = DiffDMC(torch.float32, recompute=True)
+    s = sdf.clone().requires_grad_(True)
+    d = deform.clone().requires_grad_(True)
+    v, f = ext(s, d, return_quads=True)
+    nv, nq = v.shape[0], f.shape[0]
+    w = loss_weights(nv, device, torch.float32)
+    del v, f
+
+    ms_max, kernels, phases, clocks = time_steps(ext, s, d, w, args.steps, args.warmup, world, with_clocks=True)
+    mem = peak_memory(ext, s, d, w)
+
+    # the same workload with the forward's edge record and gradient buffers kept for
+    # the backward (stored mode), for comparison
+    stored = DiffDMC(torch.float32)
+    ms_st, k_st, ph_st, _ = time_steps(stored, s, d, w, args.steps, args.warmup, world)
+    mem_st = peak_memory(stored, s, d, w)
+    del stored
+
+    # e2e: every step's inputs are copied from pinned host memory, and its mesh
+    # (verts, quads), both gradients and the loss are copied back into pinned host
+    # memory.  Inputs are double-buffered (step k+1's copy runs on a copy stream while
+    # step k computes), results go back on a third stream while the next step
+    # computes; every copy lies inside the timed region.
     e2e_steps = max(3, min(args.steps, args.e2e_steps))
     sdf_h = sdf.cpu().pin_memory()
     def_h = deform.cpu().pin_memory()
     bufs = [(torch.empty_like(sdf), torch.empty_like(deform)) for _ in range(2)]
+    out_h = [{"verts": torch.empty((nv, 3), dtype=torch.float32, pin_memory=True),
+              "quads": torch.empty((nq, 4), dtype=torch.int64, pin_memory=True),
+              "grad_sdf": torch.empty(sdf.shape, dtype=torch.float32, pin_memory=True),
+              "grad_deform": torch.empty(deform.shape, dtype=torch.float32, pin_memory=True)} for _ in range(2)]
     copy_stream = torch.cuda.Stream(device)
+    back_stream = torch.cuda.Stream(device)
     ready = [torch.cuda.Event(), torch.cuda.Event()]
     done = [torch.cuda.Event(), torch.cuda.Event()]  # the compute that read buffer i has finished
+    back_done = [torch.cuda.Event(), torch.cuda.Event()]  # host buffers i are free again
+    d2h = {"bytes": 0}
 
     def issue_copy(i):
         copy_stream.wait_event(done[i])
@@ -527,6 +586,21 @@ def run_ours(args, rank, world, device):
             bufs[i][0].copy_(sdf_h, non_blocking=True)
             bufs[i][1].copy_(def_h, non_blocking=True)
             ready[i].record(copy_stream)
+
+    def issue_back(i, tensors, cur):
+        back_stream.wait_event(back_done[i])
+        back_stream.wait_stream(cur)
+        nbytes = 0
+        with torch.cuda.stream(back_stream):
+            for name, t in tensors.items():
+                dst = out_h[i][name]
+                if dst.shape != t.shape:
+                    dst = out_h[i][name] = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                dst.copy_(t, non_blocking=True)
+                t.record_stream(back_stream)
+                nbytes += t.numel() * t.element_size()
+            back_done[i].record(back_stream)
+        d2h["bytes"] = nbytes
 
     def e2e_run(k_steps):
         cur = torch.cuda.current_stream(device)
@@ -541,11 +615,13 @@ def run_ours(args, rank, world, device):
             dg = bufs[i][1].requires_grad_(True)
             sg.grad = None
             dg.grad = None
-            v, _ = ext(sg, dg, return_quads=True)
+            v, q = ext(sg, dg, return_quads=True)
             loss = (v * w).sum()
             loss.backward()
+            issue_back(i, {"verts": v.detach(), "quads": q, "grad_sdf": sg.grad, "grad_deform": dg.grad}, cur)
             loss.item()
             done[i].record(cur)
+        back_stream.synchronize()
 
     e2e_run(2)
     torch.cuda.synchronize()
@@ -563,7 +639,7 @@ def run_ours(args, rank, world, device):
     vol = n ** 3
     nseg = (n + 1) ** 2 * ((n + 1 + 31) // 32)
     zshare = 0.0 if "zero_grads" in kernels else float(N.lib().diso_zero_count_share())
-    algo = kernel_bytes(vol, nseg, nv, nq, s_b, zshare)
+    algo = kernel_bytes(vol, nseg, nv, nq, s_b, zshare, kernels, args.steps)
     per_launch = {k: ms / max(cnt, 1) for k, (cnt, ms) in kernels.items()}
     ours = {k: v for k, v in per_launch.items() if k in algo and k != "zero_grads"}
     dom = max(ours, key=lambda k: ours[k] * kernels[k][0])
@@ -586,23 +662,76 @@ def run_ours(args, rank, world, device):
         "dtype": "f32",
         "data": "synthetic: min of 16 seeded spheres + 0.01*N(0,1) noise at 512^3, deform U(-0.45,0.45)",
         "config": {"workload": f"dmc_fwd_bwd_{n}_spheres16", "n": n, "method": "DiffDMC", "return_quads": True,
-                   "deform": True, "normalize": True, "verts": nv, "quads": nq,
+                   "deform": True, "normalize": True, "backward": "recompute", "verts": nv, "quads": nq,
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
                    "phase_ms": {k: round(v, 4) for k, v in phases.items()},
                    "kernel_ms_per_step": {k: round(ms / args.steps, 4) for k, (cnt, ms) in kernels.items()},
                    "kernel_gbs": {k: round(algo[k] / (per_launch[k] * 1e-3) / 1e9, 1) for k in per_launch
                                   if k in algo},
+                   "step_algorithmic_gb": round(step_bytes / 1e9, 4),
                    "step_algorithmic_gbs": step_bytes / (ms_step * 1e-3) / 1e9,
                    "step_hbm_frac": step_bytes / (ms_step * 1e-3) / 1e9 / peak},
+        "peak_hbm_gb": mem["peak_hbm_gb"],
+        "memory": mem,
+        "stored_mode": {"backward": "stored edge record", "ms_per_step": ms_st / args.steps,
+                        "grids_s": job_throughput(world, args.steps, ms_st),
+                        "step_hbm_frac": step_bytes / (ms_st / args.steps * 1e-3) / 1e9 / peak,
+                        "kernel_ms_per_step": {k: round(ms / args.steps, 4) for k, (cnt, ms) in k_st.items()},
+                        **mem_st},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes": algo[dom],
                      "ms_per_launch": per_launch[dom], "traffic": traffic},
         "e2e": {"value": job_throughput(world, e2e_steps, e_ms), "unit": "grids/s",
-                "h2d_bytes_per_step": int(sdf.numel() * 4 + deform.numel() * 4), "d2h_bytes_per_step": 4},
+                "h2d_bytes_per_step": int(sdf.numel() * 4 + deform.numel() * 4),
+                "d2h_bytes_per_step": int(d2h["bytes"]) + 4,
+                "d2h": "verts, quads, grad_sdf, grad_deform and the loss"},
         "gpu_launches": sum(cnt for k, (cnt, _) in kernels.items() if k != "zero_grads"),
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     return res
+
+
+# ----------------------------------------------------------------------------- reference CUDA
+def run_reference_cuda(args, device):
+    """The reference's own DiffDMC forward + backward on the same field, through its
+    unmodified Python API over its CUDA extension, built from a reference checkout
+    named by the environment variable DISO_REFERENCE_SRC (the recipe in oracle/ builds
+    it into oracle/_ref/).  Without a checkout on this machine the entry says so."""
+    src = os.environ.get("DISO_REFERENCE_SRC")
+    if not src or not os.path.exists(os.path.join(src, "src", "cudualmc.cu")):
+        return {"unavailable": "no reference checkout on this machine (set DISO_REFERENCE_SRC to one to time "
+                               "the reference's CUDA path here)"}
+    try:
+        from oracle.build_ref import load_reference
+
+        ref = load_reference(src)
+        n = args.n
+        s = spheres_field(n, device).requires_grad_(True)
+        d = deform_field(n, device).requires_grad_(True)
+        ext = ref.DiffDMC(dtype=torch.float32)
+        v, _ = ext(s, d, return_quads=True)
+        w = loss_weights(v.shape[0], device, torch.float32)
+
+        def step():
+            s.grad = None
+            d.grad = None
+            v, _ = ext(s, d, return_quads=True)
+            (v * w).sum().backward()
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            step()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        return {"ms_per_step": ms, "grids_s": 1e3 / ms, "steps": args.steps, "warmup": args.warmup,
+                "source": "reference DiffDMC (its own Python API and CUDA extension, built for sm_103a)"}
+    except Exception as e:  # report, but keep the headline line
+        return {"unavailable": f"reference build or run failed: {repr(e)[:200]}"}
 
 
 # ----------------------------------------------------------------------------- CPU
@@ -654,7 +783,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
-    ap.add_argument("--requests", type=int, default=2000, help="served-trace length (20000 for the full trace)")
+    ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -664,8 +793,10 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps, warmup = max(1, min(args.steps, 3)), max(1, min(args.warmup, 1))
-        value, planes, cores, sec = run_cpu(args, steps, warmup, budget_s=20.0)
+        steps, warmup = args.steps, args.warmup
+        # each step a bounded sample, sized so that the whole run stays within ~3 minutes
+        budget = min(20.0, max(0.1, 180.0 / max(1, steps + warmup)))
+        value, planes, cores, sec = run_cpu(args, steps, warmup, budget_s=budget)
         out = {"metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": args.gpus, "steps": steps,
                "warmup": warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (same field as ours)",
@@ -685,6 +816,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     device = torch.device("cuda", torch.cuda.current_device())
     res = run_ours(args, rank, world, device)
+    if rank == 0:
+        res["reference_cuda"] = run_reference_cuda(args, device)
     if rank == 0 and world == 1 and not args.no_batched:
         for name, fn in (("batched_mc", lambda: run_batched(device, 0)), ("batched_dmc", lambda: run_batched(device, 1)),
                          ("served", lambda: run_served(device, args.requests)),

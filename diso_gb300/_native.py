@@ -103,6 +103,7 @@ EXPORTS = {
     "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),
+    "diso_scratch_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "diso_last_error": (ctypes.c_char_p, []),
     "diso_version": (ctypes.c_char_p, []),
 }
@@ -191,6 +192,10 @@ class Extractor:
         check(lib().diso_forward_count(self._h, ptr(sdf), *sdf.shape, iso, pad, ptr(seg),
                                        stream_of(sdf.device), ctypes.byref(c)), "forward count")
         return c
+
+    def scratch_bytes(self) -> int:
+        """Device bytes held by this extractor's own scratch buffers."""
+        return int(lib().diso_scratch_bytes(self._h))
 
     def timing(self, enable: bool):
         """Time every kernel this extractor launches (CUDA events on each launch's stream)."""

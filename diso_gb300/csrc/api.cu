@@ -1453,6 +1453,19 @@ int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n)
   return DISO_OK;
 }
 
+int64_t diso_scratch_bytes(const diso_extractor* ex) {
+  if (!ex) return 0;
+  int64_t b = ex->active_cap * (int64_t)sizeof(int) + ex->codes_cap * (int64_t)sizeof(CellRec) +
+              ex->plist_cap * (int64_t)sizeof(int) + ex->split_cap * (int64_t)sizeof(uint64_t) + ex->mesh_cap +
+              ex->isog_cap * (int64_t)sizeof(double) +
+              ex->scan_cap * (int64_t)(sizeof(uint32_t) + 2 * sizeof(uint64_t));
+  if (ex->stats) b += (int64_t)sizeof(Stats) + (int64_t)sizeof(unsigned);
+  if (ex->bdesc)
+    b += (int64_t)(sizeof(BatchGrid<double>) * MAX_BATCH + sizeof(Stats) * MAX_BATCH +
+                   sizeof(uint64_t) * (MAX_BATCH + 1) + sizeof(int64_t) * (MAX_BATCH + 1));
+  return b;
+}
+
 const char* diso_last_error(void) { return g_err; }
 
 const char* diso_version(void) { return "diso_gb300 0.1.0 (sm_103a)"; }
@@ -1564,11 +1577,15 @@ int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, in
 // the scan) lives in one file-scope device array instead of buffers owned by an
 // extractor.  Host code cannot use the array's name as a device address, so at
 // the first call on each device (with that device current) the address is looked
-// up with cudaGetSymbolAddress and cached.
+// up with cudaGetSymbolAddress and cached, keyed by the device's current context:
+// a context made again after cudaDeviceReset gets a fresh lookup.
 namespace {
 
 constexpr int64_t kStaticMaxTiles = 65536;      // 4x8x32-cell tiles of one grid
-constexpr int64_t kStaticMaxScanTiles = 2048;   // look-back tiles of 2048 segments
+// look-back tiles of SCAN_TILE (512 x 16 = 8192) segments each.  A grid of at most
+// kStaticMaxTiles tiles has at most 65536 x 32 row segments (2.1M), i.e. about 256
+// scan tiles, so the tile limit above is the one that applies.
+constexpr int64_t kStaticMaxScanTiles = 2048;
 
 struct StaticScratch {
   Stats stats;
@@ -1583,12 +1600,33 @@ __device__ __align__(256) unsigned char g_static_scratch[sizeof(StaticScratch)];
 constexpr int kStaticMaxDevices = 64;
 std::mutex g_static_mu;
 StaticScratch* g_static_ptr[kStaticMaxDevices] = {};
+void* g_static_ctx[kStaticMaxDevices] = {};    // the context the cached address belongs to
 int g_static_ctas[kStaticMaxDevices][4] = {};  // resident count-kernel CTAs per (method, dtype)
+
+// the calling thread's current driver context (cuCtxGetCurrent, looked up once)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+void* current_context() {
+  static std::once_flag once;
+  static CtxGetCurrentFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (CtxGetCurrentFn)p;
+  });
+  CUcontext c = nullptr;
+  if (fn && fn(&c) != CUDA_SUCCESS) c = nullptr;
+  return (void*)c;
+}
 
 int static_setup(int dev, StaticScratch** out, int method, int dtype, int* ctas) {
   if (dev < 0 || dev >= kStaticMaxDevices) return fail(DISO_ERR_ARG, "device %d out of range", dev);
   std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_ptr[dev]) {
+  // (before the thread's first runtime call no context may be current yet: the
+  // lookup below makes the primary context current, and the key is read after it)
+  void* ctx = current_context();
+  if (!g_static_ptr[dev] || !ctx || g_static_ctx[dev] != ctx) {
     void* p = nullptr;
     CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
     int sms = 0;
@@ -1600,6 +1638,7 @@ int static_setup(int dev, StaticScratch** out, int method, int dtype, int* ctas)
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[3], count_kernel<double, DMC>, NTHREADS, 0));
     for (int k = 0; k < 4; ++k) g_static_ctas[dev][k] = sms * std::max(per[k], 1);
     g_static_ptr[dev] = (StaticScratch*)p;
+    g_static_ctx[dev] = current_context();
   }
   *out = g_static_ptr[dev];
   *ctas = g_static_ctas[dev][2 * dtype + method];

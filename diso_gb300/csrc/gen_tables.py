@@ -31,7 +31,8 @@ Table contents:
   mod 3 in the cyclic order (0,0) (-1,0) (-1,-1) (0,-1) when the edge enters
   (value rises through iso from its start point), and reversed when it exits.
 
-Run ``python gen_tables.py`` (optionally ``--reference DIR``) to rewrite the header,
+Run ``python gen_tables.py`` (optionally ``--reference DIR``; by default the checkout
+named by the environment variable DISO_REFERENCE_SRC, if any) to rewrite the header,
 ``python gen_tables.py --check`` to compare the committed header with a fresh
 derivation (the MC words are compared only when the reference source is present).
 """
@@ -44,7 +45,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 HEADER = os.path.join(HERE, "case_tables.h")
-DEFAULT_REFERENCE = "/root/reference"
+# a reference checkout, when one is on this machine (None otherwise)
+DEFAULT_REFERENCE = os.environ.get("DISO_REFERENCE_SRC")
 
 MC_CORNERS = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0),
               (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
@@ -258,7 +260,7 @@ def main(argv=None):
     ap.add_argument("--reference", default=DEFAULT_REFERENCE)
     ap.add_argument("--check", action="store_true")
     args = ap.parse_args(argv)
-    have_ref = os.path.exists(os.path.join(args.reference, "src", "cumc.cu"))
+    have_ref = bool(args.reference) and os.path.exists(os.path.join(args.reference, "src", "cumc.cu"))
     if have_ref:
         mc = mc_words_from_reference(args.reference)
     else:

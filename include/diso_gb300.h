@@ -177,22 +177,25 @@ int diso_zero_grads(diso_extractor* ex, void* grad_sdf, int64_t sdf_bytes, void*
 double diso_zero_count_share(void);
 
 /* Forward phase 1 (as diso_forward_count) for callers that cannot allocate
- * device memory: code running while a stream is being captured, where cudaMalloc
- * is not allowed, and serving processes that fix their device memory at start-up
- * and may not grow it per request.  No counterpart in the reference.
+ * device memory: serving processes that reserve all their device memory at
+ * start-up and may not grow it per request, and hosts that embed the library
+ * under a memory manager of their own, where a cudaMalloc inside a request could
+ * fail or stall.  No counterpart in the reference.
  *
  * It takes no extractor: its scratch (status words, active-tile list, scan state,
  * about 300 KB) is one static device array of this library, which every GPU that
  * loads the library holds until the process exits.  Nothing is allocated: no
- * cudaMalloc / cudaFree / cudaMallocHost.  Grids of at most 65536 4x8x32-cell tiles
- * (about 384^3; more precisely also at most 2048 x 2048 - 1 row segments) are
- * accepted, larger ones fail with DISO_ERR_ARG and a message.  The first call on a
- * device looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array: calls whose GPU work overlaps (other
- * streams, other threads) race and must be serialised by the caller.  `seg` and
- * the result have the meaning they have for diso_forward_count (diso_forward_emit
- * then needs an extractor that ran diso_forward_count; diso_backward can use this
- * `seg` directly). */
+ * cudaMalloc / cudaFree / cudaMallocHost.  Grids of at most 65536 4x8x32-cell
+ * tiles (about 384^3) are accepted, larger ones fail with DISO_ERR_ARG and a
+ * message.  The call copies the counts to the host and synchronises `stream`
+ * before it returns.  The first call on a device (and the first after that
+ * device's context was made again) looks up the array's device address.  All
+ * calls share the array: calls whose GPU work overlaps (other streams, other
+ * threads) race and must be serialised by the caller.  `seg` and the result have
+ * the meaning they have for diso_forward_count.  A `seg` from this call alone does
+ * not feed diso_forward_emit or diso_backward: those need an extractor on which
+ * diso_forward_count (or diso_forward) ran for the same grid, and the backward
+ * also the edge record of that extractor's emit. */
 int diso_forward_count_static(int method, int dtype, const void* sdf, int nx, int ny, int nz, double isovalue,
                               double padval, uint64_t* seg, void* stream, diso_counts* out);
 
@@ -338,6 +341,11 @@ int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int cor
  * "end_header") is the caller's. */
 int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
                   int64_t n_faces, int corners, void* body, void* stream);
+
+/* Bytes of device memory the extractor holds as its own scratch (grow-only
+ * buffers; not the caller's per-call `seg`, edge record or outputs), for memory
+ * reports.  No counterpart in the reference. */
+int64_t diso_scratch_bytes(const diso_extractor* ex);
 
 /* Message of the last failed call on this thread ("" if none).  Replaces the
  * reference's error paths: AT_ASSERTM / TORCH_INTERNAL_ASSERT on the inputs

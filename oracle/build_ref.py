@@ -11,6 +11,7 @@ fixtures under tests/golden/ (see tests/golden/make_golden.py); nothing in the
 GPU tests, smoke() or bench.py loads it.
 
 Usage:  python oracle/build_ref.py --src <reference checkout>
+(default: the checkout named by the environment variable DISO_REFERENCE_SRC)
 """
 from __future__ import annotations
 
@@ -21,7 +22,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference"
+DEFAULT_SRC = os.environ.get("DISO_REFERENCE_SRC")
 
 
 def _torch_flags():
@@ -43,6 +44,8 @@ def build(src: str = DEFAULT_SRC, verbose: bool = False):
     """Compile the three reference sources into oracle/_ref/_C.so and import it."""
     import subprocess
 
+    if not src:
+        raise RuntimeError("no reference checkout given (pass src or set DISO_REFERENCE_SRC)")
     os.makedirs(OUT, exist_ok=True)
     so = os.path.join(OUT, "_C.so")
     srcs = [os.path.join(src, "src", f) for f in ("pybind.cpp", "cumc.cu", "cudualmc.cu")]
@@ -91,7 +94,7 @@ def load_reference(src: str = DEFAULT_SRC):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default=DEFAULT_SRC)
+    ap.add_argument("--src", default=DEFAULT_SRC, required=DEFAULT_SRC is None)
     args = ap.parse_args()
     m = build(args.src, verbose=True)
     print("built", m.__file__, [n for n in dir(m) if n.startswith("CU")])

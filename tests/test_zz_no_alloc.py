@@ -1,6 +1,7 @@
 """diso_forward_count_static: the forward count phase for callers that cannot
-allocate device memory (code inside a stream capture, where cudaMalloc is not
-allowed, or serving processes whose device memory is fixed at start-up).
+allocate device memory (serving processes whose device memory is reserved at
+start-up and may not grow per request, or hosts whose own memory manager owns
+the device).
 
 Called through the C ABI and checked against diso_forward_count on the same
 inputs, twice in a row, because every call reuses the same static scratch
@@ -31,17 +32,19 @@ def _counts_tuple(c):
     return (c.n_verts, c.n_faces, c.sdf_min, c.sdf_max, c.empty, c.n_active_tiles)
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("method", [0, 1])
-def test_static_count_matches_extractor_count_twice(cuda_device, method):
+def test_static_count_matches_extractor_count_twice(cuda_device, method, dtype):
     from diso_gb300 import _native as N
 
     lib = N.lib()
-    ex = N.Extractor(method, torch.float32)
+    ex = N.Extractor(method, dtype)
     stream = N.stream_of(cuda_device)
+    np_dtype = np.float32 if dtype == torch.float32 else np.float64
     # two different grids in a row: the second call must not see the first one's state
     for shape, seed in [((70, 45, 90), 1), ((33, 64, 17), 2)]:
-        g = torch.tensor(_field(shape, seed).astype(np.float32), device=cuda_device)
-        iso, pad = N.iso_values(0.0, torch.float32)
+        g = torch.tensor(_field(shape, seed).astype(np_dtype), device=cuda_device)
+        iso, pad = N.iso_values(0.0, dtype)
         slots = N.Extractor.segment_slots(g.shape)
         # the record is the scanned segment counts, their total and one activity byte per
         # tile; the bytes that pad the last slot are not written, so both start equal
@@ -49,8 +52,8 @@ def test_static_count_matches_extractor_count_twice(cuda_device, method):
         ref = ex.count(g, iso, pad, seg_ref)
         seg = torch.full((slots,), -1, dtype=torch.int64, device=cuda_device)
         out = N.Counts()
-        rc = lib.diso_forward_count_static(method, N.F32, N.ptr(g), *g.shape, iso, pad, N.ptr(seg), stream,
-                                           ctypes.byref(out))
+        rc = lib.diso_forward_count_static(method, N.dtype_tag(dtype), N.ptr(g), *g.shape, iso, pad, N.ptr(seg),
+                                           stream, ctypes.byref(out))
         assert rc == 0, lib.diso_last_error()
         torch.cuda.synchronize()
         # integer outputs: exact (the tolerance of every count and index in this suite)
