@@ -74,6 +74,10 @@ EXPORTS = {
                                      ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_backward_recompute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_isovalue_grad": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_forward_count_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
@@ -287,6 +291,17 @@ class Extractor:
         check(lib().diso_backward(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg), ptr(record),
                                   int(bool(normalize)), flags, ptr(grad_verts), ptr(grad_sdf),
                                   ptr(grad_deform), stream_of(sdf.device)), "backward")
+
+    def backward_recompute(self, sdf, deform, iso, pad, seg, normalize, grad_verts, grad_sdf, grad_deform,
+                           exact=False):
+        """Backward of a forward that kept only its segment record: every element of
+        grad_sdf (and grad_deform) is written (see diso_backward_recompute); the
+        zeros that the extractor's second stream writes are joined into the caller's
+        stream before the call returns its work to it."""
+        flags = GRAD_EXACT if exact else 0
+        check(lib().diso_backward_recompute(self._h, ptr(sdf), ptr(deform), *sdf.shape, iso, pad, ptr(seg),
+                                            int(bool(normalize)), flags, ptr(grad_verts), ptr(grad_sdf),
+                                            ptr(grad_deform), stream_of(sdf.device)), "backward (recompute)")
 
     def isovalue_grad(self, grad_sdf, seg=None):
         """dL/d(isovalue) = -(sum of dL/dsdf), as a 0-dim float64 tensor on the

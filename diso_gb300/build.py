@@ -8,7 +8,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libdiso_gb300.so")
 SOURCES = [os.path.join(CSRC, "api.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("common.cuh", "fields.cuh", "kernels.cuh", "mesh.cuh", "scan.cuh", "tma.cuh", "case_tables.h")] + [
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("backward.cuh", "common.cuh", "fields.cuh", "kernels.cuh", "mesh.cuh", "scan.cuh", "tma.cuh", "case_tables.h")] + [
     os.path.join(os.path.dirname(HERE), "include", "diso_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/diso_gb300.h"
+#include "backward.cuh"
 #include "fields.cuh"
 #include "kernels.cuh"
 #include "mesh.cuh"
@@ -40,10 +41,11 @@ int fail(int code, const char* fmt, ...) {
 
 // kernels timed by diso_timing
 enum KernelId {
-  K_COUNT, K_SCAN, K_EMIT, K_ZERO_GRADS, K_ZERO_TILES, K_ACTIVE_PTILES, K_EDGE, K_GATHER, K_SPLIT, K_NKERNELS
+  K_COUNT, K_SCAN, K_EMIT, K_ZERO_GRADS, K_ZERO_TILES, K_ACTIVE_PTILES, K_EDGE, K_GATHER, K_SPLIT, K_FUSED_BWD,
+  K_NKERNELS
 };
 static const char* const kKernelNames[K_NKERNELS] = {"count",       "scan", "emit",   "zero_grads", "zero_tiles",
-                                                      "active_list", "edge", "gather", "split"};
+                                                      "active_list", "edge", "gather", "split",     "fused_bwd"};
 
 struct diso_extractor {
   int method = 0, dtype = 0, device = -1;
@@ -74,6 +76,7 @@ struct diso_extractor {
   int tma_ctas = 0;              // the same for the TMA count kernel
   int gather_ctas = 0;           // the same for the point gather
   int emit_ctas = 0;             // the same for the emit
+  int fused_ctas = 0;            // the same for the fused backward
   int sms = 0;
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -308,6 +311,14 @@ int bind_device(diso_extractor* ex) {
           &per_e, ex->method == DISO_MC ? (const void*)mc_emit_kernel<double> : (const void*)dmc_emit_kernel<double>,
           NTHREADS, 0));
     ex->emit_ctas = sms * std::max(per_e, 1);
+    int per_f = 0;
+    const void* fk = ex->dtype == DISO_F32
+                         ? (ex->method == DISO_MC ? (const void*)fused_backward_kernel<float, MC>
+                                                  : (const void*)fused_backward_kernel<float, DMC>)
+                         : (ex->method == DISO_MC ? (const void*)fused_backward_kernel<double, MC>
+                                                  : (const void*)fused_backward_kernel<double, DMC>);
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, fk, NTHREADS, 0));
+    ex->fused_ctas = sms * std::max(per_f, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
@@ -620,6 +631,47 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   }
   CUDA_TRY(cudaGetLastError());
   return zeroed ? DISO_OK : side_join(ex, s);
+}
+
+// the backward of a forward that kept only its segment record (backward.cuh): the
+// zeros of the point tiles with no crossing nearby on the second stream, the fused
+// pass over the list of the others on `s`
+template <class S>
+int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz, double iso,
+                   double padval, const uint64_t* seg, int normalize, int flags, const void* gv, void* gsdf,
+                   void* gdef, cudaStream_t s) {
+  Geom g;
+  g.init(nx, ny, nz);
+  Field<S> f = make_field<S>(sdf, deform, nx, ny, nz, iso, padval);
+  const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  int rc;
+  if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
+  // few zero CTAs per SM, so that the fused pass over the active tiles finds room beside them
+  if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
+  {
+    KernelTimer kt(ex, K_ZERO_TILES, ex->side);
+    zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf,
+                                                                       (S*)gdef);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
+  {
+    KernelTimer kt(ex, K_ACTIVE_PTILES, s);
+    active_ptiles_kernel<<<stride_ctas(g.nptiles(), ex->sms * 8), 256, 0, s>>>(g, tile_flags(seg, g), ex->plist,
+                                                                               ex->plist_n);
+  }
+  CUDA_TRY(cudaGetLastError());
+  {
+    KernelTimer kt(ex, K_FUSED_BWD, s);
+    if (ex->method == DISO_MC)
+      fused_backward_kernel<S, MC><<<(unsigned)ex->fused_ctas, NTHREADS, 0, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gsdf, (S*)gdef, ex->stats);
+    else
+      fused_backward_kernel<S, DMC><<<(unsigned)ex->fused_ctas, NTHREADS, 0, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return side_join(ex, s);
 }
 
 // the zeros as memsets on stream z, after the work queued on s so far
@@ -1317,6 +1369,22 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                                : backward<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg, edge_record,
                                                   normalize, flags, grad_verts, grad_sdf,
                                                   deform ? grad_deform : nullptr, s);
+}
+
+int diso_backward_recompute(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
+                            double isovalue, double padval, const uint64_t* seg, int normalize, int flags,
+                            const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream) {
+  if (!seg || !grad_sdf) return fail(DISO_ERR_ARG, "null seg or grad_sdf");
+  if (!grad_verts) return fail(DISO_ERR_ARG, "null grad_verts");
+  if (deform && !grad_deform) return fail(DISO_ERR_ARG, "deform given without grad_deform");
+  int rc = check_common(ex, sdf, nx, ny, nz);
+  if (rc != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  void* gd = deform ? grad_deform : nullptr;
+  return ex->dtype == DISO_F32 ? backward_fused<float>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg,
+                                                        normalize, flags, grad_verts, grad_sdf, gd, s)
+                               : backward_fused<double>(ex, sdf, deform, nx, ny, nz, isovalue, padval, seg,
+                                                         normalize, flags, grad_verts, grad_sdf, gd, s);
 }
 
 int diso_isovalue_grad(diso_extractor* ex, const void* grad_sdf, int nx, int ny, int nz, const uint64_t* seg,

@@ -1,0 +1,356 @@
+// Backward of a forward that kept only its segment record: one pass over the point
+// tiles near the surface that writes every gradient element there once.
+//
+// The reference's backward runs its forward again to rebuild the crossing lists
+// (diso/__init__.py:32-37, 86-91) and then scatters each vertex's gradient with
+// atomics (adj_create_cell_mc_verts_kernel, src/cumc.cu:474-512;
+// adj_create_dmc_verts_kernel, src/cudualmc.cu:957-1005).  Here nothing of the
+// crossing lists is kept either, but they are recomputed per point tile in shared
+// memory instead of as a second forward:
+//
+//   * the tile's point rows and a halo become row masks (one ballot per row);
+//   * the crossing edges that touch the tile's points (those owned by the window
+//     cells [X0, X0+TX] x [Y0, Y0+TY] x [Z0, Z0+TZ]) get window slots;
+//   * MC: an edge's vertex id is the scanned crossing count of its segment (the
+//     forward's record) plus its rank inside the segment;
+//     DMC: the cells around the window edges ([X0-1, X0+TX] x [Y0-1, Y0+TY] x
+//     [Z0-1, Z0+TZ]) get their codes after the ambiguity test and their first
+//     patch id (the segment's scanned patch count plus an in-segment prefix), from
+//     which each edge's four patches and their edge counts follow;
+//   * each window edge's adjoint at both end points is computed once into shared
+//     memory (the same arithmetic, in the same order, as the stored backward's edge
+//     pass), and each point adds the adjoints of its at most six edges in a fixed
+//     order: deterministic and bit-identical to the stored backward;
+//   * point tiles with no crossing nearby (the forward's tile bits) only get zeros,
+//     written by another kernel on a second stream while this one runs.
+//
+// Tiles whose window holds more crossing edges than the shared-memory cache compute
+// each edge's adjoint at both of its end points instead.
+#pragma once
+#include "kernels.cuh"
+
+namespace diso {
+
+constexpr int FB_ADJ_BYTES = 16384;  // shared memory for the window edges' adjoints
+template <class S>
+__host__ __device__ constexpr int fb_cap() {
+  return FB_ADJ_BYTES / (8 * (int)sizeof(S));
+}
+
+template <class S, int METHOD>
+struct FusedShared {
+  static constexpr int LO = METHOD == DMC ? 1 : 0;  // mask rows start at (X0 - LO, Y0 - LO)
+  static constexpr int WX = TX + 2 + LO, WY = TY + 2 + LO;
+  static constexpr int CX = TX + 1, CY = TY + 1;  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
+  static constexpr int KX = METHOD == DMC ? TX + 2 : 1, KY = METHOD == DMC ? TY + 2 : 1;  // DMC window cell rows
+  uint64_t m[WX][WY];
+  RowBits wb[CX][CY];
+  uint32_t eb[CX][CY][2];          // scanned crossing counts of chunks zc, zc + 1 (MC vertex ids)
+  uint32_t pb[KX][KY][2];          // scanned patch counts of chunks zc, zc + 1 (DMC)
+  uint16_t wcell[CX][CY][TZ + 1];  // per edge-row cell: its first window slot | crossing flags << 13
+  uint16_t witems[fb_cap<S>()];
+  uint8_t w32[CX][CY];
+  uint8_t rc[KX][KY][TZ + 2];     // DMC window cells (z index j + 1 for Z0 + j): code after the ambiguity test
+  int32_t first[KX][KY][TZ + 2];  //   and the id of its first patch
+  uint32_t wsum[NTHREADS / 32 + 1];
+  uint32_t nwi;
+  __align__(16) S adj[fb_cap<S>()][8];
+};
+
+// The gradient reaching the lerp vertex of window edge (x, y, j, a) (owner cell
+// (X0 + x, Y0 + y, Z0 + j), x in [0, TX], y in [0, TY], j in [0, TZ]), in padded
+// coordinates (the chain rule of the shift and the normalisation in `scale`), as
+// the stored backward's edge pass forms it (edge_adjoint_at in kernels.cuh).
+template <class S, int METHOD>
+__device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh, int x, int y, int j, int a,
+                                                const S* __restrict__ gv, int64_t V, const S scale[3], int exact,
+                                                S gvec[3], bool& bad) {
+  if constexpr (METHOD == MC) {
+    // the edge's vertex: the scanned crossings of its segment, then the crossings
+    // of the cells before it in the segment, then its axes before a
+    const int fl = sh.wcell[x][y][j] >> 13;
+    int64_t v;
+    if (j == TZ) {
+      v = (int64_t)sh.eb[x][y][1] + __popc(fl & ((1 << a) - 1));
+    } else {
+      v = (int64_t)sh.eb[x][y][0] + row_prefix(sh.wb[x][y], j) + __popc(fl & ((1 << a) - 1));
+    }
+    if (v >= V) {
+      bad = true;
+      v = 0;
+    }
+    load_grad<S>(gv, v, scale, gvec);
+  } else {
+    // the four cells around the edge, one step back by db along axis b = a + 1 and
+    // dc along c = a + 2, in the order db + 2 dc; in each the edge starts at the
+    // cell's corner (db along b, dc along c)
+    const int b = a == 2 ? 0 : a + 1, c = a == 0 ? 2 : a - 1;
+    gvec[0] = gvec[1] = gvec[2] = S(0);
+#pragma unroll
+    for (int at = 0; at < 4; ++at) {
+      const int db = at & 1, dc = at >> 1;
+      const int wx = x + 1 - (b == 0 ? db : 0) - (c == 0 ? dc : 0);
+      const int wy = y + 1 - (b == 1 ? db : 0) - (c == 1 ? dc : 0);
+      const int wj = j + 1 - (b == 2 ? db : 0) - (c == 2 ? dc : 0);
+      const int s = (db << b) | (dc << c);
+      const int e = __ldg(g_edge_of + 3 * s + a);
+      const int rc = sh.rc[wx][wy][wj];
+      const int q = dmc_patch_of(dmc_case(rc), e);
+      const int cnt = __popc((uint32_t)(__ldg(&g_dmc_pmask.m[rc]) >> (12 * q)) & 0xfffu);
+      int64_t p = (int64_t)sh.first[wx][wy][wj] + (exact ? q : 0);
+      if (p < 0 || p >= V || cnt == 0) {
+        bad = true;
+        p = 0;
+      }
+      S v[3];
+      load_grad<S>(gv, p, scale, v);
+      const S inv = recip<S>(cnt);
+      gvec[0] = fma_rn(v[0], inv, gvec[0]);
+      gvec[1] = fma_rn(v[1], inv, gvec[1]);
+      gvec[2] = fma_rn(v[2], inv, gvec[2]);
+    }
+  }
+}
+
+// adjoints (c0 at the edge's first point, c1 at its second) of window edge (x, y, j, a)
+template <class S, int METHOD>
+__device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
+                                                   int Y0, int Z0, int x, int y, int j, int a,
+                                                   const S* __restrict__ gv, int64_t V, const S scale[3], int exact,
+                                                   S c0[4], S c1[4], bool& bad) {
+  S gvec[3];
+  fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
+  edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
+}
+
+// the uncached path's per-point call, kept out of line (it runs only for tiles with
+// more window edges than the cache holds): adds the adjoint at end k of window
+// edge (x, y, j, a) to acc
+template <class S, int METHOD>
+__device__ __noinline__ void fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
+                                                    int Y0, int Z0, int x, int y, int j, int a,
+                                                    const S* __restrict__ gv, int64_t V, const S* scale, int exact,
+                                                    int k, S* acc, bool* bad) {
+  S c0[4], c1[4];
+  bool b = false;
+  fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, b);
+  const S* o = k ? c1 : c0;
+  acc[0] += o[0];
+  acc[1] += o[1];
+  acc[2] += o[2];
+  acc[3] += o[3];
+  if (b) *bad = true;
+}
+
+// one active point tile (see the top of this file)
+template <class S, int METHOD>
+__device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+                                           const uint64_t* __restrict__ seg, int64_t ptile, const S* __restrict__ gv,
+                                           int64_t V, const S scale[3], int exact, S* __restrict__ gsdf,
+                                           S* __restrict__ gdef, bool& bad) {
+  using SH = FusedShared<S, METHOD>;
+  constexpr int LO = SH::LO, CX = SH::CX, CY = SH::CY, KX = SH::KX, KY = SH::KY;
+  constexpr int CAP = fb_cap<S>();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int X0, Y0, Z0;
+  ptile_coords(ptile, g, X0, Y0, Z0);
+  const int zc = Z0 / TZ;
+  // segment values first, so that their loads overlap the mask loads: MC, the
+  // crossing counts of the edge rows; DMC, the patch counts of the window cell rows
+  constexpr int RY = METHOD == MC ? CY : KY;
+  constexpr int NSV = (METHOD == MC ? CX * CY : KX * KY) * 2;
+  static_assert(NSV <= NTHREADS, "one segment value per thread");
+  uint64_t sv = 0;
+  const int si = threadIdx.x, sk = si & 1, sy = (si >> 1) % RY, sx = (si >> 1) / RY;
+  if (si < NSV) {
+    const int X = X0 - LO + sx, Y = Y0 - LO + sy, c = zc + sk;
+    if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && c < g.nzc) sv = seg[g.seg(X, Y, c)];
+  }
+  S dmn, dmx;
+  bool dseen = false;
+  load_masks<S, SH::WX, SH::WY, false>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
+  if (si < NSV) {
+    if constexpr (METHOD == MC)
+      sh.eb[sx][sy][sk] = Counts::lo(sv);
+    else
+      sh.pb[sx][sy][sk] = Counts::hi(sv);
+  }
+  __syncthreads();
+  // edge rows: crossing bits and the crossing flags of cell Z0 + TZ, one warp per row
+  const uint32_t valid = zvalid(g, Z0);
+  for (int r = warp; r < CX * CY; r += NTHREADS / 32) {
+    const int x = r / CY, y = r % CY;
+    RowBits rw = {0u, 0u, 0u, 0u};
+    int f32 = 0;
+    if (X0 + x < g.c[0] && Y0 + y < g.c[1]) {
+      const uint64_t ma = sh.m[x + LO][y + LO], mb = sh.m[x + 1 + LO][y + LO], mc = sh.m[x + LO][y + 1 + LO],
+                     md = sh.m[x + 1 + LO][y + 1 + LO];
+      rw = row_bits(ma, mb, mc, md, valid);
+      if (Z0 + TZ < g.c[2]) f32 = flags_at(ma, mb, mc, TZ + 1);
+    }
+    if (lane == 0) {
+      sh.wb[x][y] = rw;
+      sh.w32[x][y] = (uint8_t)f32;
+    }
+  }
+  if constexpr (METHOD == DMC) {
+    // window cells: codes after the ambiguity test and first patch ids, one warp per
+    // cell row; lane j takes cell Z0 + j, lane 0 also cell Z0 - 1, lane 31 cell Z0 + TZ
+    for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+      const uint64_t ma = sh.m[wx][wy], mb = sh.m[wx + 1][wy], mc = sh.m[wx][wy + 1], md = sh.m[wx + 1][wy + 1];
+      int rc = 0;
+      if (row && Z0 + lane < g.c[2]) {
+        const int code = code8(ma, mb, mc, md, lane + 1);
+        if (code != 0 && code != 255) rc = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g);
+      }
+      const uint32_t np = (uint32_t)dmc_npatch(dmc_case(rc));
+      const uint32_t incl = warp_incl(np);
+      const uint32_t base = sh.pb[wx][wy][0];
+      sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
+      sh.first[wx][wy][lane + 1] = (int32_t)(base + incl - np);
+      if (lane == 0) {
+        int rp = 0;
+        if (row && Z0 >= 1) {
+          const int code = code8(ma, mb, mc, md, 0);
+          if (code != 0 && code != 255) rp = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 - 1, g);
+        }
+        sh.rc[wx][wy][0] = (uint8_t)rp;
+        sh.first[wx][wy][0] = (int32_t)(base - (uint32_t)dmc_npatch(dmc_case(rp)));
+      }
+      if (lane == 31) {
+        int rn = 0;
+        if (row && Z0 + TZ < g.c[2]) {
+          const int code = code8(ma, mb, mc, md, TZ + 1);
+          if (code != 0 && code != 255) rn = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + TZ, g);
+        }
+        sh.rc[wx][wy][TZ + 1] = (uint8_t)rn;
+        sh.first[wx][wy][TZ + 1] = (int32_t)sh.pb[wx][wy][1];
+      }
+    }
+  }
+  __syncthreads();
+  // window slots: rows' bases by a block scan; slots in (row, cell, axis) order
+  {
+    uint32_t ce = 0;
+    const int ex_ = threadIdx.x / CY, ey = threadIdx.x % CY;
+    if (threadIdx.x < CX * CY) {
+      const RowBits w = sh.wb[ex_][ey];
+      ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(sh.w32[ex_][ey]);
+    }
+    uint32_t tot;
+    const uint32_t off = block_excl_scan(ce, sh.wsum, tot);
+    if (threadIdx.x == 0) sh.nwi = tot;
+    // the row's first slot, parked in its cell TZ entry until the row is written
+    if (threadIdx.x < CX * CY) sh.wcell[ex_][ey][TZ] = (uint16_t)off;
+  }
+  __syncthreads();
+  // one warp per row writes its cells' first slots and flags, and the items
+  for (int r = warp; r < CX * CY; r += NTHREADS / 32) {
+    const int x = r / CY, y = r % CY;
+    const uint32_t rbase = sh.wcell[x][y][TZ];
+    __syncwarp();
+    const RowBits w = sh.wb[x][y];
+    const int fl = row_flags(w, lane);
+    uint32_t o = rbase + (uint32_t)row_prefix(w, lane);
+    sh.wcell[x][y][lane] = (uint16_t)(o | (fl << 13));
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      if (fl & (1 << a)) {
+        if (o < (uint32_t)CAP) sh.witems[o] = item_code(x, y, lane, a);
+        ++o;
+      }
+    if (lane == 31) {
+      const int f32 = sh.w32[x][y];
+      sh.wcell[x][y][TZ] = (uint16_t)(o | (f32 << 13));
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        if (f32 & (1 << a)) {
+          if (o < (uint32_t)CAP) sh.witems[o] = item_code(x, y, TZ, a);
+          ++o;
+        }
+    }
+  }
+  __syncthreads();
+  const uint32_t nwi = sh.nwi;
+  const bool cached = nwi <= (uint32_t)CAP;
+  if (cached) {
+    for (uint32_t i = threadIdx.x; i < nwi; i += blockDim.x) {
+      int x, y, j, a;
+      item_decode(sh.witems[i], x, y, j, a);
+      S c0[4], c1[4];
+      fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
+      store_adj<S>(&sh.adj[0][0], i, c0, c1);
+    }
+    __syncthreads();
+  }
+  // window slot of the edge along a owned by edge-row cell (x, y, j)
+  auto slot = [&](int x, int y, int j, int a) -> int {
+    const int w = sh.wcell[x][y][j];
+    return (w & 0x1fff) + __popc((w >> 13) & ((1 << a) - 1));
+  };
+  // adds the adjoint at end k (0: the edge's first point, 1: its second) of window edge (x, y, j, a)
+  auto add = [&](int x, int y, int j, int a, int k, S acc[4]) {
+    if (cached) {
+      const S* o = &sh.adj[slot(x, y, j, a)][4 * k];
+      acc[0] += o[0];
+      acc[1] += o[1];
+      acc[2] += o[2];
+      acc[3] += o[3];
+    } else {
+      fused_edge_adjoint_far<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, k, acc, &bad);
+    }
+  };
+#pragma unroll 1
+  for (int ix = 0; ix < TX; ++ix) {
+    const int x = ix + 1, y = warp + 1, j = lane + 1;
+    S acc[4] = {S(0), S(0), S(0), S(0)};
+    // per axis the edge from this point (its first point), then the edge ending here,
+    // in the stored backward's order (gather_tile in kernels.cuh)
+    const int fo = sh.wcell[x][y][j] >> 13, fx = sh.wcell[x - 1][y][j] >> 13, fy = sh.wcell[x][y - 1][j] >> 13,
+              fz = sh.wcell[x][y][j - 1] >> 13;
+    if (fo & 1) add(x, y, j, 0, 0, acc);
+    if (fx & 1) add(x - 1, y, j, 0, 1, acc);
+    if (fo & 2) add(x, y, j, 1, 0, acc);
+    if (fy & 2) add(x, y - 1, j, 1, 1, acc);
+    if (fo & 4) add(x, y, j, 2, 0, acc);
+    if (fz & 4) add(x, y, j - 1, 2, 1, acc);
+    const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
+    if (f.inside(X, Y, Z)) {
+      const int64_t i = f.lin(X, Y, Z);
+      gsdf[i] = acc[0];
+      if (gdef) {
+        gdef[3 * i + 0] = acc[1];
+        gdef[3 * i + 1] = acc[2];
+        gdef[3 * i + 2] = acc[3];
+      }
+    }
+  }
+  __syncthreads();  // the shared arrays are reused by the CTA's next tile
+}
+
+// Persistent over the active point tiles in list[0 .. *count) (active_ptiles_kernel
+// in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...; the zeros of the
+// other tiles are written beside it (zero_tiles_kernel).  Bit 3 of stats->error is
+// set when an index derived from the grid falls outside the forward's counts (the
+// grid no longer matches the forward's record); no access leaves its buffer.
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS, 3)
+    fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
+                          const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
+                          S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats) {
+  __shared__ FusedShared<S, METHOD> sh;
+  const uint64_t tot = seg[g.nseg];
+  const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
+  S scale[3];
+  grad_scale<S>(g, normalize, scale);
+  const unsigned n = *count;
+  bool bad = false;
+#pragma unroll 1
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
+    fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad);
+  if (bad) atomicOr(&stats->error, 8ull);
+}
+
+}  // namespace diso

@@ -176,7 +176,8 @@ struct Stats {
   unsigned long long max_key;   // order key of max(sdf)
   unsigned long long n_active;  // active forward tiles
   unsigned long long error;     // bit 0: scan look-back gave up, bit 1: output capacity exceeded,
-                                // bit 2: a TMA wait gave up
+                                // bit 2: a TMA wait gave up, bit 3: the fused backward found an
+                                // index outside the forward's counts
   unsigned long long scan_tile; // dynamic tile counter of the look-back scan
   unsigned long long emit_tile; // dynamic tile counter of the emit
   unsigned long long total;      // the segment scan's total (the forward's counts)

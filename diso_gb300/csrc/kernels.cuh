@@ -1621,11 +1621,18 @@ __global__ void __launch_bounds__(NTHREADS, 4) dmc_emit_kernel(F f, Geom g, cons
 
 // ------------------------------------------------------------------ backward
 
+// explicitly rounded product and fused multiply-add: the same rounding wherever the
+// compiler inlines them
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 // dL/dverts of vertex i in padded coordinates: the chain rule of "- 1" and "/ (dim - 1)"
 template <class S>
 __device__ __forceinline__ void load_grad(const S* __restrict__ gv, int64_t i, const S scale[3], S out[3]) {
 #pragma unroll
-  for (int k = 0; k < 3; ++k) out[k] = __ldg(gv + 3 * i + k) * scale[k];
+  for (int k = 0; k < 3; ++k) out[k] = mul_rn(__ldg(gv + 3 * i + k), scale[k]);
 }
 
 // adjoint of edge_vertex (adjComputeMcVert, src/cumc.cu:412-453) for the edge from
@@ -1646,15 +1653,17 @@ __device__ __forceinline__ void edge_adjoint2(const Field<S>& f, int X, int Y, i
   f.deform(X + ex, Y + ey, Z + ez, q1);
   const S dp[3] = {(S(X + ex) + q1[0]) - (S(X) + q0[0]), (S(Y + ey) + q1[1]) - (S(Y) + q0[1]),
                    (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
-  const S adj_t = dp[0] * gvec[0] + dp[1] * gvec[1] + dp[2] * gvec[2];
+  const S adj_t = fma_rn(dp[2], gvec[2], fma_rn(dp[1], gvec[1], mul_rn(dp[0], gvec[0])));
   const S den = (d1 - d0) * (d1 - d0);
   const S w0 = S(1) - t;
-  c0[0] = (f.iso - d1) / den * adj_t;
-  c1[0] = (d0 - f.iso) / den * adj_t;
+  // rounded products: the backward's two forms (the adjoints stored, then added
+  // per point; or added where they are computed) must not fuse them into the sums
+  c0[0] = mul_rn((f.iso - d1) / den, adj_t);
+  c1[0] = mul_rn((d0 - f.iso) / den, adj_t);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    c0[k + 1] = w0 * gvec[k];
-    c1[k + 1] = t * gvec[k];
+    c0[k + 1] = mul_rn(w0, gvec[k]);
+    c1[k + 1] = mul_rn(t, gvec[k]);
   }
 }
 
@@ -1780,9 +1789,9 @@ __device__ __forceinline__ void edge_adjoint_at(const Field<S>& f, const EdgeRec
       const S inv = recip<S>((int)(x & 15u));
       S v[3];
       load_grad<S>(gv, exact ? p : p - (int64_t)(x >> 4), scale, v);
-      gvec[0] += v[0] * inv;
-      gvec[1] += v[1] * inv;
-      gvec[2] += v[2] * inv;
+      gvec[0] = fma_rn(v[0], inv, gvec[0]);
+      gvec[1] = fma_rn(v[1], inv, gvec[1]);
+      gvec[2] = fma_rn(v[2], inv, gvec[2]);
     }
   }
   S c0[4], c1[4];

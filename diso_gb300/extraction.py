@@ -20,9 +20,11 @@ Differences that are invisible to callers of the reference API:
   the sum of dL/dsdf (the reference's isovalue is a plain scalar).
 
 With recompute=True the forward keeps nothing for the backward but the inputs
-(no edge record, no gradient buffers: the reference's memory profile), and the
-backward runs the forward again to rebuild the edge record; slower, and the
-same gradients bit for bit.
+and its segment record (the scanned output counts per 32-cell row segment, 8
+bytes per 32 cells): no edge record and no gradient buffers.  The backward
+recomputes the crossings, the DMC cell codes and patch ids and every edge's
+adjoint per point tile in one pass that writes each gradient element once
+(diso_backward_recompute); the gradients are the stored mode's bit for bit.
 
 The outputs are the reference's: the same vertex, face and quad order, the same
 dtypes, including the int32 empty faces of the guard.
@@ -87,8 +89,7 @@ class _ExtractFunction(Function):
         ctx.iso, ctx.pad, ctx.normalize, ctx.exact_grad = iso, pad, normalize, exact_grad
         ctx.has_deform = deform is not None
         ctx.recompute, ctx.counts = recompute, (nv, nf)
-        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0),
-                              seg if not recompute else seg.new_empty(0),
+        ctx.save_for_backward(grid, deform if deform is not None else grid.new_empty(0), seg,
                               record if record is not None else seg.new_empty(0))
         ctx.mark_non_differentiable(faces)
         # the faces never get a gradient; without this autograd would fill one with zeros
@@ -102,12 +103,13 @@ class _ExtractFunction(Function):
         d = deform.detach().contiguous() if ctx.has_deform else None
         with torch.cuda.device(g.device):
             if grad_verts is None:
-                grad_verts = torch.zeros(0, 3, dtype=g.dtype, device=g.device)
+                grad_verts = torch.zeros(ctx.counts[0], 3, dtype=g.dtype, device=g.device)
             gv = grad_verts.contiguous()
             _mark("backward", "start")
             if ctx.recompute:
-                seg, record, gs, gd = _recompute(ctx.ex, g, d, ctx.iso, ctx.pad, ctx.normalize, *ctx.counts)
-                zeroed = True
+                gs = torch.empty_like(g)
+                gd = torch.empty_like(d) if d is not None else None
+                ctx.ex.backward_recompute(g, d, ctx.iso, ctx.pad, seg, ctx.normalize, gv, gs, gd, ctx.exact_grad)
             else:
                 gs, gd = ctx.gs, ctx.gd
                 zeroed = gs is not None
@@ -115,35 +117,14 @@ class _ExtractFunction(Function):
                     gs = torch.empty_like(g)
                     gd = torch.empty_like(d) if d is not None else None
                 ctx.gs = ctx.gd = None
-            ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
-                            zeroed=zeroed)
+                ctx.ex.backward(g, d, ctx.iso, ctx.pad, seg, record, ctx.normalize, gv, gs, gd, ctx.exact_grad,
+                                zeroed=zeroed)
             giso = None
             if ctx.needs_input_grad[12]:
                 dtype, device, shape = ctx.iso_like
                 giso = ctx.ex.isovalue_grad(gs, seg).to(device=device, dtype=dtype).reshape(shape)
             _mark("backward", "end")
         return gs, gd, None, None, None, None, None, None, None, None, None, None, giso, None
-
-
-def _recompute(ex, g, d, iso, pad, normalize, nv, nf):
-    """The forward once more, for a backward whose forward kept nothing: the
-    segment record, the edge record (the outputs are rebuilt into temporaries) and
-    gradient buffers that this forward zeroes.  The reference's backward re-runs its
-    forward in the same way (diso/__init__.py:32, 86)."""
-    dev = g.device
-    seg = torch.empty(N.Extractor.segment_slots(g.shape), dtype=torch.int64, device=dev)
-    gs = torch.empty_like(g)
-    gd = torch.empty_like(d) if d is not None else None
-    ex.zero_grads(gs, gd)
-    width = 3 if ex.method == N.MC else 4
-    verts = torch.empty((nv, 3), dtype=ex.dtype, device=dev)
-    faces = torch.empty((nf, width), dtype=torch.int64, device=dev)
-    record = torch.empty(max(1, ex.record_slots(n_verts=nv, n_faces=nf)), dtype=torch.int64, device=dev)
-    counts = ex.forward(g, d, iso, pad, seg, normalize, verts, faces, record)
-    if not counts.emitted or int(counts.n_verts) != nv or int(counts.n_faces) != nf:
-        raise RuntimeError("the forward run again for the backward gave another mesh "
-                           "(was the grid changed in place?)")
-    return seg, record, gs, gd
 
 
 def _capacity(n):
@@ -158,7 +139,8 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
     the reference) receives dL/d(isovalue) in the backward.
 
     recompute=True keeps no edge record and no gradient buffers between the
-    forward and the backward; the backward runs the forward again instead.
+    forward and the backward, only the segment record; the backward recomputes
+    the crossing lists per point tile.
 
     exact_grad (DMC only) replaces the reference's backward in cells with several
     patches, where every patch receives the first patch's gradient
@@ -227,7 +209,8 @@ class DiffMC(nn.Module):
     """Differentiable marching cubes (diso/__init__.py:9-61).
 
     ``recompute=True`` (keyword only, not in the reference) keeps nothing between
-    the forward and the backward but the inputs; the backward runs the forward again."""
+    the forward and the backward but the inputs and the segment record; the
+    backward recomputes the crossing lists."""
 
     def __init__(self, dtype=torch.float32, *, recompute=False):
         super().__init__()

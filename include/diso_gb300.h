@@ -142,6 +142,24 @@ int diso_backward(diso_extractor* ex, const void* sdf, const void* deform, int n
                   double padval, const uint64_t* seg, uint64_t* edge_record, int normalize, int flags,
                   const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
 
+/* Backward of a forward that kept nothing but its `seg` (no edge record, no
+ * gradient buffers): dL/dsdf [nx][ny][nz] and dL/ddeform [nx][ny][nz][3] (when
+ * deform is not NULL) from dL/dverts [n_verts][3], every element of both written.
+ * The crossings near each point tile, the vertex ids (MC) or the DMC cells' codes
+ * after the ambiguity test and their patch ids, each edge's adjoint and each point's
+ * sum are recomputed per tile in one pass (the tiles with no crossing nearby get
+ * zeros on a second stream of the extractor): the same values, bit for bit, as
+ * diso_backward with the forward's edge record (flags as there).  The inputs must
+ * hold the values the forward saw; every index derived from them is checked against
+ * the counts in `seg`, so a grid changed since the forward gives wrong gradients but
+ * no access outside the buffers.  No host synchronisation.  Replaces
+ * DMCFunction.backward / DDMCFunction.backward (diso/__init__.py:30-44, 84-98),
+ * which re-run the forward to rebuild the crossing lists, and CuMC::backward /
+ * CUDualMC::backward (src/cumc.cu:734-743, src/cudualmc.cu:1130-1138). */
+int diso_backward_recompute(diso_extractor* ex, const void* sdf, const void* deform, int nx, int ny, int nz,
+                            double isovalue, double padval, const uint64_t* seg, int normalize, int flags,
+                            const void* grad_verts, void* grad_sdf, void* grad_deform, void* stream);
+
 /* dL/d(isovalue) of an extraction, from the dL/dsdf [nx][ny][nz] that
  * diso_backward wrote: minus its sum (moving the isovalue by e moves every crossing
  * as moving every grid value by -e; the pad value isovalue + 1 moves with it).  The

@@ -97,6 +97,22 @@ def test_backward_needs_an_aligned_edge_record(lib):
     lib.diso_destroy(h)
 
 
+def test_recompute_backward_checks_its_arguments(lib):
+    h = ctypes.c_void_p()
+    assert lib.diso_create(1, 0, ctypes.byref(h)) == 0
+    p = ctypes.c_void_p(4096)
+    # (ex, sdf, deform, nx, ny, nz, iso, pad, seg, normalize, flags, grad_verts, grad_sdf, grad_deform, stream)
+    assert lib.diso_backward_recompute(h, p, None, 4, 4, 4, 0.0, 1.0, None, 1, 0, p, p, None, None) == 1
+    assert b"null seg" in lib.diso_last_error()
+    assert lib.diso_backward_recompute(h, p, None, 4, 4, 4, 0.0, 1.0, p, 1, 0, None, p, None, None) == 1
+    assert b"null grad_verts" in lib.diso_last_error()
+    assert lib.diso_backward_recompute(h, p, p, 4, 4, 4, 0.0, 1.0, p, 1, 0, p, p, None, None) == 1
+    assert b"without grad_deform" in lib.diso_last_error()
+    assert lib.diso_backward_recompute(h, p, None, 0, 4, 4, 0.0, 1.0, p, 1, 0, p, p, None, None) == 1
+    assert b"grid dims" in lib.diso_last_error()
+    lib.diso_destroy(h)
+
+
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     from diso_gb300 import _native
 

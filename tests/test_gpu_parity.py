@@ -15,18 +15,18 @@ pytestmark = pytest.mark.gpu
 DT = {"float32": torch.float32, "float64": torch.float64}
 
 
-def run(case, sdf_np, def_np, weights=None, exact_grad=False, device="cuda:0"):
+def run(case, sdf_np, def_np, weights=None, exact_grad=False, device="cuda:0", recompute=False):
     from diso_gb300 import DiffDMC, DiffMC
 
     dt = DT[case["dtype"]]
     sdf = torch.tensor(sdf_np, device=device, requires_grad=True)
     deform = torch.tensor(def_np, device=device, requires_grad=True) if def_np is not None else None
     if case["method"] == "mc":
-        verts, faces = DiffMC(dt)(sdf, deform, isovalue=case["iso"], normalize=case["normalize"])
+        verts, faces = DiffMC(dt, recompute=recompute)(sdf, deform, isovalue=case["iso"],
+                                                        normalize=case["normalize"])
     else:
-        verts, faces = DiffDMC(dt, exact_grad=exact_grad)(sdf, deform, isovalue=case["iso"],
-                                                           return_quads=case["return_quads"],
-                                                           normalize=case["normalize"])
+        verts, faces = DiffDMC(dt, exact_grad=exact_grad, recompute=recompute)(
+            sdf, deform, isovalue=case["iso"], return_quads=case["return_quads"], normalize=case["normalize"])
     out = dict(verts=verts.detach().cpu().numpy(), faces=faces.cpu().numpy(), faces_dtype=str(faces.dtype))
     if weights is not None and verts.shape[0]:
         (verts * torch.tensor(weights, device=device)).sum().backward()
@@ -36,11 +36,12 @@ def run(case, sdf_np, def_np, weights=None, exact_grad=False, device="cuda:0"):
     return out
 
 
+@pytest.mark.parametrize("recompute", [False, True])
 @pytest.mark.parametrize("name", fixture_names())
-def test_matches_reference_fixture(cuda_device, name):
+def test_matches_reference_fixture(cuda_device, name, recompute):
     fx = load_fixture(name)
     c = fx["case"]
-    out = run(c, fx["sdf"], fx["deform"], fx.get("weights"))
+    out = run(c, fx["sdf"], fx["deform"], fx.get("weights"), recompute=recompute)
     assert out["faces_dtype"] == fx["faces_dtype"]
     assert_verts_close(out["verts"], fx["verts"], c)
     assert_faces_equal(out["faces"], fx["faces"], c, fx["verts"])
@@ -86,8 +87,9 @@ ORACLE_CASES = [
 ]
 
 
+@pytest.mark.parametrize("recompute", [False, True])
 @pytest.mark.parametrize("method,dtype,field,shape,deform,iso,normalize,rq", ORACLE_CASES)
-def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, normalize, rq):
+def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, normalize, rq, recompute):
     rng = np.random.default_rng(zlib.crc32(repr((method, dtype, field, shape)).encode()))
     sdf = _field(field, shape, rng).astype(dtype)
     dfm = rng.uniform(-deform, deform, shape + (3,)).astype(dtype) if deform else None
@@ -95,7 +97,7 @@ def test_matches_oracle(cuda_device, method, dtype, field, shape, deform, iso, n
     m = O.MC if method == "mc" else O.DMC
     v_ref, f_ref, info = O.extract(m, sdf, dfm, iso, normalize, rq, dtype)
     w = rng.standard_normal(v_ref.shape).astype(dtype)
-    out = run(case, sdf, dfm, w)
+    out = run(case, sdf, dfm, w, recompute=recompute)
     if info["empty_guard"]:
         assert out["verts"].shape == (0, 3) and out["faces_dtype"] == "torch.int32"
         return

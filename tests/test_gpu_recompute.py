@@ -1,7 +1,10 @@
-"""recompute=True: the forward keeps no edge record and no gradient buffers (the
-reference's memory profile: its backward re-runs the forward, diso/__init__.py:32,
-86); the backward runs the forward again.  Outputs and gradients equal the default
-mode's bit for bit, and the forward holds less device memory."""
+"""recompute=True: the forward keeps no edge record and no gradient buffers, only
+its segment record (the reference keeps nothing and its backward re-runs the
+forward, diso/__init__.py:32, 86); the backward recomputes the crossing lists per
+point tile in one fused pass (diso_backward_recompute).  Outputs and gradients
+equal the default mode's bit for bit (also where a tile's window holds too many
+crossing edges for the shared-memory cache, on dense random fields), and the
+forward holds less device memory."""
 import numpy as np
 import pytest
 import torch
@@ -45,6 +48,64 @@ def test_recompute_equals_stored(cuda_device, method, kw, dtype, with_deform):
         b = _step(_module(method, dtype, True), sdf, deform, kw, iso)
         for x, y in zip(a, b):
             assert (x is None and y is None) or torch.equal(x, y)
+
+
+def _dense(shape, dtype, dev, seed):
+    rng = np.random.default_rng(seed)
+    npdt = np.float32 if dtype == torch.float32 else np.float64
+    sdf = rng.uniform(-1, 1, shape).astype(npdt)
+    deform = rng.uniform(-0.45, 0.45, shape + (3,)).astype(npdt)
+    return torch.tensor(sdf, device=dev), torch.tensor(deform, device=dev)
+
+
+@pytest.mark.parametrize("method,kw,exact", [("mc", {}, False), ("dmc", {"return_quads": True}, False),
+                                             ("dmc", {"return_quads": True}, True)])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("shape,field", [((37, 50, 70), "dense"), ((65, 33, 97), "sphere"),
+                                         ((96, 96, 96), "dense")])
+def test_fused_backward_equals_stored(cuda_device, method, kw, exact, dtype, shape, field):
+    """Dense U(-1, 1) fields put thousands of crossing edges in a tile's window (the
+    uncached path); odd sizes leave partial tiles on every axis and rows that are no
+    multiple of four values (the scalar zero path); exact_grad takes each patch's own
+    gradient."""
+    from diso_gb300 import DiffDMC, DiffMC
+
+    if field == "dense":
+        sdf, deform = _dense(shape, dtype, cuda_device, 5)
+    else:
+        sdf, deform = _inputs(shape[0], dtype, cuda_device, 6)
+        sdf, deform = sdf[:, :shape[1], :shape[2]].contiguous(), deform[:, :shape[1], :shape[2]].contiguous()
+    res = []
+    for recompute in (False, True):
+        mod = (DiffMC(dtype, recompute=recompute) if method == "mc"
+               else DiffDMC(dtype, recompute=recompute, exact_grad=exact))
+        for normalize in (True, False):
+            s = sdf.clone().requires_grad_(True)
+            d = deform.clone().requires_grad_(True)
+            v, f = mod(s, d, 0.0, normalize=normalize, **kw)
+            w = torch.randn(v.shape, dtype=v.dtype, device=v.device,
+                            generator=torch.Generator(v.device).manual_seed(7))
+            (v * w).sum().backward()
+            res.append((v.detach(), f, s.grad, d.grad))
+    for x, y in zip(res[:2], res[2:]):
+        for a, b in zip(x, y):
+            assert torch.equal(a, b)
+
+
+def test_fused_backward_repeats_bit_for_bit(cuda_device):
+    from diso_gb300 import DiffDMC
+
+    sdf, deform = _dense((48, 48, 48), torch.float32, cuda_device, 8)
+    mod = DiffDMC(torch.float32, recompute=True)
+    out = []
+    for _ in range(3):
+        s = sdf.clone().requires_grad_(True)
+        d = deform.clone().requires_grad_(True)
+        v, _ = mod(s, d, return_quads=True)
+        (v * v).sum().backward()
+        out.append((s.grad, d.grad))
+    for a, b in out[1:]:
+        assert torch.equal(a, out[0][0]) and torch.equal(b, out[0][1])
 
 
 def test_recompute_isovalue_grad(cuda_device):
