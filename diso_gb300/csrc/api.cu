@@ -77,6 +77,7 @@ struct diso_extractor {
   int gather_ctas = 0;           // the same for the point gather
   int emit_ctas = 0;             // the same for the emit
   int fused_ctas = 0;            // the same for the fused backward
+  int fused_smem = 0;            // its dynamic shared memory per CTA
   int sms = 0;
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -317,7 +318,11 @@ int bind_device(diso_extractor* ex) {
                                                   : (const void*)fused_backward_kernel<float, DMC>)
                          : (ex->method == DISO_MC ? (const void*)fused_backward_kernel<double, MC>
                                                   : (const void*)fused_backward_kernel<double, DMC>);
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, fk, NTHREADS, 0));
+    ex->fused_smem = (int)(ex->dtype == DISO_F32
+                               ? (ex->method == DISO_MC ? fused_smem<float, MC>() : fused_smem<float, DMC>())
+                               : (ex->method == DISO_MC ? fused_smem<double, MC>() : fused_smem<double, DMC>()));
+    CUDA_TRY(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, fk, NTHREADS, ex->fused_smem));
     ex->fused_ctas = sms * std::max(per_f, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
@@ -664,10 +669,10 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   {
     KernelTimer kt(ex, K_FUSED_BWD, s);
     if (ex->method == DISO_MC)
-      fused_backward_kernel<S, MC><<<(unsigned)ex->fused_ctas, NTHREADS, 0, s>>>(
+      fused_backward_kernel<S, MC><<<(unsigned)ex->fused_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
           f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gsdf, (S*)gdef, ex->stats);
     else
-      fused_backward_kernel<S, DMC><<<(unsigned)ex->fused_ctas, NTHREADS, 0, s>>>(
+      fused_backward_kernel<S, DMC><<<(unsigned)ex->fused_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
           f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats);
   }
   CUDA_TRY(cudaGetLastError());

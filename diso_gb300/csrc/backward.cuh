@@ -31,10 +31,13 @@
 
 namespace diso {
 
-constexpr int FB_ADJ_BYTES = 16384;  // shared memory for the window edges' adjoints
+// Window edges whose adjoints a tile keeps in shared memory: sized so that three
+// CTAs share an SM (the tile's state is about 72 KB of dynamic shared memory in
+// either precision); at 512^3 on a noisy union of spheres about 99% of the windows
+// fit (the largest hold some 1900 edges, the median about 400).
 template <class S>
 __host__ __device__ constexpr int fb_cap() {
-  return FB_ADJ_BYTES / (8 * (int)sizeof(S));
+  return sizeof(S) == 4 ? 1664 : 832;
 }
 
 template <class S, int METHOD>
@@ -336,11 +339,17 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
 // set when an index derived from the grid falls outside the forward's counts (the
 // grid no longer matches the forward's record); no access leaves its buffer.
 template <class S, int METHOD>
+__host__ __device__ constexpr size_t fused_smem() {
+  return sizeof(FusedShared<S, METHOD>);
+}
+
+template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3)
     fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
                           S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats) {
-  __shared__ FusedShared<S, METHOD> sh;
+  extern __shared__ __align__(16) unsigned char fb_smem[];
+  FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
   const uint64_t tot = seg[g.nseg];
   const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
   S scale[3];
