@@ -126,23 +126,56 @@ __device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>&
   edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
 }
 
+template <class S>
+struct Adj4 {
+  S v[4];
+  bool bad;
+};
+
 // the uncached path's per-point call, kept out of line (it runs only for tiles with
-// more window edges than the cache holds): adds the adjoint at end k of window
-// edge (x, y, j, a) to acc
+// more window edges than the cache holds): the adjoint at end k of window edge
+// (x, y, j, a)
 template <class S, int METHOD>
-__device__ __noinline__ void fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
-                                                    int Y0, int Z0, int x, int y, int j, int a,
-                                                    const S* __restrict__ gv, int64_t V, const S* scale, int exact,
-                                                    int k, S* acc, bool* bad) {
+__device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
+                                                       int Y0, int Z0, int x, int y, int j, int a,
+                                                       const S* __restrict__ gv, int64_t V, S sx, S sy, S sz,
+                                                       int exact, int k) {
   S c0[4], c1[4];
-  bool b = false;
-  fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, b);
-  const S* o = k ? c1 : c0;
-  acc[0] += o[0];
-  acc[1] += o[1];
-  acc[2] += o[2];
-  acc[3] += o[3];
-  if (b) *bad = true;
+  const S scale[3] = {sx, sy, sz};
+  Adj4<S> r;
+  r.bad = false;
+  fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, r.bad);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) r.v[i] = k ? c1[i] : c0[i];
+  return r;
+}
+
+// Morton code of cell (X, Y, Z) from global memory, out of line: the DMC ambiguity
+// test needs it only for an ambiguous cell whose neighbour lies outside the masks
+template <class S>
+__device__ __noinline__ int fused_code_far(const Field<S>& f, int X, int Y, int Z) {
+  return cell_code_far<S>(f, X, Y, Z);
+}
+
+// dmc_resolve_m (kernels.cuh) with the neighbour's code from the masks when its
+// corners lie in them, otherwise from fused_code_far
+template <class S, int WX, int WY>
+__device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
+                                             int code, int X, int Y, int Z, const Geom& g) {
+  const int dir = dmc_dir(dmc_case(code));
+  if (dir == 7) return code;
+  const int comp = dir >> 1, d = (dir & 1) ? 1 : -1;
+  const int NX = X + (comp == 0 ? d : 0), NY = Y + (comp == 1 ? d : 0), NZ = Z + (comp == 2 ? d : 0);
+  const int nc = comp == 0 ? NX : (comp == 1 ? NY : NZ);
+  if (nc < 0 || nc >= g.c[comp]) return code;
+  const unsigned x = (unsigned)(NX - WX0), y = (unsigned)(NY - WY0);
+  const int sft = NZ - Z0 + 1;
+  int ncode;
+  if (x < (unsigned)(WX - 1) && y < (unsigned)(WY - 1) && sft >= 0 && sft + 1 <= MASK_TOP)
+    ncode = code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], sft);
+  else
+    ncode = fused_code_far<S>(f, NX, NY, NZ);
+  return dmc_dir(dmc_case(ncode)) != 7 ? (code ^ 0xff) : code;
 }
 
 // one active point tile (see the top of this file)
@@ -197,40 +230,41 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
     }
   }
   if constexpr (METHOD == DMC) {
-    // window cells: codes after the ambiguity test and first patch ids, one warp per
-    // cell row; lane j takes cell Z0 + j, lane 0 also cell Z0 - 1, lane 31 cell Z0 + TZ
+    // window cells: codes after the ambiguity test and first patch ids.  One warp per
+    // cell row, lane j for cell Z0 + j (rows without a non-trivial cell need no test
+    // and no scan); then one thread per row end for cells Z0 - 1 and Z0 + TZ.
     for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
       const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
       const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
-      const uint64_t ma = sh.m[wx][wy], mb = sh.m[wx + 1][wy], mc = sh.m[wx][wy + 1], md = sh.m[wx + 1][wy + 1];
-      int rc = 0;
-      if (row && Z0 + lane < g.c[2]) {
-        const int code = code8(ma, mb, mc, md, lane + 1);
-        if (code != 0 && code != 255) rc = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g);
+      const uint32_t base = sh.pb[wx][wy][0];
+      int code = 0;
+      if (row && Z0 + lane < g.c[2]) code = code8(sh.m[wx][wy], sh.m[wx + 1][wy], sh.m[wx][wy + 1], sh.m[wx + 1][wy + 1],
+                                                  lane + 1);
+      const bool nt = code != 0 && code != 255;
+      if (!__any_sync(0xffffffffu, nt)) {
+        sh.rc[wx][wy][lane + 1] = 0;
+        sh.first[wx][wy][lane + 1] = (int32_t)base;
+        continue;
       }
+      const int rc = nt ? fused_resolve<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g) : 0;
       const uint32_t np = (uint32_t)dmc_npatch(dmc_case(rc));
       const uint32_t incl = warp_incl(np);
-      const uint32_t base = sh.pb[wx][wy][0];
       sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
       sh.first[wx][wy][lane + 1] = (int32_t)(base + incl - np);
-      if (lane == 0) {
-        int rp = 0;
-        if (row && Z0 >= 1) {
-          const int code = code8(ma, mb, mc, md, 0);
-          if (code != 0 && code != 255) rp = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 - 1, g);
-        }
-        sh.rc[wx][wy][0] = (uint8_t)rp;
-        sh.first[wx][wy][0] = (int32_t)(base - (uint32_t)dmc_npatch(dmc_case(rp)));
+    }
+    if (threadIdx.x < 2 * KX * KY) {
+      const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const int Z = end ? Z0 + TZ : Z0 - 1;
+      int rc = 0;
+      if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && Z >= 0 && Z < g.c[2]) {
+        const int code = code8(sh.m[wx][wy], sh.m[wx + 1][wy], sh.m[wx][wy + 1], sh.m[wx + 1][wy + 1],
+                               end ? TZ + 1 : 0);
+        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z, g);
       }
-      if (lane == 31) {
-        int rn = 0;
-        if (row && Z0 + TZ < g.c[2]) {
-          const int code = code8(ma, mb, mc, md, TZ + 1);
-          if (code != 0 && code != 255) rn = dmc_resolve_m<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + TZ, g);
-        }
-        sh.rc[wx][wy][TZ + 1] = (uint8_t)rn;
-        sh.first[wx][wy][TZ + 1] = (int32_t)sh.pb[wx][wy][1];
-      }
+      sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
+      sh.first[wx][wy][end ? TZ + 1 : 0] =
+          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(dmc_case(rc)));
     }
   }
   __syncthreads();
@@ -293,18 +327,6 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
     const int w = sh.wcell[x][y][j];
     return (w & 0x1fff) + __popc((w >> 13) & ((1 << a) - 1));
   };
-  // adds the adjoint at end k (0: the edge's first point, 1: its second) of window edge (x, y, j, a)
-  auto add = [&](int x, int y, int j, int a, int k, S acc[4]) {
-    if (cached) {
-      const S* o = &sh.adj[slot(x, y, j, a)][4 * k];
-      acc[0] += o[0];
-      acc[1] += o[1];
-      acc[2] += o[2];
-      acc[3] += o[3];
-    } else {
-      fused_edge_adjoint_far<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, k, acc, &bad);
-    }
-  };
 #pragma unroll 1
   for (int ix = 0; ix < TX; ++ix) {
     const int x = ix + 1, y = warp + 1, j = lane + 1;
@@ -313,12 +335,32 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
     // in the stored backward's order (gather_tile in kernels.cuh)
     const int fo = sh.wcell[x][y][j] >> 13, fx = sh.wcell[x - 1][y][j] >> 13, fy = sh.wcell[x][y - 1][j] >> 13,
               fz = sh.wcell[x][y][j - 1] >> 13;
-    if (fo & 1) add(x, y, j, 0, 0, acc);
-    if (fx & 1) add(x - 1, y, j, 0, 1, acc);
-    if (fo & 2) add(x, y, j, 1, 0, acc);
-    if (fy & 2) add(x, y - 1, j, 1, 1, acc);
-    if (fo & 4) add(x, y, j, 2, 0, acc);
-    if (fz & 4) add(x, y, j - 1, 2, 1, acc);
+    const int on = (fo & 1) | ((fx & 1) << 1) | ((fo & 2) << 1) | ((fy & 2) << 2) | ((fo & 4) << 2) |
+                   ((fz & 4) << 3);
+    if (cached) {
+#pragma unroll
+      for (int e = 0; e < 6; ++e)
+        if ((on >> e) & 1) {
+          const S* o = &sh.adj[slot(x - (e == 1), y - (e == 3), j - (e == 5), e >> 1)][4 * (e & 1)];
+          acc[0] += o[0];
+          acc[1] += o[1];
+          acc[2] += o[2];
+          acc[3] += o[3];
+        }
+    } else {
+#pragma unroll 1
+      for (int e = 0; e < 6; ++e)
+        if ((on >> e) & 1) {
+          const Adj4<S> o =
+              fused_edge_adjoint_far<S, METHOD>(sh, f, X0, Y0, Z0, x - (e == 1), y - (e == 3), j - (e == 5), e >> 1,
+                                                gv, V, scale[0], scale[1], scale[2], exact, e & 1);
+          acc[0] += o.v[0];
+          acc[1] += o.v[1];
+          acc[2] += o.v[2];
+          acc[3] += o.v[3];
+          bad = bad || o.bad;
+        }
+    }
     const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
     if (f.inside(X, Y, Z)) {
       const int64_t i = f.lin(X, Y, Z);
