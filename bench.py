@@ -399,34 +399,60 @@ class PhaseEvents:
         return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in self.done.items()}
 
 
-def kernel_bytes(vol, nseg, nv, nq, s, zshare, kernels, steps):
+def kernel_bytes(vol, nseg, nv, nq, s, zshare, active_pts):
     """Algorithmic bytes per launch of each kernel of the 512^3 DMC step: what the
     kernel's function must read and write at least (nq crossing edges = quads, nv
-    patches = vertices, s bytes per scalar), from its bytes per step divided by its
-    launches per step (in recompute mode the count, the scan and the emit run once in
-    the forward and once more in the backward).  The zeros of the two gradient arrays
-    are written once per step, by the count (the share zshare) and the emit (the
-    rest), or by memsets ("zero_grads") when the buffers do not allow it."""
+    patches = vertices, s bytes per scalar, active_pts = points of the point tiles
+    with a crossing edge nearby).
+
+    Stored mode: the forward's count and emit also write the zeros of the two
+    gradient arrays (the count the share zshare, the emit the rest; memsets,
+    "zero_grads", when the buffers do not allow it) and the emit the edge record;
+    the backward's edge pass and gather read it.  Recompute mode: the forward writes
+    no zeros and no record; the backward zeroes the point tiles with no crossing
+    nearby (zero_tiles) and recomputes the rest in one pass (fused_bwd)."""
     zeros = vol * 4 * s
-    per = {k: max(1, round(cnt / steps)) for k, (cnt, _) in kernels.items()}
-    k_count, k_scan, k_emit = per.get("count", 1), per.get("scan", 1), per.get("emit", 1)
-    step = {
-        # the SDF once per launch; the per-segment counts out; the count's share of the zeros
-        "count": k_count * (vol * s + nseg * 8) + zshare * zeros,
+    return {
+        # the SDF once; the per-segment counts out; its share of the zeros (stored mode)
+        "count": vol * s + nseg * 8 + zshare * zeros,
         # segment counts in and out
-        "scan": k_scan * 2 * nseg * 8,
-        # per launch both end points of every crossing edge (SDF + deform) in, vertices and
-        # quads out; once per step the edge record (cell + axis, four patch ids, a byte per
-        # vertex) and the rest of the zeros
-        "emit": k_emit * (2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8) + nq * (8 + 16) + nv + (1 - zshare) * zeros,
+        "scan": 2 * nseg * 8,
+        # both end points of every crossing edge (SDF + deform) in; vertices and quads out;
+        # stored mode: the edge record (cell + axis, four patch ids, a byte per vertex) and
+        # the rest of the zeros
+        "emit": 2 * nq * 4 * s + nv * 3 * s + nq * 4 * 8 + (nq * (8 + 16) + nv + (1 - zshare) * zeros if zshare else 0),
         "zero_grads": zeros,
         # per edge: record (cell, 4 patch ids), 4 patch bytes and 4 dL/dverts in, end points
         # (SDF + deform) in, 2 x 4 adjoints out
         "edge": nq * (8 + 16 + 4 + 4 * 3 * s + 2 * 4 * s + 8 * s),
         # the adjoints of every edge, once from each end
         "gather": nq * 8 * s,
+        # the gradients of the point tiles with no crossing nearby
+        "zero_tiles": (vol - active_pts) * 4 * s,
+        # the SDF of the active tiles in, their gradients out; the deform at both ends of
+        # every crossing edge and dL/dverts in
+        "fused_bwd": active_pts * 5 * s + nq * 2 * 3 * s + nv * 3 * s,
     }
-    return {k: v / per.get(k, 1) for k, v in step.items()}
+
+
+def active_points(sdf, iso=0.0):
+    """Points of the 4 x 8 x 32 point tiles that hold a point with a crossing edge
+    (the tiles the backward's fused pass works on; the grid is padded with
+    iso + 1 as in the forward)."""
+    with torch.no_grad():
+        b = torch.nn.functional.pad(sdf.unsqueeze(0).unsqueeze(0) >= iso, (1, 1, 1, 1, 1, 1), value=True)[0, 0]
+        inc = torch.zeros_like(b, dtype=torch.bool)
+        for ax in range(3):
+            c = b.narrow(ax, 1, b.shape[ax] - 1) != b.narrow(ax, 0, b.shape[ax] - 1)
+            inc.narrow(ax, 1, b.shape[ax] - 1).logical_or_(c)
+            inc.narrow(ax, 0, b.shape[ax] - 1).logical_or_(c)
+        inner = inc[1:-1, 1:-1, 1:-1]
+        n0, n1, n2 = inner.shape
+        t = torch.zeros(((n0 + 3) // 4) * 4, ((n1 + 7) // 8) * 8, ((n2 + 31) // 32) * 32, dtype=torch.bool,
+                        device=sdf.device)
+        t[:n0, :n1, :n2] = inner
+        act = t.view(t.shape[0] // 4, 4, t.shape[1] // 8, 8, t.shape[2] // 32, 32).any(5).any(3).any(1)
+        return int(act.sum()) * 4 * 8 * 32
 
 
 def read_profile_traffic(kernel):
@@ -638,8 +664,10 @@ def run_ours(args, rank, world, device):
     s_b = 4
     vol = n ** 3
     nseg = (n + 1) ** 2 * ((n + 1 + 31) // 32)
-    zshare = 0.0 if "zero_grads" in kernels else float(N.lib().diso_zero_count_share())
-    algo = kernel_bytes(vol, nseg, nv, nq, s_b, zshare, kernels, args.steps)
+    act_pts = active_points(sdf)
+    algo = kernel_bytes(vol, nseg, nv, nq, s_b, 0.0, act_pts)
+    zshare = 0.0 if "zero_grads" in k_st else float(N.lib().diso_zero_count_share())
+    algo_st = kernel_bytes(vol, nseg, nv, nq, s_b, zshare, act_pts)
     per_launch = {k: ms / max(cnt, 1) for k, (cnt, ms) in kernels.items()}
     ours = {k: v for k, v in per_launch.items() if k in algo and k != "zero_grads"}
     dom = max(ours, key=lambda k: ours[k] * kernels[k][0])
@@ -668,12 +696,15 @@ def run_ours(args, rank, world, device):
                    "kernel_ms_per_step": {k: round(ms / args.steps, 4) for k, (cnt, ms) in kernels.items()},
                    "kernel_gbs": {k: round(algo[k] / (per_launch[k] * 1e-3) / 1e9, 1) for k in per_launch
                                   if k in algo},
+                   "active_point_tiles": act_pts // 1024,
                    "step_algorithmic_gb": round(step_bytes / 1e9, 4),
                    "step_algorithmic_gbs": step_bytes / (ms_step * 1e-3) / 1e9,
                    "step_hbm_frac": step_bytes / (ms_step * 1e-3) / 1e9 / peak},
         "peak_hbm_gb": mem["peak_hbm_gb"],
         "memory": mem,
         "stored_mode": {"backward": "stored edge record", "ms_per_step": ms_st / args.steps,
+                        "kernel_gbs": {k: round(algo_st[k] / (ms / max(cnt, 1) * 1e-3) / 1e9, 1)
+                                       for k, (cnt, ms) in k_st.items() if k in algo_st},
                         "grids_s": job_throughput(world, args.steps, ms_st),
                         "step_hbm_frac": step_bytes / (ms_st / args.steps * 1e-3) / 1e9 / peak,
                         "kernel_ms_per_step": {k: round(ms / args.steps, 4) for k, (cnt, ms) in k_st.items()},
