@@ -651,14 +651,13 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
   int rc;
   if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
-  // one CTA of three warps per SM for the zeros: the fused pass holds three CTAs of
-  // 256 threads x 80 registers per SM (61440 of the 65536 registers), and three warps
-  // of the zero kernel fit in the rest, so neither waits for the other's slots; a few
-  // warps per SM still keep the stores streaming
+  // two zero CTAs per SM, launched first: fewer warps make the zeros (and the fused
+  // pass beside them, measured) slower
   if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
   {
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
-    zero_tiles_kernel<S><<<(unsigned)ex->sms, 96, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf, (S*)gdef);
+    zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf,
+                                                                       (S*)gdef);
   }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
