@@ -57,6 +57,11 @@ struct FusedShared {
   int32_t first[KX][KY][TZ + 2];  //   and the id of its first patch
   uint32_t wsum[NTHREADS / 32 + 1];
   uint32_t nwi;
+  // DMC case words (dmc_case in common.cuh) and the cell-local edge lookup: beside
+  // three CTAs' shared memory the L1 cache is small, and these lookups sit on the
+  // dependent chains of the code and adjoint phases
+  uint64_t cases[METHOD == DMC ? 256 : 1];
+  uint8_t edge_of[24];
   __align__(16) S adj[fb_cap<S>()][8];
 };
 
@@ -96,10 +101,10 @@ __device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh
       const int wy = y + 1 - (b == 1 ? db : 0) - (c == 1 ? dc : 0);
       const int wj = j + 1 - (b == 2 ? db : 0) - (c == 2 ? dc : 0);
       const int s = (db << b) | (dc << c);
-      const int e = __ldg(g_edge_of + 3 * s + a);
-      const int rc = sh.rc[wx][wy][wj];
-      const int q = dmc_patch_of(dmc_case(rc), e);
-      const int cnt = __popc((uint32_t)(__ldg(&g_dmc_pmask.m[rc]) >> (12 * q)) & 0xfffu);
+      const int e = sh.edge_of[3 * s + a];
+      const uint64_t w = sh.cases[sh.rc[wx][wy][wj]];
+      const int q = dmc_patch_of(w, e);
+      const int cnt = (int)((w >> (32 + 4 * q)) & 15);  // the edges of patch q
       int64_t p = (int64_t)sh.first[wx][wy][wj] + (exact ? q : 0);
       if (p < 0 || p >= V || cnt == 0) {
         bad = true;
@@ -160,9 +165,10 @@ __device__ __noinline__ int fused_code_far(const Field<S>& f, int X, int Y, int 
 // dmc_resolve_m (kernels.cuh) with the neighbour's code from the masks when its
 // corners lie in them, otherwise from fused_code_far
 template <class S, int WX, int WY>
-__device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const Field<S>& f, int WX0, int WY0, int Z0,
-                                             int code, int X, int Y, int Z, const Geom& g) {
-  const int dir = dmc_dir(dmc_case(code));
+__device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const uint64_t* cases, const Field<S>& f,
+                                             int WX0, int WY0, int Z0, int code, int X, int Y, int Z,
+                                             const Geom& g) {
+  const int dir = dmc_dir(cases[code]);
   if (dir == 7) return code;
   const int comp = dir >> 1, d = (dir & 1) ? 1 : -1;
   const int NX = X + (comp == 0 ? d : 0), NY = Y + (comp == 1 ? d : 0), NZ = Z + (comp == 2 ? d : 0);
@@ -175,7 +181,7 @@ __device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const 
     ncode = code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], sft);
   else
     ncode = fused_code_far<S>(f, NX, NY, NZ);
-  return dmc_dir(dmc_case(ncode)) != 7 ? (code ^ 0xff) : code;
+  return dmc_dir(cases[ncode]) != 7 ? (code ^ 0xff) : code;
 }
 
 // one active point tile (see the top of this file)
@@ -246,8 +252,8 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
         sh.first[wx][wy][lane + 1] = (int32_t)base;
         continue;
       }
-      const int rc = nt ? fused_resolve<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g) : 0;
-      const uint32_t np = (uint32_t)dmc_npatch(dmc_case(rc));
+      const int rc = nt ? fused_resolve<S>(sh.m, sh.cases, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g) : 0;
+      const uint32_t np = (uint32_t)dmc_npatch(sh.cases[rc]);
       const uint32_t incl = warp_incl(np);
       sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
       sh.first[wx][wy][lane + 1] = (int32_t)(base + incl - np);
@@ -260,11 +266,11 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && Z >= 0 && Z < g.c[2]) {
         const int code = code8(sh.m[wx][wy], sh.m[wx + 1][wy], sh.m[wx][wy + 1], sh.m[wx + 1][wy + 1],
                                end ? TZ + 1 : 0);
-        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z, g);
+        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, sh.cases, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z, g);
       }
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
       sh.first[wx][wy][end ? TZ + 1 : 0] =
-          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(dmc_case(rc)));
+          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
     }
   }
   __syncthreads();
@@ -396,6 +402,9 @@ __global__ void __launch_bounds__(NTHREADS, 3)
   const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
   S scale[3];
   grad_scale<S>(g, normalize, scale);
+  if constexpr (METHOD == DMC) sh.cases[threadIdx.x & 255] = dmc_case(threadIdx.x & 255);
+  if (threadIdx.x < 24) sh.edge_of[threadIdx.x] = __ldg(g_edge_of + threadIdx.x);
+  __syncthreads();
   const unsigned n = *count;
   bool bad = false;
 #pragma unroll 1
