@@ -159,7 +159,21 @@ __device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METH
 // test needs it only for an ambiguous cell whose neighbour lies outside the masks
 template <class S>
 __device__ __noinline__ int fused_code_far(const Field<S>& f, int X, int Y, int Z) {
-  return cell_code_far<S>(f, X, Y, Z);
+  // the eight corners' loads issued together: clamped addresses, the pad value
+  // selected afterwards for corners outside the grid
+  S v[8];
+  bool in[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int x = X - 1 + (i & 1), y = Y - 1 + ((i >> 1) & 1), z = Z - 1 + ((i >> 2) & 1);
+    in[i] = (unsigned)x < (unsigned)f.n0 && (unsigned)y < (unsigned)f.n1 && (unsigned)z < (unsigned)f.n2;
+    const int cx = min(max(x, 0), f.n0 - 1), cy = min(max(y, 0), f.n1 - 1), cz = min(max(z, 0), f.n2 - 1);
+    v[i] = __ldg(f.sdf + ((int64_t)cx * f.n1 + cy) * f.n2 + cz);
+  }
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c |= ((in[i] ? v[i] : f.pad) >= f.iso) << i;
+  return c;
 }
 
 // dmc_resolve_m (kernels.cuh) with the neighbour's code from the masks when its
@@ -210,7 +224,9 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
   }
   S dmn, dmx;
   bool dseen = false;
-  load_masks<S, SH::WX, SH::WY, false>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
+  // all of a warp's mask rows in one batch of loads
+  load_masks<S, SH::WX, SH::WY, false, Field<S>, (SH::WX * SH::WY + NTHREADS / 32 - 1) / (NTHREADS / 32)>(
+      sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
   if (si < NSV) {
     if constexpr (METHOD == MC)
       sh.eb[sx][sy][sk] = Counts::lo(sv);

@@ -221,10 +221,10 @@ __device__ __forceinline__ void unpack_loc(int64_t l, int& X, int& Y, int& Z, in
 // Warp w takes rows w, w + NW, ...; it issues the loads of BATCH rows before their
 // ballots, so each warp keeps BATCH row loads in flight.  Tracks min / max of the
 // caller's (interior) values when TRACK.  Needs blockDim.x == NTHREADS.
-template <class S, int WX, int WY, bool TRACK, class F = Field<S>>
+template <class S, int WX, int WY, bool TRACK, class F = Field<S>, int BATCH = 8>
 __device__ __forceinline__ void load_masks(uint64_t (&m)[WX][WY], const F& f, int WX0, int WY0, int Z0, S& mn,
                                            S& mx, bool& seen) {
-  constexpr int NW = NTHREADS / 32, NR = WX * WY, BATCH = 8;
+  constexpr int NW = NTHREADS / 32, NR = WX * WY;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Z = Z0 - 1 + lane, Ze = Z0 + 31 + lane;
   const bool zin = (unsigned)(Z - 1) < (unsigned)f.n2;
@@ -1641,16 +1641,30 @@ template <class S>
 __device__ __forceinline__ void edge_adjoint2(const Field<S>& f, int X, int Y, int Z, int a, const S gvec[3], S c0[4],
                                               S c1[4]) {
   const int ex = a == 0, ey = a == 1, ez = a == 2;
-  const S d0 = f.at(X, Y, Z), d1 = f.at(X + ex, Y + ey, Z + ez);
+  // both end points' values and deforms loaded together from clamped addresses, the
+  // pad value (and a zero deform) selected afterwards for points outside the grid
+  const bool in0 = f.inside(X, Y, Z), in1 = f.inside(X + ex, Y + ey, Z + ez);
+  const int64_t i0 = ((int64_t)min(max(X - 1, 0), f.n0 - 1) * f.n1 + min(max(Y - 1, 0), f.n1 - 1)) * f.n2 +
+                     min(max(Z - 1, 0), f.n2 - 1);
+  const int64_t i1 = ((int64_t)min(max(X - 1 + ex, 0), f.n0 - 1) * f.n1 + min(max(Y - 1 + ey, 0), f.n1 - 1)) * f.n2 +
+                     min(max(Z - 1 + ez, 0), f.n2 - 1);
+  const S v0 = __ldg(f.sdf + i0), v1 = __ldg(f.sdf + i1);
+  S q0[3] = {S(0), S(0), S(0)}, q1[3] = {S(0), S(0), S(0)};
+  if (f.def) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const S u0 = __ldg(f.def + 3 * i0 + k), u1 = __ldg(f.def + 3 * i1 + k);
+      q0[k] = in0 ? u0 : S(0);
+      q1[k] = in1 ? u1 : S(0);
+    }
+  }
+  const S d0 = in0 ? v0 : f.pad, d1 = in1 ? v1 : f.pad;
   S t = S(0.5);
   if (d1 != d0) {
     S r = (f.iso - d0) / (d1 - d0);
     r = S(0) > r ? S(0) : r;
     t = r < S(1) ? r : S(1);
   }
-  S q0[3], q1[3];
-  f.deform(X, Y, Z, q0);
-  f.deform(X + ex, Y + ey, Z + ez, q1);
   const S dp[3] = {(S(X + ex) + q1[0]) - (S(X) + q0[0]), (S(Y + ey) + q1[1]) - (S(Y) + q0[1]),
                    (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
   const S adj_t = fma_rn(dp[2], gvec[2], fma_rn(dp[1], gvec[1], mul_rn(dp[0], gvec[0])));
