@@ -42,8 +42,12 @@ __host__ __device__ constexpr int fb_cap() {
 
 template <class S, int METHOD>
 struct FusedShared {
-  static constexpr int LO = METHOD == DMC ? 1 : 0;  // mask rows start at (X0 - LO, Y0 - LO)
-  static constexpr int WX = TX + 2 + LO, WY = TY + 2 + LO;
+  // mask rows start at (X0 - LO, Y0 - LO): MC, the edge rows' points; DMC, two rows
+  // further, so that the ambiguity test of every window cell finds its neighbour's
+  // code in the masks (on the noisy surfaces of dense fields most window rows hold
+  // ambiguous cells, and a neighbour from global memory stalls the row's warp)
+  static constexpr int LO = METHOD == DMC ? 2 : 0;
+  static constexpr int WX = TX + 2 + (METHOD == DMC ? 3 : 0), WY = TY + 2 + (METHOD == DMC ? 3 : 0);
   static constexpr int CX = TX + 1, CY = TY + 1;  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
   static constexpr int KX = METHOD == DMC ? TX + 2 : 1, KY = METHOD == DMC ? TY + 2 : 1;  // DMC window cell rows
   uint64_t m[WX][WY];
@@ -213,20 +217,21 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
   const int zc = Z0 / TZ;
   // segment values first, so that their loads overlap the mask loads: MC, the
   // crossing counts of the edge rows; DMC, the patch counts of the window cell rows
-  constexpr int RY = METHOD == MC ? CY : KY;
+  constexpr int RY = METHOD == MC ? CY : KY, SLO = METHOD == MC ? 0 : 1;
   constexpr int NSV = (METHOD == MC ? CX * CY : KX * KY) * 2;
   static_assert(NSV <= NTHREADS, "one segment value per thread");
   uint64_t sv = 0;
   const int si = threadIdx.x, sk = si & 1, sy = (si >> 1) % RY, sx = (si >> 1) / RY;
   if (si < NSV) {
-    const int X = X0 - LO + sx, Y = Y0 - LO + sy, c = zc + sk;
+    const int X = X0 - SLO + sx, Y = Y0 - SLO + sy, c = zc + sk;
     if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && c < g.nzc) sv = seg[g.seg(X, Y, c)];
   }
   S dmn, dmx;
   bool dseen = false;
-  // all of a warp's mask rows in one batch of loads
-  load_masks<S, SH::WX, SH::WY, false, Field<S>, (SH::WX * SH::WY + NTHREADS / 32 - 1) / (NTHREADS / 32)>(
-      sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
+  // a warp's mask rows in batches of at most eight loads (more spill registers)
+  constexpr int ROWS_PW = (SH::WX * SH::WY + NTHREADS / 32 - 1) / (NTHREADS / 32);
+  constexpr int MBATCH = ROWS_PW <= 10 ? ROWS_PW : (ROWS_PW + 1) / 2;
+  load_masks<S, SH::WX, SH::WY, false, Field<S>, MBATCH>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
   if (si < NSV) {
     if constexpr (METHOD == MC)
       sh.eb[sx][sy][sk] = Counts::lo(sv);
@@ -259,16 +264,17 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
       const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
       const uint32_t base = sh.pb[wx][wy][0];
+      const uint64_t ma = sh.m[wx + 1][wy + 1], mb = sh.m[wx + 2][wy + 1], mc = sh.m[wx + 1][wy + 2],
+                     md = sh.m[wx + 2][wy + 2];
       int code = 0;
-      if (row && Z0 + lane < g.c[2]) code = code8(sh.m[wx][wy], sh.m[wx + 1][wy], sh.m[wx][wy + 1], sh.m[wx + 1][wy + 1],
-                                                  lane + 1);
+      if (row && Z0 + lane < g.c[2]) code = code8(ma, mb, mc, md, lane + 1);
       const bool nt = code != 0 && code != 255;
       if (!__any_sync(0xffffffffu, nt)) {
         sh.rc[wx][wy][lane + 1] = 0;
         sh.first[wx][wy][lane + 1] = (int32_t)base;
         continue;
       }
-      const int rc = nt ? fused_resolve<S>(sh.m, sh.cases, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z0 + lane, g) : 0;
+      const int rc = nt ? fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z0 + lane, g) : 0;
       const uint32_t np = (uint32_t)dmc_npatch(sh.cases[rc]);
       const uint32_t incl = warp_incl(np);
       sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
@@ -280,9 +286,9 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       const int Z = end ? Z0 + TZ : Z0 - 1;
       int rc = 0;
       if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && Z >= 0 && Z < g.c[2]) {
-        const int code = code8(sh.m[wx][wy], sh.m[wx + 1][wy], sh.m[wx][wy + 1], sh.m[wx + 1][wy + 1],
-                               end ? TZ + 1 : 0);
-        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, sh.cases, f, X0 - 1, Y0 - 1, Z0, code, X, Y, Z, g);
+        const int code = code8(sh.m[wx + 1][wy + 1], sh.m[wx + 2][wy + 1], sh.m[wx + 1][wy + 2],
+                               sh.m[wx + 2][wy + 2], end ? TZ + 1 : 0);
+        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z, g);
       }
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
       sh.first[wx][wy][end ? TZ + 1 : 0] =
