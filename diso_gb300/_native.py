@@ -107,6 +107,7 @@ EXPORTS = {
     "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),
+    "diso_scan_wait_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p]),
     "diso_scratch_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "diso_last_error": (ctypes.c_char_p, []),
     "diso_version": (ctypes.c_char_p, []),

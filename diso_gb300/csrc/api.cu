@@ -377,7 +377,7 @@ int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s, bool pr
   ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
   {
     KernelTimer kt(ex, K_SCAN, s);
-    scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats, total_out);
+    scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(a, n, st, ex->stats, total_out, SCAN_SPIN_LIMIT);
   }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
@@ -948,7 +948,8 @@ int batch_count(diso_extractor* ex, cudaStream_t s) {
   const int64_t tiles = (ex->bseg_total + 1 + SCAN_TILE - 1) / SCAN_TILE;
   CUDA_TRY(cudaMemsetAsync(ex->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
   ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
-  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(ex->brecord, ex->bseg_total, st, ex->stats, nullptr);
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(ex->brecord, ex->bseg_total, st, ex->stats, nullptr,
+                                                                SCAN_SPIN_LIMIT);
   CUDA_TRY(cudaGetLastError());
   const int64_t* doffs = (const int64_t*)((char*)ex->bbound + sizeof(uint64_t) * (MAX_BATCH + 1));
   gather_bounds_kernel<<<1, 256, 0, s>>>(ex->brecord, doffs, n, ex->bbound);
@@ -1527,6 +1528,30 @@ int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n)
   return DISO_OK;
 }
 
+int diso_scan_wait_probe(diso_extractor* ex, unsigned spin_limit, void* stream) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (spin_limit < 1 || spin_limit > SCAN_SPIN_LIMIT)
+    return fail(DISO_ERR_ARG, "spin limit %u outside [1, %u]", spin_limit, SCAN_SPIN_LIMIT);
+  int rc = bind_device(ex);
+  if (rc != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  // two whole scan tiles in the extractor's split scratch; only tile 1 runs
+  const int64_t n = 2 * (int64_t)SCAN_TILE;
+  if ((rc = grow(ex->split, ex->split_cap, n + 1)) != DISO_OK) return rc;
+  const int64_t tiles = scan_reserve(ex, n);
+  if (tiles == 0) return DISO_ERR_CUDA;
+  CUDA_TRY(cudaMemsetAsync(ex->split, 0, (size_t)(n + 1) * sizeof(uint64_t), s));
+  scan_probe_prep_kernel<<<1, 64, 0, s>>>(ex->stats, ex->scan_flag, tiles, 1ull);
+  CUDA_TRY(cudaGetLastError());
+  ScanState st{ex->scan_flag, ex->scan_agg, ex->scan_incl};
+  scan_lookback_kernel<<<1, SCAN_THREADS, 0, s>>>(ex->split, n, st, ex->stats, nullptr, spin_limit);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(ex->stats_host, ex->stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (ex->stats_host->error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
+  return DISO_OK;
+}
+
 int64_t diso_scratch_bytes(const diso_extractor* ex) {
   if (!ex) return 0;
   int64_t b = ex->active_cap * (int64_t)sizeof(int) + ex->codes_cap * (int64_t)sizeof(CellRec) +
@@ -1739,7 +1764,8 @@ int forward_count_static(int method, StaticScratch* sc, int ctas, const void* sd
   const int64_t tiles = (g.nseg + 1 + SCAN_TILE - 1) / SCAN_TILE;
   CUDA_TRY(cudaMemsetAsync(sc->scan_flag, 0, (size_t)tiles * sizeof(uint32_t), s));
   ScanState st{sc->scan_flag, sc->scan_agg, sc->scan_incl};
-  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(seg, g.nseg, st, &sc->stats, nullptr);
+  scan_lookback_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(seg, g.nseg, st, &sc->stats, nullptr,
+                                                                SCAN_SPIN_LIMIT);
   CUDA_TRY(cudaGetLastError());
   Stats h;
   uint64_t total = 0;

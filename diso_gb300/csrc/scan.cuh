@@ -18,7 +18,7 @@ namespace diso {
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_ITEMS = 16;  // a thread's elements: 128 contiguous bytes
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr unsigned SCAN_SPIN_LIMIT = 1u << 22;
+constexpr unsigned SCAN_SPIN_LIMIT = 1u << 22;  // look-back polls per predecessor (64 ns sleeps), the default
 
 struct ScanState {
   uint32_t* flag;   // 0 none, 1 aggregate published, 2 inclusive prefix published
@@ -35,10 +35,11 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// total_out (may be null) also receives the total a[n]
+// total_out (may be null) also receives the total a[n]; spin_limit bounds the polls
+// of each predecessor's flag
 __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* __restrict__ a, int64_t n,
                                                                      ScanState st, Stats* stats,
-                                                                     uint64_t* total_out) {
+                                                                     uint64_t* total_out, unsigned spin_limit) {
   __shared__ uint64_t warp_tot[SCAN_THREADS / 32];
   __shared__ uint64_t tile_excl;
   __shared__ int64_t tile_id_s;
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(uint64_t* _
         if (idx >= 0) {
           unsigned spins = 0;
           while ((f = ld_acquire(st.flag + idx)) == 0u) {
-            if (++spins >= SCAN_SPIN_LIMIT) {
+            if (++spins >= spin_limit) {
               failed = true;
               break;
             }
@@ -160,6 +161,20 @@ __global__ void __launch_bounds__(256) count_prep_kernel(Stats* stats, uint32_t*
   if (threadIdx.x == 0) {
     Stats z = {};
     z.min_key = ~0ull;
+    *stats = z;
+  }
+  for (int64_t i = threadIdx.x; i < tiles; i += blockDim.x) scan_flag[i] = 0u;
+}
+
+// Set-up of the look-back wait probe (diso_scan_wait_probe): fresh status words, the
+// flags of `tiles` tiles cleared, and the scan's tile counter at `first`, so that the
+// tiles before `first` are never run and never publish their flags
+__global__ void scan_probe_prep_kernel(Stats* stats, uint32_t* __restrict__ scan_flag, int64_t tiles,
+                                       unsigned long long first) {
+  if (threadIdx.x == 0) {
+    Stats z = {};
+    z.min_key = ~0ull;
+    z.scan_tile = first;
     *stats = z;
   }
   for (int64_t i = threadIdx.x; i < tiles; i += blockDim.x) scan_flag[i] = 0u;

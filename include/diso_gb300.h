@@ -360,6 +360,16 @@ int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int cor
 int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
                   int64_t n_faces, int corners, void* body, void* stream);
 
+/* Check of the bounded device-side waits: runs the segment scan's look-back on two
+ * tiles of the extractor's scratch with only the second tile launched, so that the
+ * flag it waits for is never published, and each poll limited to spin_limit tries
+ * (1 .. 2^22; the forward's own scans use 2^22).  Returns DISO_ERR_SCAN with the
+ * scan's message when the wait gave up (the expected result), after which the
+ * extractor is usable as before; DISO_OK would mean the wait never ran out.  Lets a
+ * caller see that a stalled look-back ends in an error status instead of a hang.
+ * No counterpart in the reference.  Synchronises the stream. */
+int diso_scan_wait_probe(diso_extractor* ex, unsigned spin_limit, void* stream);
+
 /* Bytes of device memory the extractor holds as its own scratch (grow-only
  * buffers; not the caller's per-call `seg`, edge record or outputs), for memory
  * reports.  No counterpart in the reference. */

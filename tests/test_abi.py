@@ -113,6 +113,16 @@ def test_recompute_backward_checks_its_arguments(lib):
     lib.diso_destroy(h)
 
 
+def test_scan_wait_probe_checks_its_arguments(lib):
+    assert lib.diso_scan_wait_probe(None, 16, None) == 1
+    h = ctypes.c_void_p()
+    assert lib.diso_create(0, 0, ctypes.byref(h)) == 0
+    assert lib.diso_scan_wait_probe(h, 0, None) == 1
+    assert b"spin limit" in lib.diso_last_error()
+    assert lib.diso_scan_wait_probe(h, (1 << 22) + 1, None) == 1
+    lib.diso_destroy(h)
+
+
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     from diso_gb300 import _native
 
@@ -164,7 +174,8 @@ def _c_kind(decl):
     decl = re.sub(r"\b(const|struct)\b", " ", decl)
     if "*" in decl:
         return "pointer"
-    return {"int": "int", "int64_t": "int64", "uint64_t": "int64", "double": "double", "void": "void"}[decl.split()[0]]
+    return {"int": "int", "unsigned": "uint", "int64_t": "int64", "uint64_t": "int64", "double": "double",
+            "void": "void"}[decl.split()[0]]
 
 
 def _ctypes_kind(t):
@@ -172,7 +183,8 @@ def _ctypes_kind(t):
         return "void"
     if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
         return "pointer"
-    return {ctypes.c_int: "int", ctypes.c_int64: "int64", ctypes.c_uint64: "int64", ctypes.c_double: "double"}[t]
+    return {ctypes.c_int: "int", ctypes.c_uint: "uint", ctypes.c_int64: "int64", ctypes.c_uint64: "int64",
+            ctypes.c_double: "double"}[t]
 
 
 def test_bindings_match_the_header_signatures():

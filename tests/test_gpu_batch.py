@@ -101,3 +101,32 @@ def test_batch_plan_graph_replay(cuda_device, method):
     for i, f in enumerate(fields2):
         v, fc = extract(ex, torch.tensor(f, device=cuda_device), plan.deform[i], 0.0, True, True)
         assert torch.equal(meshes[i][1], fc) and torch.equal(meshes[i][0], v)
+
+
+@pytest.mark.parametrize("method,rq", [("mc", False), ("dmc", True)])
+def test_uneven_batch_at_full_size(cuda_device, method, rq):
+    """The batched workload itself: 64 grids, N log-uniform in [32, 256] (seeded),
+    spheres and rounded boxes with N(0, 0.02) noise, deform U(-0.3, 0.3) (about 10^8
+    cells in one flattened queue); every grid's mesh and gradients equal the
+    single-grid module's bit for bit."""
+    import bench
+    from diso_gb300 import DiffDMC, DiffDMCBatch, DiffMC, DiffMCBatch
+
+    sdfs, defs = bench.uneven_batch(64, device=cuda_device)
+    assert sum(s.numel() for s in sdfs) > 5e7
+    batch = DiffMCBatch(torch.float32) if method == "mc" else DiffDMCBatch(torch.float32)
+    single = DiffMC(torch.float32) if method == "mc" else DiffDMC(torch.float32)
+    kw = {} if method == "mc" else {"return_quads": rq}
+    s_b = [s.clone().requires_grad_(True) for s in sdfs]
+    d_b = [d.clone().requires_grad_(True) for d in defs]
+    outs = batch(s_b, d_b, **kw)
+    ws = [torch.randn(v.shape, device=cuda_device, generator=torch.Generator(cuda_device).manual_seed(k))
+          for k, (v, _) in enumerate(outs)]
+    sum((v * w).sum() for (v, _), w in zip(outs, ws)).backward()
+    for i in range(len(sdfs)):
+        s = sdfs[i].clone().requires_grad_(True)
+        d = defs[i].clone().requires_grad_(True)
+        v, f = single(s, d, **kw)
+        assert torch.equal(outs[i][1], f) and torch.equal(outs[i][0], v), f"grid {i}: mesh differs"
+        (v * ws[i]).sum().backward()
+        assert torch.equal(s_b[i].grad, s.grad) and torch.equal(d_b[i].grad, d.grad), f"grid {i}: gradients differ"

@@ -1,0 +1,116 @@
+"""The 256^3 configuration against the float64 oracle: the round cube
+(length(max(|x| - 0.5, 0)) - 0.1 on linspace(-1, 1)) and a dense U(-1, 1) field
+(every cell near a crossing: about 25 million DMC vertices and 50 million
+triangles, the reference README's "rand init" case), deform U(-0.45, 0.45),
+MC and DMC (quads and triangles), float32 and float64, loss = sum(verts * w) with
+seeded N(0, 1) weights.  The tolerances are the suite's (tests/helpers.py); the
+DMC triangle split is compared vectorised (quads may flip only on near-ties)."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import SPLIT_TIE, assert_faces_equal, assert_grads_close, assert_verts_close, oracle_grad_rtol
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+SEED = 0
+
+
+def make_field(kind, dtype):
+    rng = np.random.default_rng(SEED)
+    if kind == "random":
+        sdf = rng.uniform(-1, 1, (N, N, N))
+    else:
+        a = np.linspace(-1, 1, N)
+        X, Y, Z = np.meshgrid(a, a, a, indexing="ij")
+        q = np.stack([np.maximum(np.abs(c) - 0.5, 0) for c in (X, Y, Z)], -1)
+        sdf = np.sqrt((q * q).sum(-1)) - 0.1
+    deform = rng.uniform(-0.45, 0.45, (N, N, N, 3))
+    return sdf.astype(dtype), deform.astype(dtype)
+
+
+def split_pairs(tris):
+    """Triangle pairs of a quad split (vectorised): quads [Q, 4] and configs (1: (q0, q1, q3),
+    (q1, q2, q3); 2: (q0, q1, q2), (q0, q2, q3))."""
+    t = tris.reshape(-1, 2, 3)
+    a, b = t[:, 0], t[:, 1]
+    c1 = (a[:, 1] == b[:, 0]) & (a[:, 2] == b[:, 2])
+    c2 = (a[:, 0] == b[:, 0]) & (a[:, 2] == b[:, 1])
+    assert (c1 | c2).all(), "not quad split pairs"
+    quads = np.where(c1[:, None], np.stack([a[:, 0], a[:, 1], b[:, 1], a[:, 2]], 1),
+                     np.stack([a[:, 0], a[:, 1], a[:, 2], b[:, 2]], 1))
+    return quads, np.where(c1, 1, 2)
+
+
+def max_cos(V, i, j, k):
+    p = [V[i], V[j], V[k]]
+    out = None
+    for r in range(3):
+        o, u, w = p[r], p[(r + 1) % 3], p[(r + 2) % 3]
+        e1, e2 = u - o, w - o
+        e1 = e1 / np.maximum(np.linalg.norm(e1, axis=1, keepdims=True), 1e-12)
+        e2 = e2 / np.maximum(np.linalg.norm(e2, axis=1, keepdims=True), 1e-12)
+        c = (e1 * e2).sum(1)
+        out = c if out is None else np.maximum(out, c)
+    return out
+
+
+def assert_split_close(tris, tris_ref, verts_ref, dtype):
+    assert tris.shape == tris_ref.shape
+    if np.array_equal(tris, tris_ref):
+        return
+    q, c = split_pairs(tris)
+    qr, cr = split_pairs(tris_ref)
+    key = lambda Q: np.lexsort(Q.T[::-1])
+    i, ir = key(q), key(qr)
+    assert np.array_equal(q[i], qr[ir]), "different quad sets"
+    flip = c[i] != cr[ir]
+    F = qr[ir][flip]
+    V = verts_ref.astype(np.float64)
+    m1 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 3]), max_cos(V, F[:, 1], F[:, 2], F[:, 3]))
+    m2 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 2]), max_cos(V, F[:, 0], F[:, 2], F[:, 3]))
+    marg = np.abs(m1 - m2)
+    assert (marg < SPLIT_TIE[dtype]).all(), f"{int((marg >= SPLIT_TIE[dtype]).sum())} splits differ off a tie"
+
+
+CASES = [(kind, method, rq, dtype, recompute)
+         for kind in ("round_cube", "random")
+         for method, rq in (("mc", False), ("dmc", True), ("dmc", False))
+         for dtype in ("float32", "float64")
+         for recompute in ((False, True) if (method, rq, dtype) == ("dmc", True, "float32") else (False,))]
+
+
+@pytest.mark.parametrize("kind,method,rq,dtype,recompute", CASES)
+def test_config256_against_oracle(cuda_device, kind, method, rq, dtype, recompute):
+    from diso_gb300 import DiffDMC, DiffMC
+
+    sdf_np, def_np = make_field(kind, dtype)
+    dt = torch.float32 if dtype == "float32" else torch.float64
+    sdf = torch.tensor(sdf_np, device=cuda_device, requires_grad=True)
+    deform = torch.tensor(def_np, device=cuda_device, requires_grad=True)
+    if method == "mc":
+        verts, faces = DiffMC(dt, recompute=recompute)(sdf, deform)
+    else:
+        verts, faces = DiffDMC(dt, recompute=recompute)(sdf, deform, return_quads=rq)
+    m = O.MC if method == "mc" else O.DMC
+    v_ref, f_ref, _ = O.extract(m, sdf_np, def_np, 0.0, True, rq, dtype)
+    case = dict(method=method, dtype=dtype, iso=0.0, normalize=True, return_quads=rq, shape=(N, N, N))
+    v = verts.detach().cpu().numpy()
+    assert_verts_close(v, v_ref, case)
+    f = faces.cpu().numpy()
+    if method == "dmc" and not rq:
+        assert_split_close(f, f_ref, v_ref, dtype)
+    else:
+        assert_faces_equal(f, f_ref, case)
+    if kind == "random":
+        assert v.shape[0] > 1_000_000  # the dense case really is dense
+    del f, f_ref
+    w = np.random.default_rng(SEED + 1).standard_normal(v.shape).astype(dtype)
+    (verts * torch.tensor(w, device=cuda_device)).sum().backward()
+    gs_ref, gd_ref = O.backward(m, sdf_np, def_np, w, 0.0, True, dtype)
+    rtol = oracle_grad_rtol(dtype, (N, N, N))
+    assert_grads_close(sdf.grad.cpu().numpy(), gs_ref, dtype, "grad_sdf", rtol)
+    del gs_ref
+    assert_grads_close(deform.grad.cpu().numpy(), gd_ref, dtype, "grad_deform", rtol)

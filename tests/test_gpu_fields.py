@@ -88,3 +88,30 @@ def test_materialize_matches_the_field_definition(cuda_device, dtype):
     for cx, cy, cz, r in sph:
         ref = np.minimum(ref, np.sqrt((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2) - r)
     assert np.abs(got - ref).max() <= (1e-5 if dtype == "float32" else 1e-12)
+
+
+@pytest.mark.parametrize("method,rq", [("mc", False), ("dmc", True), ("dmc", False)])
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("kind,shape,iso,normalize", [("spheres", (96, 80, 112), 0.0, True),
+                                                      ("faces", (70, 65, 33), 0.0, True),
+                                                      ("spheres", (57, 40, 77), 0.1, False)])
+def test_fused_field_matches_oracle(cuda_device, method, rq, dtype, kind, shape, iso, normalize):
+    """The fused forward against the float64 oracle on the field's grid, so that the
+    evaluated-field path is tied to the reference's algorithm directly, not only
+    through the dense CUDA path."""
+    from diso_gb300 import DiffDMC, DiffMC
+    from helpers import assert_faces_equal, assert_verts_close
+    from oracle import oracle as O
+
+    dt = DT[dtype]
+    field = _field(kind, cuda_device, dt)
+    grid = field.materialize(shape, dt).cpu().numpy()
+    if method == "mc":
+        v, f = DiffMC(dt).forward_field(field, shape, iso, normalize)
+    else:
+        v, f = DiffDMC(dt).forward_field(field, shape, iso, rq, normalize)
+    m = O.MC if method == "mc" else O.DMC
+    v_ref, f_ref, _ = O.extract(m, grid, None, iso, normalize, rq, dtype)
+    case = dict(method=method, dtype=dtype, iso=iso, normalize=normalize, return_quads=rq, shape=shape)
+    assert_verts_close(v.cpu().numpy(), v_ref, case)
+    assert_faces_equal(f.cpu().numpy(), f_ref, case, v_ref)

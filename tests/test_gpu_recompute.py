@@ -148,3 +148,29 @@ def test_recompute_detects_a_changed_grid(cuda_device):
         s.add_(0.5)  # in place, after the forward: autograd's version check refuses the backward
     with pytest.raises(RuntimeError):
         v.sum().backward()
+
+
+@pytest.mark.parametrize("method,kw", [("mc", {}), ("dmc", {"return_quads": True}), ("dmc", {})])
+@pytest.mark.parametrize("recompute", [False, True])
+def test_interleaved_forwards_before_one_backward(cuda_device, method, kw, recompute):
+    """Forward of grid A, forward of grid B on the same module, then one backward of
+    lossA + lossB: the case the reference re-runs its forward in backward for
+    (diso/__init__.py:32, 86).  Each grid's gradients equal those of a module that
+    saw only that grid."""
+    sdf_a, def_a = _inputs(40, torch.float32, cuda_device, 11)
+    sdf_b, def_b = _dense((33, 45, 38), torch.float32, cuda_device, 12)
+    mod = _module(method, torch.float32, recompute)
+    sa, da = sdf_a.clone().requires_grad_(True), def_a.clone().requires_grad_(True)
+    sb, db = sdf_b.clone().requires_grad_(True), def_b.clone().requires_grad_(True)
+    va, fa = mod(sa, da, **kw)
+    vb, fb = mod(sb, db, **kw)
+    wa = torch.randn(va.shape, device=cuda_device, generator=torch.Generator(cuda_device).manual_seed(1))
+    wb = torch.randn(vb.shape, device=cuda_device, generator=torch.Generator(cuda_device).manual_seed(2))
+    ((va * wa).sum() + (vb * wb).sum()).backward()
+    for s_in, d_in, w, v0, f0, s_g, d_g in ((sdf_a, def_a, wa, va, fa, sa, da), (sdf_b, def_b, wb, vb, fb, sb, db)):
+        s = s_in.clone().requires_grad_(True)
+        d = d_in.clone().requires_grad_(True)
+        v, f = _module(method, torch.float32, recompute)(s, d, **kw)
+        assert torch.equal(v, v0.detach()) and torch.equal(f, f0)
+        (v * w).sum().backward()
+        assert torch.equal(s.grad, s_g.grad) and torch.equal(d.grad, d_g.grad)
