@@ -57,7 +57,21 @@ def max_cos(V, i, j, k):
     return out
 
 
-def assert_split_close(tris, tris_ref, verts_ref, dtype):
+def margins(V, F):
+    """(max corner cosine of split 1, of split 2) per quad, in float64."""
+    V = V.astype(np.float64)
+    m1 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 3]), max_cos(V, F[:, 1], F[:, 2], F[:, 3]))
+    m2 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 2]), max_cos(V, F[:, 0], F[:, 2], F[:, 3]))
+    return m1, m2
+
+
+def assert_split_close(tris, tris_ref, verts, verts_ref, dtype):
+    """The same quads; a quad may be split differently from the oracle's only where
+    the choice is a near-tie on the oracle's vertices, or where it is the right
+    choice (the smaller largest corner cosine, evaluated in float64) on the vertices
+    this extraction returned: in float32 those differ from the oracle's float64
+    vertices by rounding, which flips the choice for nearly degenerate quads of
+    dense random fields."""
     assert tris.shape == tris_ref.shape
     if np.array_equal(tris, tris_ref):
         return
@@ -67,12 +81,12 @@ def assert_split_close(tris, tris_ref, verts_ref, dtype):
     i, ir = key(q), key(qr)
     assert np.array_equal(q[i], qr[ir]), "different quad sets"
     flip = c[i] != cr[ir]
-    F = qr[ir][flip]
-    V = verts_ref.astype(np.float64)
-    m1 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 3]), max_cos(V, F[:, 1], F[:, 2], F[:, 3]))
-    m2 = np.maximum(max_cos(V, F[:, 0], F[:, 1], F[:, 2]), max_cos(V, F[:, 0], F[:, 2], F[:, 3]))
-    marg = np.abs(m1 - m2)
-    assert (marg < SPLIT_TIE[dtype]).all(), f"{int((marg >= SPLIT_TIE[dtype]).sum())} splits differ off a tie"
+    F, mine = qr[ir][flip], c[i][flip]
+    r1, r2 = margins(verts_ref, F)
+    o1, o2 = margins(verts, F)
+    tie = SPLIT_TIE[dtype]
+    ok = (np.abs(r1 - r2) < tie) | (np.abs(o1 - o2) < tie) | (np.where(o1 < o2, 1, 2) == mine)
+    assert ok.all(), f"{int((~ok).sum())} of {len(F)} differing splits are neither ties nor right for the vertices"
 
 
 CASES = [(kind, method, rq, dtype, recompute)
@@ -101,7 +115,7 @@ def test_config256_against_oracle(cuda_device, kind, method, rq, dtype, recomput
     assert_verts_close(v, v_ref, case)
     f = faces.cpu().numpy()
     if method == "dmc" and not rq:
-        assert_split_close(f, f_ref, v_ref, dtype)
+        assert_split_close(f, f_ref, v, v_ref, dtype)
     else:
         assert_faces_equal(f, f_ref, case)
     if kind == "random":
