@@ -4,7 +4,8 @@
 triangles, the reference README's "rand init" case), deform U(-0.45, 0.45),
 MC and DMC (quads and triangles), float32 and float64, loss = sum(verts * w) with
 seeded N(0, 1) weights.  The tolerances are the suite's (tests/helpers.py); the
-DMC triangle split is compared vectorised (quads may flip only on near-ties)."""
+DMC triangle split is compared vectorised (assert_split_close says which quads may
+be split differently from the oracle)."""
 import numpy as np
 import pytest
 import torch
