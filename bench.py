@@ -180,12 +180,16 @@ def run_batched(device, method, steps=10, warmup=3, ngrids=64):
         plan.deform[i].copy_(d)
     nv, _ = plan.size_outputs()
     plan.grad_verts[:nv].copy_(torch.cat(ws))
+    from diso_gb300 import tune
+
+    tuned = tune.tune_plan(plan)
     ms_eager = timed(plan.run, steps)
     plan.capture()
     ms_graph = timed(plan.replay, steps)
     plan.results()
     return {"grids": ngrids, "loop_grids_s": ngrids / (ms_loop * 1e-3), "batched_grids_s": ngrids / (ms_eager * 1e-3),
             "graph_grids_s": ngrids / (ms_graph * 1e-3), "speedup_vs_loop": ms_loop / ms_graph,
+            "launch": tuned["params"],
             "ms_loop": ms_loop, "ms_graph": ms_graph}
 
 
@@ -561,7 +565,7 @@ def peak_memory(ext, s, d, w):
 
 
 def run_ours(args, rank, world, device):
-    from diso_gb300 import DiffDMC
+    from diso_gb300 import DiffDMC, tune
     from diso_gb300 import _native as N
 
     n = args.n
@@ -569,6 +573,9 @@ def run_ours(args, rank, world, device):
     deform = deform_field(n, device)
     # the large configuration: the backward recomputes the crossing lists
     ext = DiffDMC(torch.float32, recompute=True)
+    # launch widths from the package's autotuner (timed on a synthetic field of this
+    # size, outside the timed region; cached per GPU, method, dtype, size and mode)
+    tuned = tune.tune_module(ext, (n, n, n), retune=args.retune)
     s = sdf.clone().requires_grad_(True)
     d = deform.clone().requires_grad_(True)
     v, f = ext(s, d, return_quads=True)
@@ -582,6 +589,7 @@ def run_ours(args, rank, world, device):
     # the same workload with the forward's edge record and gradient buffers kept for
     # the backward (stored mode), for comparison
     stored = DiffDMC(torch.float32)
+    tuned_st = tune.tune_module(stored, (n, n, n), retune=args.retune)
     ms_st, k_st, ph_st, _ = time_steps(stored, s, d, w, args.steps, args.warmup, world)
     mem_st = peak_memory(stored, s, d, w)
     del stored
@@ -697,12 +705,15 @@ def run_ours(args, rank, world, device):
                    "kernel_gbs": {k: round(algo[k] / (per_launch[k] * 1e-3) / 1e9, 1) for k in per_launch
                                   if k in algo},
                    "active_point_tiles": act_pts // 1024,
+                   "launch": {"tuned": tuned["params"], "tuned_ms": round(tuned["ms"], 4),
+                              "default_ms": round(tuned["default_ms"], 4), "trials": tuned["trials"]},
                    "step_algorithmic_gb": round(step_bytes / 1e9, 4),
                    "step_algorithmic_gbs": step_bytes / (ms_step * 1e-3) / 1e9,
                    "step_hbm_frac": step_bytes / (ms_step * 1e-3) / 1e9 / peak},
         "peak_hbm_gb": mem["peak_hbm_gb"],
         "memory": mem,
         "stored_mode": {"backward": "stored edge record", "ms_per_step": ms_st / args.steps,
+                        "launch": tuned_st["params"],
                         "kernel_gbs": {k: round(algo_st[k] / (ms / max(cnt, 1) * 1e-3) / 1e9, 1)
                                        for k, (cnt, ms) in k_st.items() if k in algo_st},
                         "grids_s": job_throughput(world, args.steps, ms_st),
@@ -813,6 +824,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--retune", action="store_true", help="time the launch widths again instead of the cached ones")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     args = ap.parse_args()

@@ -21,6 +21,10 @@ F32, F64 = 0, 1
 GRAD_EXACT = 1
 GRAD_ZEROED = 2
 
+# launch parameters of diso_tune_set
+TUNE_PARAMS = {"count_ctas": 0, "emit_ctas": 1, "gather_ctas": 2, "fused_ctas": 3, "zero_ctas": 4, "edge_ctas": 5,
+               "batch_ctas": 6, "zero_share": 7}
+
 _lock = threading.Lock()
 _lib = None
 
@@ -107,6 +111,8 @@ EXPORTS = {
     "diso_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_timing_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),
+    "diso_tune_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "diso_tune_value": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "diso_scan_wait_probe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p]),
     "diso_scratch_bytes": (ctypes.c_int64, [ctypes.c_void_p]),
     "diso_last_error": (ctypes.c_char_p, []),
@@ -197,6 +203,16 @@ class Extractor:
         check(lib().diso_forward_count(self._h, ptr(sdf), *sdf.shape, iso, pad, ptr(seg),
                                        stream_of(sdf.device), ctypes.byref(c)), "forward count")
         return c
+
+    def set_launch(self, params: dict):
+        """Launch widths for this extractor's later calls ({name: value}, names of
+        TUNE_PARAMS; 0 restores a default); outputs do not depend on them."""
+        for name, value in params.items():
+            check(lib().diso_tune_set(self._h, TUNE_PARAMS[name], int(value)), f"launch parameter {name}")
+
+    def launch(self) -> dict:
+        """The launch widths set on this extractor (0: default)."""
+        return {name: int(lib().diso_tune_value(self._h, i)) for name, i in TUNE_PARAMS.items()}
 
     def scratch_bytes(self) -> int:
         """Device bytes held by this extractor's own scratch buffers."""

@@ -78,6 +78,10 @@ struct diso_extractor {
   int emit_ctas = 0;             // the same for the emit
   int fused_ctas = 0;            // the same for the fused backward
   int fused_smem = 0;            // its dynamic shared memory per CTA
+  int per_sm[4] = {1, 1, 1, 1};  // resident CTAs per SM of the count (TMA), emit, gather, fused backward
+  // launch widths set by diso_tune_set (0: the default), and the zeros' count share
+  int tune[DISO_TUNE_N] = {};
+  double zero_share = 0.35;
   int sms = 0;
   cudaStream_t side = nullptr;   // second stream of the backward (zeros of the inactive point tiles)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -217,6 +221,21 @@ int grow(T*& p, int64_t& cap, int64_t need) {
   return DISO_OK;
 }
 
+// ------------------------------------------------------------------ launch widths
+
+// Persistent CTAs of a kernel: `dflt` (all that fit) unless diso_tune_set chose a
+// number per SM (at most the `cap` per SM that fit); every kernel's output is the
+// same for any width.
+inline unsigned tuned_ctas(const diso_extractor* ex, int param, int dflt, int cap) {
+  const int v = ex->tune[param];
+  return (unsigned)std::max(1, v > 0 ? ex->sms * std::min(v, cap) : dflt);
+}
+// CTAs of the kernels sized in CTAs per SM with a fixed default (zeros, edge pass, batches)
+inline unsigned per_sm_ctas(const diso_extractor* ex, int param, int dflt_per_sm) {
+  const int v = ex->tune[param];
+  return (unsigned)std::max(1, ex->sms * (v > 0 ? v : dflt_per_sm));
+}
+
 // ------------------------------------------------------------------ TMA tensor maps
 
 // cuTensorMapEncodeTiled from the driver, looked up once
@@ -296,12 +315,14 @@ int bind_device(diso_extractor* ex) {
     else
       CUDA_TRY(tma_occupancy<double>(ex->method, &per_tma));
     ex->tma_ctas = sms * std::max(per_tma, 1);
+    ex->per_sm[0] = std::max(per_tma, 1);
     int per_g = 0;
     if (ex->dtype == DISO_F32)
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_g, gather_list_kernel<float>, NTHREADS, 0));
     else
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_g, gather_list_kernel<double>, NTHREADS, 0));
     ex->gather_ctas = sms * std::max(per_g, 1);
+    ex->per_sm[2] = std::max(per_g, 1);
     int per_e = 0;
     if (ex->dtype == DISO_F32)
       CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -312,6 +333,7 @@ int bind_device(diso_extractor* ex) {
           &per_e, ex->method == DISO_MC ? (const void*)mc_emit_kernel<double> : (const void*)dmc_emit_kernel<double>,
           NTHREADS, 0));
     ex->emit_ctas = sms * std::max(per_e, 1);
+    ex->per_sm[1] = std::max(per_e, 1);
     int per_f = 0;
     const void* fk = ex->dtype == DISO_F32
                          ? (ex->method == DISO_MC ? (const void*)fused_backward_kernel<float, MC>
@@ -324,6 +346,7 @@ int bind_device(diso_extractor* ex) {
     CUDA_TRY(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, fk, NTHREADS, ex->fused_smem));
     ex->fused_ctas = sms * std::max(per_f, 1);
+    ex->per_sm[3] = std::max(per_f, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
@@ -438,7 +461,8 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   if (tma) {
     const int64_t units = count_tma_units(g);
     const int64_t want =
-        std::max<int64_t>(ex->tma_ctas, (units * TMA_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
+        std::max<int64_t>(tuned_ctas(ex, DISO_TUNE_COUNT_CTAS, ex->tma_ctas, ex->per_sm[0]),
+                          (units * TMA_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     const size_t smem = count_tma_smem<S>();
     ZeroJob zj;
@@ -548,7 +572,8 @@ int forward_emit(diso_extractor* ex, const void* sdf, const void* deform, int nx
                  double padval, const uint64_t* seg, int normalize, void* verts, int64_t* faces, void* record,
                  cudaStream_t s) {
   if (ex->last_active <= 0) return flush_emit_zero(ex, s);
-  const unsigned grid = (unsigned)std::min<int64_t>(ex->last_active, ex->emit_ctas);
+  const unsigned grid = (unsigned)std::min<int64_t>(
+      ex->last_active, tuned_ctas(ex, DISO_TUNE_EMIT_CTAS, ex->emit_ctas, ex->per_sm[1]));
   return emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record, grid,
                         INT64_MAX, INT64_MAX, s);
 }
@@ -566,7 +591,8 @@ int forward_all(diso_extractor* ex, const void* sdf, const void* deform, int nx,
   if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
   // the emit is queued before the host waits for the counts, and still runs when it returns
   if ((rc = emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record,
-                           (unsigned)ex->emit_ctas, vcap, fcap, s)) != DISO_OK)
+                           tuned_ctas(ex, DISO_TUNE_EMIT_CTAS, ex->emit_ctas, ex->per_sm[1]), vcap, fcap, s)) !=
+      DISO_OK)
     return rc;
   if ((rc = count_read<S>(ex, nx, ny, nz, iso, seg, s, out)) != DISO_OK) return rc;
   out->emitted = (out->n_verts <= vcap && out->n_faces <= fcap) ? 1 : 0;
@@ -574,7 +600,7 @@ int forward_all(diso_extractor* ex, const void* sdf, const void* deform, int nx,
 }
 
 // CTAs of the persistent edge pass
-inline unsigned edge_ctas(const diso_extractor* ex) { return (unsigned)std::max(1, ex->sms * 8); }
+inline unsigned edge_ctas(const diso_extractor* ex) { return per_sm_ctas(ex, DISO_TUNE_EDGE_CTAS, 8); }
 
 // CTAs of a grid-stride pass over n items of 256 threads, at most `cap`
 inline unsigned stride_ctas(int64_t n, unsigned cap) {
@@ -610,8 +636,8 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
     if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
     // few CTAs per SM, so that the gather of the active tiles finds room beside them
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
-    zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf,
-                                                                       (S*)gdef);
+    zero_tiles_kernel<S><<<per_sm_ctas(ex, DISO_TUNE_ZERO_CTAS, 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g),
+                                                                                        (S*)gsdf, (S*)gdef);
     CUDA_TRY(cudaGetLastError());
   }
   CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
@@ -631,7 +657,7 @@ int backward(diso_extractor* ex, const void* sdf, const void* deform, int nx, in
   CUDA_TRY(cudaGetLastError());
   {
     KernelTimer kt(ex, K_GATHER, s);
-    gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(f, g, seg, ex->plist, ex->plist_n, record,
+    gather_list_kernel<S><<<tuned_ctas(ex, DISO_TUNE_GATHER_CTAS, ex->gather_ctas, ex->per_sm[2]), NTHREADS, 0, s>>>(f, g, seg, ex->plist, ex->plist_n, record,
                                                                         (S*)gsdf, (S*)gdef);
   }
   CUDA_TRY(cudaGetLastError());
@@ -656,8 +682,8 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
   {
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
-    zero_tiles_kernel<S><<<(unsigned)(ex->sms * 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g), (S*)gsdf,
-                                                                       (S*)gdef);
+    zero_tiles_kernel<S><<<per_sm_ctas(ex, DISO_TUNE_ZERO_CTAS, 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g),
+                                                                                        (S*)gsdf, (S*)gdef);
   }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
@@ -670,10 +696,12 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   {
     KernelTimer kt(ex, K_FUSED_BWD, s);
     if (ex->method == DISO_MC)
-      fused_backward_kernel<S, MC><<<(unsigned)ex->fused_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+      fused_backward_kernel<S, MC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
+                                     (size_t)ex->fused_smem, s>>>(
           f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gsdf, (S*)gdef, ex->stats);
     else
-      fused_backward_kernel<S, DMC><<<(unsigned)ex->fused_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+      fused_backward_kernel<S, DMC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
+                                      (size_t)ex->fused_smem, s>>>(
           f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats);
   }
   CUDA_TRY(cudaGetLastError());
@@ -751,7 +779,7 @@ int take_zero_job(diso_extractor* ex, const Geom& g, int64_t units, unsigned gri
   zj->n0 = nv[0] * 16;
   const int64_t n = (nv[0] + nv[1]) * 16;
   if (n == 0) return DISO_OK;
-  const int64_t split = (int64_t)((double)n * ZERO_COUNT_SHARE) / 16 * 16;
+  const int64_t split = (int64_t)((double)n * ex->zero_share) / 16 * 16;
   ex->zemit = *zj;
   ex->zemit.begin = split;
   ex->zemit.end = n;
@@ -968,7 +996,7 @@ template <class S>
 int batch_emit(diso_extractor* ex, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
                void* record, cudaStream_t s) {
   const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
-  const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
+  const unsigned grid = per_sm_ctas(ex, DISO_TUNE_BATCH_CTAS, 4);
   const EdgeRecord<S> rec = batch_record<S>(ex, record, vcap, fcap);
   if (ex->method == DISO_MC)
     batch_emit_kernel<S, MC><<<grid, NTHREADS, 0, s>>>(d, ex->active, &ex->bstats->n_active, (S*)verts, faces, vcap,
@@ -984,13 +1012,13 @@ template <class S>
 int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv, void* record, int64_t vcap,
                    int64_t fcap, cudaStream_t s) {
   const BatchGrid<S>* d = (const BatchGrid<S>*)ex->bdesc;
-  const unsigned grid = (unsigned)std::max(1, ex->bwork_ctas);
+  const unsigned grid = per_sm_ctas(ex, DISO_TUNE_BATCH_CTAS, 4);
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
   const EdgeRecord<S> rec = batch_record<S>(ex, record, vcap, fcap);
   (void)grid;
   int rc;
   if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
-  const unsigned zgrid = (unsigned)(ex->sms * 2), lgrid = stride_ctas(ex->bptiles, ex->sms * 8);
+  const unsigned zgrid = per_sm_ctas(ex, DISO_TUNE_ZERO_CTAS, 2), lgrid = stride_ctas(ex->bptiles, ex->sms * 8);
   if (ex->method == DISO_MC)
     batch_zero_tiles_kernel<S, MC><<<zgrid, 256, 0, ex->side>>>(d, ex->bn, ex->bptiles, vcap, fcap);
   else
@@ -1011,7 +1039,8 @@ int batch_backward(diso_extractor* ex, int normalize, int flags, const void* gv,
                                                                     normalize, exact);
   }
   CUDA_TRY(cudaGetLastError());
-  batch_gather_list_kernel<S><<<(unsigned)ex->gather_ctas, NTHREADS, 0, s>>>(d, ex->bn, ex->plist, ex->plist_n,
+  batch_gather_list_kernel<S><<<tuned_ctas(ex, DISO_TUNE_GATHER_CTAS, ex->gather_ctas, ex->per_sm[2]), NTHREADS, 0,
+                                s>>>(d, ex->bn, ex->plist, ex->plist_n,
                                                                             record);
   CUDA_TRY(cudaGetLastError());
   return side_join(ex, s);
@@ -1526,6 +1555,21 @@ int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n)
   }
   *n = std::min(k, max);
   return DISO_OK;
+}
+
+int diso_tune_set(diso_extractor* ex, int param, int value) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  if (param < 0 || param >= DISO_TUNE_N) return fail(DISO_ERR_ARG, "unknown launch parameter %d", param);
+  const int hi = param == DISO_TUNE_ZERO_SHARE ? 1000 : 64;
+  if (value < 0 || value > hi) return fail(DISO_ERR_ARG, "value %d of launch parameter %d outside [0, %d]", value, param, hi);
+  ex->tune[param] = value;
+  if (param == DISO_TUNE_ZERO_SHARE) ex->zero_share = value > 0 ? value / 1000.0 : ZERO_COUNT_SHARE;
+  return DISO_OK;
+}
+
+int diso_tune_value(const diso_extractor* ex, int param) {
+  if (!ex || param < 0 || param >= DISO_TUNE_N) return -1;
+  return ex->tune[param];
 }
 
 int diso_scan_wait_probe(diso_extractor* ex, unsigned spin_limit, void* stream) {

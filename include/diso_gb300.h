@@ -360,6 +360,32 @@ int64_t diso_mesh_ply_bytes(int dtype, int64_t n_verts, int64_t n_faces, int cor
 int diso_mesh_ply(diso_extractor* ex, const void* verts, const void* normals, int64_t n_verts, const int64_t* faces,
                   int64_t n_faces, int corners, void* body, void* stream);
 
+/* ---- Launch widths ----
+ * Free parameters of the kernels' launches, for the package's autotuner
+ * (diso_gb300/tune.py), which times candidates on the caller's GPU and grid size and
+ * caches the winners.  None changes any output: every kernel gives the same bits for
+ * any width.  The reference fixes its block size (BLOCK_SIZE 512, src/cumc.cu:93;
+ * src/cudualmc.cu:93) and has nothing to tune. */
+enum {
+  DISO_TUNE_COUNT_CTAS = 0,  /* persistent CTAs per SM of the forward count (capped by occupancy) */
+  DISO_TUNE_EMIT_CTAS = 1,   /* ... of the forward emit */
+  DISO_TUNE_GATHER_CTAS = 2, /* ... of the stored backward's point gather (single grids and batches) */
+  DISO_TUNE_FUSED_CTAS = 3,  /* ... of the recompute backward's fused pass */
+  DISO_TUNE_ZERO_CTAS = 4,   /* CTAs per SM of the point-tile zeros beside a backward (default 2) */
+  DISO_TUNE_EDGE_CTAS = 5,   /* CTAs per SM of the stored backward's edge pass (default 8) */
+  DISO_TUNE_BATCH_CTAS = 6,  /* CTAs per SM of the batches' emit and backward passes (default 4) */
+  DISO_TUNE_ZERO_SHARE = 7,  /* stored mode: per mille of the gradient zeros the count writes (default 350) */
+  DISO_TUNE_N = 8
+};
+
+/* Set launch parameter `param` of the extractor's later calls to `value` (0 restores
+ * the default; CTAs per SM 1..64, the zero share 1..1000 per mille).  No counterpart
+ * in the reference. */
+int diso_tune_set(diso_extractor* ex, int param, int value);
+
+/* The value set for `param` (0: the default), -1 for a bad argument. */
+int diso_tune_value(const diso_extractor* ex, int param);
+
 /* Check of the bounded device-side waits: runs the segment scan's look-back on two
  * tiles of the extractor's scratch with only the second tile launched, so that the
  * flag it waits for is never published, and each poll limited to spin_limit tries
