@@ -555,9 +555,12 @@ def job_throughput(world, steps, ms):
 
 def time_steps(ext, s, d, w, steps, warmup, world, with_clocks=False):
     """`steps` timed forward + backward steps of `ext` on the resident inputs (after
-    `warmup` untimed ones), bracketed by barrier + synchronize; CUDA events around
-    every launch of the extractor (its timing mode) and around the phases.  Returns
-    (ms over all steps, max over ranks; per-kernel totals; phase means; clocks)."""
+    `warmup` untimed ones), bracketed by barrier + synchronize, with CUDA events on
+    the stream around the whole loop only; then the same number of steps again with
+    CUDA events around every launch of the extractor (its timing mode) and around
+    the phases, for the per-kernel breakdown.  Returns (ms over the first loop's
+    steps, max over ranks; per-kernel totals and phase means of the second loop;
+    clocks sampled during the first)."""
     import diso_gb300.extraction as X
 
     def step():
@@ -572,9 +575,6 @@ def time_steps(ext, s, d, w, steps, warmup, world, with_clocks=False):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    ph = PhaseEvents()
-    X.phase_timer = ph
-    ext._ex.timing(True)  # CUDA events around every launch of the extractor, on its stream
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clk = ClockSampler(smi_id(s.device)) if with_clocks else None
     if clk:
@@ -588,13 +588,21 @@ def time_steps(ext, s, d, w, steps, warmup, world, with_clocks=False):
     finally:
         if clk:
             clk.__exit__()
-        X.phase_timer = None
-    kernels = ext._ex.timing_read()
-    ext._ex.timing(False)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     ms = max_over_ranks(t0.elapsed_time(t1), world, s.device)
+    ph = PhaseEvents()
+    X.phase_timer = ph
+    ext._ex.timing(True)  # CUDA events around every launch of the extractor, on its stream
+    try:
+        for _ in range(steps):
+            step()
+        torch.cuda.synchronize()
+    finally:
+        X.phase_timer = None
+    kernels = ext._ex.timing_read()
+    ext._ex.timing(False)
     return ms, kernels, ph.mean_ms(), (clk.summary() if clk else None)
 
 
