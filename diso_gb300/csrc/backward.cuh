@@ -31,13 +31,13 @@
 
 namespace diso {
 
-// Window edges whose adjoints a tile keeps in shared memory: sized so that four
-// CTAs share an SM (the tile's state is about 56 KB of dynamic shared memory in
-// either precision); at 512^3 on a noisy union of spheres about 97% of the windows
+// Window edges whose adjoints a tile keeps in shared memory: sized so that three
+// CTAs share an SM (the tile's state is about 72 KB of dynamic shared memory in
+// either precision); at 512^3 on a noisy union of spheres about 99% of the windows
 // fit (the largest hold some 1900 edges, the median about 400).
 template <class S>
 __host__ __device__ constexpr int fb_cap() {
-  return sizeof(S) == 4 ? 1376 : 688;
+  return sizeof(S) == 4 ? 1664 : 832;
 }
 
 template <class S, int METHOD>
@@ -58,7 +58,7 @@ struct FusedShared {
   uint16_t witems[fb_cap<S>()];
   uint8_t w32[CX][CY];
   uint8_t rc[KX][KY][TZ + 2];     // DMC window cells (z index j + 1 for Z0 + j): code after the ambiguity test
-  int16_t first[KX][KY][TZ + 2];  //   and the id of its first patch less its row's pb[..][0]
+  int32_t first[KX][KY][TZ + 2];  //   and the id of its first patch
   uint32_t wsum[NTHREADS / 32 + 1];
   uint32_t nwi;
   // DMC case words (dmc_case in common.cuh) and the cell-local edge lookup: beside
@@ -109,7 +109,7 @@ __device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh
       const uint64_t w = sh.cases[sh.rc[wx][wy][wj]];
       const int q = dmc_patch_of(w, e);
       const int cnt = (int)((w >> (32 + 4 * q)) & 15);  // the edges of patch q
-      int64_t p = (int64_t)sh.pb[wx][wy][0] + sh.first[wx][wy][wj] + (exact ? q : 0);
+      int64_t p = (int64_t)sh.first[wx][wy][wj] + (exact ? q : 0);
       if (p < 0 || p >= V || cnt == 0) {
         bad = true;
         p = 0;
@@ -271,14 +271,14 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       const bool nt = code != 0 && code != 255;
       if (!__any_sync(0xffffffffu, nt)) {
         sh.rc[wx][wy][lane + 1] = 0;
-        sh.first[wx][wy][lane + 1] = 0;
+        sh.first[wx][wy][lane + 1] = (int32_t)base;
         continue;
       }
       const int rc = nt ? fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z0 + lane, g) : 0;
       const uint32_t np = (uint32_t)dmc_npatch(sh.cases[rc]);
       const uint32_t incl = warp_incl(np);
       sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
-      sh.first[wx][wy][lane + 1] = (int16_t)(incl - np);
+      sh.first[wx][wy][lane + 1] = (int32_t)(base + incl - np);
     }
     if (threadIdx.x < 2 * KX * KY) {
       const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
@@ -291,10 +291,8 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
         if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z, g);
       }
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
-      // the first patch of the row's cell Z0 + TZ is the next segment's base; that of
-      // cell Z0 - 1 lies its own patches before this segment's base
       sh.first[wx][wy][end ? TZ + 1 : 0] =
-          (int16_t)(end ? (int32_t)(sh.pb[wx][wy][1] - sh.pb[wx][wy][0]) : -dmc_npatch(sh.cases[rc]));
+          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
     }
   }
   __syncthreads();
@@ -416,7 +414,7 @@ __host__ __device__ constexpr size_t fused_smem() {
 }
 
 template <class S, int METHOD>
-__global__ void __launch_bounds__(NTHREADS, sizeof(S) == 4 ? 4 : 3)
+__global__ void __launch_bounds__(NTHREADS, 3)
     fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
                           S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats) {
