@@ -46,12 +46,13 @@ class Counts(ctypes.Structure):
 
 
 class SphereFieldDesc(ctypes.Structure):
-    """diso_sphere_field: spheres [count][4] (x, y, z, r) in device memory, grid bounds."""
+    """diso_sphere_field: spheres [count][4] (x, y, z, r) in device memory, grid bounds, deform or NULL."""
     _fields_ = [
         ("spheres", ctypes.c_void_p),
         ("count", ctypes.c_int),
         ("lo", ctypes.c_double * 3),
         ("hi", ctypes.c_double * 3),
+        ("deform", ctypes.c_void_p),
     ]
 
 
@@ -94,6 +95,10 @@ EXPORTS = {
                                           ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_void_p, ctypes.POINTER(Counts)]),
+    "diso_backward_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SphereFieldDesc), ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_field_materialize": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(SphereFieldDesc), ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_mesh_normals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
@@ -278,6 +283,13 @@ class Extractor:
                                        ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], stream_of(verts.device),
                                        ctypes.byref(c)), "forward of a field")
         return c
+
+    def backward_field(self, desc, shape, iso, pad, seg, normalize, grad_verts, grad_spheres, grad_deform,
+                       exact=False):
+        """Sphere-parameter (and deform) gradients of a forward_field (see diso_backward_field)."""
+        check(lib().diso_backward_field(self._h, ctypes.byref(desc), *shape, iso, pad, ptr(seg), int(bool(normalize)),
+                                        GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_spheres),
+                                        ptr(grad_deform), stream_of(grad_verts.device)), "backward of a field")
 
     # mesh consumers (diso_mesh_*): the extractor supplies the dtype and the scratch
     def mesh_normals(self, verts, faces, out):

@@ -102,6 +102,8 @@ struct diso_extractor {
   unsigned* plist_n = nullptr;
   double* isog = nullptr;        // per-CTA partial sums of the isovalue gradient
   int64_t isog_cap = 0;
+  double* fpart = nullptr;       // per-CTA sums of a field backward's sphere gradients
+  int64_t fpart_cap = 0;
 
   // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
   void* bdesc = nullptr;         // device BatchGrid<S>[MAX_BATCH]
@@ -167,6 +169,9 @@ struct diso_extractor {
     cudaFree(isog);
     isog = nullptr;
     isog_cap = 0;
+    cudaFree(fpart);
+    fpart = nullptr;
+    fpart_cap = 0;
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -1083,6 +1088,7 @@ template <class S>
 SphereField<S> make_sphere_field(const diso_sphere_field* d, int nx, int ny, int nz, double iso, double padval) {
   SphereField<S> f;
   f.sph = (const S*)d->spheres;
+  f.def = (const S*)d->deform;
   f.K = d->count;
   const int n[3] = {nx, ny, nz};
   for (int a = 0; a < 3; ++a) {
@@ -1146,6 +1152,37 @@ int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint6
   CUDA_TRY(cudaGetLastError());
   if ((rc = count_read<S>(ex, f.n0, f.n1, f.n2, iso, seg, s, out)) != DISO_OK) return rc;
   out->emitted = (out->n_verts <= vcap && out->n_faces <= fcap) ? 1 : 0;
+  return DISO_OK;
+}
+
+// the backward of an evaluated union of spheres (field_backward_kernel)
+template <class S>
+int backward_field(diso_extractor* ex, const SphereField<S>& f, const uint64_t* seg, int normalize, int flags,
+                   const void* gv, double* grad_spheres, void* gdef, cudaStream_t s) {
+  Geom g;
+  g.init(f.n0, f.n1, f.n2);
+  const size_t smem = ex->method == DISO_MC ? field_bwd_smem<S, MC>(f.K) : field_bwd_smem<S, DMC>(f.K);
+  const void* k = ex->method == DISO_MC ? (const void*)field_backward_kernel<S, MC>
+                                        : (const void*)field_backward_kernel<S, DMC>;
+  CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NTHREADS, smem));
+  const unsigned grid = (unsigned)(ex->sms * std::max(per, 1));
+  int rc;
+  if ((rc = grow(ex->fpart, ex->fpart_cap, (int64_t)grid * f.K * 4)) != DISO_OK) return rc;
+  const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  {
+    KernelTimer kt(ex, K_FUSED_BWD, s);
+    if (ex->method == DISO_MC)
+      field_backward_kernel<S, MC><<<grid, NTHREADS, smem, s>>>(f, g, seg, (const S*)gv, normalize, 0, (S*)gdef,
+                                                                ex->fpart, ex->stats);
+    else
+      field_backward_kernel<S, DMC><<<grid, NTHREADS, smem, s>>>(f, g, seg, (const S*)gv, normalize, exact, (S*)gdef,
+                                                                 ex->fpart, ex->stats);
+  }
+  CUDA_TRY(cudaGetLastError());
+  field_grad_final_kernel<<<1, 256, 0, s>>>(ex->fpart, (int)grid, f.K * 4, grad_spheres);
+  CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
 
@@ -1599,6 +1636,7 @@ int diso_scan_wait_probe(diso_extractor* ex, unsigned spin_limit, void* stream) 
 int64_t diso_scratch_bytes(const diso_extractor* ex) {
   if (!ex) return 0;
   int64_t b = ex->active_cap * (int64_t)sizeof(int) + ex->codes_cap * (int64_t)sizeof(CellRec) +
+              ex->fpart_cap * (int64_t)sizeof(double) +
               ex->plist_cap * (int64_t)sizeof(int) + ex->split_cap * (int64_t)sizeof(uint64_t) + ex->mesh_cap +
               ex->isog_cap * (int64_t)sizeof(double) +
               ex->scan_cap * (int64_t)(sizeof(uint32_t) + 2 * sizeof(uint64_t));
@@ -1690,6 +1728,27 @@ int diso_forward_field(diso_extractor* ex, const diso_sphere_field* field, int n
                                 normalize, verts, vcap, faces, fcap, s, out);
   return forward_field<double>(ex, make_sphere_field<double>(field, nx, ny, nz, isovalue, padval), isovalue, seg,
                                normalize, verts, vcap, faces, fcap, s, out);
+}
+
+int diso_backward_field(diso_extractor* ex, const diso_sphere_field* field, int nx, int ny, int nz, double isovalue,
+                        double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
+                        double* grad_spheres, void* grad_deform, void* stream) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  int rc = check_field(field, nx, ny, nz);
+  if (rc != DISO_OK) return rc;
+  if (field->count > FIELD_BWD_MAX_SPHERES)
+    return fail(DISO_ERR_ARG, "the field backward takes at most %d spheres (got %d)", FIELD_BWD_MAX_SPHERES,
+                field->count);
+  if (!seg || !grad_verts || !grad_spheres) return fail(DISO_ERR_ARG, "null seg, grad_verts or grad_spheres");
+  if (field->deform && !grad_deform) return fail(DISO_ERR_ARG, "a field with a deform needs grad_deform");
+  if ((rc = check_common(ex, field->spheres, nx, ny, nz)) != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  void* gd = field->deform ? grad_deform : nullptr;
+  return ex->dtype == DISO_F32
+             ? backward_field<float>(ex, make_sphere_field<float>(field, nx, ny, nz, isovalue, padval), seg, normalize,
+                                     flags, grad_verts, grad_spheres, gd, s)
+             : backward_field<double>(ex, make_sphere_field<double>(field, nx, ny, nz, isovalue, padval), seg,
+                                      normalize, flags, grad_verts, grad_spheres, gd, s);
 }
 
 int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, int ny, int nz, void* sdf,

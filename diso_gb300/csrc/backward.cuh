@@ -27,6 +27,7 @@
 // Tiles whose window holds more crossing edges than the shared-memory cache compute
 // each edge's adjoint at both of its end points instead.
 #pragma once
+#include "fields.cuh"
 #include "kernels.cuh"
 
 namespace diso {
@@ -125,14 +126,23 @@ __device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh
 }
 
 // adjoints (c0 at the edge's first point, c1 at its second) of window edge (x, y, j, a)
-template <class S, int METHOD>
-__device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
-                                                   int Y0, int Z0, int x, int y, int j, int a,
-                                                   const S* __restrict__ gv, int64_t V, const S scale[3], int exact,
-                                                   S c0[4], S c1[4], bool& bad) {
+template <class S, int METHOD, class F>
+__device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>& sh, const F& f, int X0, int Y0,
+                                                   int Z0, int x, int y, int j, int a, const S* __restrict__ gv,
+                                                   int64_t V, const S scale[3], int exact, S c0[4], S c1[4],
+                                                   bool& bad) {
   S gvec[3];
   fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
-  edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
+  if constexpr (F::kDense) {
+    edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
+  } else {
+    // an evaluated field: its values where the edge's ends lie, the same arithmetic
+    const int X = X0 + x, Y = Y0 + y, Z = Z0 + j, ex = a == 0, ey = a == 1, ez = a == 2;
+    S q0[3], q1[3];
+    f.deform(X, Y, Z, q0);
+    f.deform(X + ex, Y + ey, Z + ez, q1);
+    edge_adjoint_math<S>(f.iso, X, Y, Z, a, f.at(X, Y, Z), f.at(X + ex, Y + ey, Z + ez), q0, q1, gvec, c0, c1);
+  }
 }
 
 template <class S>
@@ -144,8 +154,8 @@ struct Adj4 {
 // the uncached path's per-point call, kept out of line (it runs only for tiles with
 // more window edges than the cache holds): the adjoint at end k of window edge
 // (x, y, j, a)
-template <class S, int METHOD>
-__device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const Field<S>& f, int X0,
+template <class S, int METHOD, class F>
+__device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const F& f, int X0,
                                                        int Y0, int Z0, int x, int y, int j, int a,
                                                        const S* __restrict__ gv, int64_t V, S sx, S sy, S sz,
                                                        int exact, int k) {
@@ -153,7 +163,7 @@ __device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METH
   const S scale[3] = {sx, sy, sz};
   Adj4<S> r;
   r.bad = false;
-  fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, r.bad);
+  fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, r.bad);
 #pragma unroll
   for (int i = 0; i < 4; ++i) r.v[i] = k ? c1[i] : c0[i];
   return r;
@@ -161,8 +171,11 @@ __device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METH
 
 // Morton code of cell (X, Y, Z) from global memory, out of line: the DMC ambiguity
 // test needs it only for an ambiguous cell whose neighbour lies outside the masks
-template <class S>
-__device__ __noinline__ int fused_code_far(const Field<S>& f, int X, int Y, int Z) {
+template <class S, class F>
+__device__ __noinline__ int fused_code_far(const F& f, int X, int Y, int Z) {
+  if constexpr (!F::kDense) {
+    return cell_code_far<S, F>(f, X, Y, Z);
+  } else {
   // the eight corners' loads issued together: clamped addresses, the pad value
   // selected afterwards for corners outside the grid
   S v[8];
@@ -178,12 +191,13 @@ __device__ __noinline__ int fused_code_far(const Field<S>& f, int X, int Y, int 
 #pragma unroll
   for (int i = 0; i < 8; ++i) c |= ((in[i] ? v[i] : f.pad) >= f.iso) << i;
   return c;
+  }
 }
 
 // dmc_resolve_m (kernels.cuh) with the neighbour's code from the masks when its
 // corners lie in them, otherwise from fused_code_far
-template <class S, int WX, int WY>
-__device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const uint64_t* cases, const Field<S>& f,
+template <class S, class F, int WX, int WY>
+__device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const uint64_t* cases, const F& f,
                                              int WX0, int WY0, int Z0, int code, int X, int Y, int Z,
                                              const Geom& g) {
   const int dir = dmc_dir(cases[code]);
@@ -198,16 +212,63 @@ __device__ __forceinline__ int fused_resolve(const uint64_t (&m)[WX][WY], const 
   if (x < (unsigned)(WX - 1) && y < (unsigned)(WY - 1) && sft >= 0 && sft + 1 <= MASK_TOP)
     ncode = code8(m[x][y], m[x + 1][y], m[x][y + 1], m[x + 1][y + 1], sft);
   else
-    ncode = fused_code_far<S>(f, NX, NY, NZ);
+    ncode = fused_code_far<S, F>(f, NX, NY, NZ);
   return dmc_dir(cases[ncode]) != 7 ? (code ^ 0xff) : code;
 }
 
-// one active point tile (see the top of this file)
-template <class S, int METHOD>
-__device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Field<S>& f, const Geom& g,
+// The gradient at unpadded point (x, y, z) of an evaluated union of spheres (the
+// first `has` lanes' points) goes to the parameters of the sphere that attains the
+// field's value there: d(|p - c| - r)/dc = -(p - c) / |p - c|, d/dr = -1.  Per warp and
+// sphere in a fixed order (a shuffle tree over the lanes, then part[warp][k][.] in
+// the warp's tile order), so the sums repeat bit for bit.  part: [NTHREADS / 32][K][4].
+template <class S>
+__device__ __forceinline__ void field_param_add(const SphereField<S>& f, double* __restrict__ part, bool has, int x,
+                                                int y, int z, S grad) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int k = -1;
+  double c[4] = {0.0, 0.0, 0.0, 0.0};
+  if (has) {
+    S off[3];
+    k = f.argmin(x, y, z, off);
+    const double dist = sqrt((double)off[0] * off[0] + (double)off[1] * off[1] + (double)off[2] * off[2]);
+    const double gg = (double)grad;
+    if (dist > 0.0) {
+      c[0] = -gg * (double)off[0] / dist;
+      c[1] = -gg * (double)off[1] / dist;
+      c[2] = -gg * (double)off[2] / dist;
+    }
+    c[3] = -gg;
+  }
+  unsigned pending = __ballot_sync(0xffffffffu, has);
+  while (pending) {
+    const int kk = __shfl_sync(0xffffffffu, k, __ffs(pending) - 1);
+    const bool mine = has && k == kk;
+    double v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      v[i] = mine ? c[i] : 0.0;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    }
+    if (lane == 0) {
+      double* p = part + ((int64_t)warp * f.K + kk) * 4;
+      p[0] += v[0];
+      p[1] += v[1];
+      p[2] += v[2];
+      p[3] += v[3];
+    }
+    pending &= ~__ballot_sync(0xffffffffu, mine);
+  }
+}
+
+// one active point tile (see the top of this file); for an evaluated field the
+// point gradients go to the spheres' parameters (field_param_add into `part`) and
+// only the deform's gradient is written
+template <class S, int METHOD, class F = Field<S>>
+__device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& f, const Geom& g,
                                            const uint64_t* __restrict__ seg, int64_t ptile, const S* __restrict__ gv,
                                            int64_t V, const S scale[3], int exact, S* __restrict__ gsdf,
-                                           S* __restrict__ gdef, bool& bad) {
+                                           S* __restrict__ gdef, bool& bad, double* __restrict__ part = nullptr) {
   using SH = FusedShared<S, METHOD>;
   constexpr int LO = SH::LO, CX = SH::CX, CY = SH::CY, KX = SH::KX, KY = SH::KY;
   constexpr int CAP = fb_cap<S>();
@@ -231,7 +292,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
   // a warp's mask rows in batches of at most eight loads (more spill registers)
   constexpr int ROWS_PW = (SH::WX * SH::WY + NTHREADS / 32 - 1) / (NTHREADS / 32);
   constexpr int MBATCH = ROWS_PW <= 10 ? ROWS_PW : (ROWS_PW + 1) / 2;
-  load_masks<S, SH::WX, SH::WY, false, Field<S>, MBATCH>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
+  load_masks<S, SH::WX, SH::WY, false, F, MBATCH>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
   if (si < NSV) {
     if constexpr (METHOD == MC)
       sh.eb[sx][sy][sk] = Counts::lo(sv);
@@ -274,7 +335,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
         sh.first[wx][wy][lane + 1] = (int32_t)base;
         continue;
       }
-      const int rc = nt ? fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z0 + lane, g) : 0;
+      const int rc = nt ? fused_resolve<S, F>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z0 + lane, g) : 0;
       const uint32_t np = (uint32_t)dmc_npatch(sh.cases[rc]);
       const uint32_t incl = warp_incl(np);
       sh.rc[wx][wy][lane + 1] = (uint8_t)rc;
@@ -288,7 +349,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && Z >= 0 && Z < g.c[2]) {
         const int code = code8(sh.m[wx + 1][wy + 1], sh.m[wx + 2][wy + 1], sh.m[wx + 1][wy + 2],
                                sh.m[wx + 2][wy + 2], end ? TZ + 1 : 0);
-        if (code != 0 && code != 255) rc = fused_resolve<S>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z, g);
+        if (code != 0 && code != 255) rc = fused_resolve<S, F>(sh.m, sh.cases, f, X0 - LO, Y0 - LO, Z0, code, X, Y, Z, g);
       }
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
       sh.first[wx][wy][end ? TZ + 1 : 0] =
@@ -345,7 +406,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       int x, y, j, a;
       item_decode(sh.witems[i], x, y, j, a);
       S c0[4], c1[4];
-      fused_edge_adjoint<S, METHOD>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
+      fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
       store_adj<S>(&sh.adj[0][0], i, c0, c1);
     }
     __syncthreads();
@@ -380,7 +441,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
       for (int e = 0; e < 6; ++e)
         if ((on >> e) & 1) {
           const Adj4<S> o =
-              fused_edge_adjoint_far<S, METHOD>(sh, f, X0, Y0, Z0, x - (e == 1), y - (e == 3), j - (e == 5), e >> 1,
+              fused_edge_adjoint_far<S, METHOD, F>(sh, f, X0, Y0, Z0, x - (e == 1), y - (e == 3), j - (e == 5), e >> 1,
                                                 gv, V, scale[0], scale[1], scale[2], exact, e & 1);
           acc[0] += o.v[0];
           acc[1] += o.v[1];
@@ -390,15 +451,17 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const Fie
         }
     }
     const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
-    if (f.inside(X, Y, Z)) {
-      const int64_t i = f.lin(X, Y, Z);
-      gsdf[i] = acc[0];
+    const bool in = f.inside(X, Y, Z);
+    const int64_t i = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 + (Z - 1);
+    if (in) {
+      if constexpr (F::kDense) gsdf[i] = acc[0];
       if (gdef) {
         gdef[3 * i + 0] = acc[1];
         gdef[3 * i + 1] = acc[2];
         gdef[3 * i + 2] = acc[3];
       }
     }
+    if constexpr (!F::kDense) field_param_add<S>(f, part, in && acc[0] != S(0), X - 1, Y - 1, Z - 1, acc[0]);
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
@@ -433,6 +496,77 @@ __global__ void __launch_bounds__(NTHREADS, 3)
   for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
     fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad);
   if (bad) atomicOr(&stats->error, 8ull);
+}
+
+// ------------------------------------------------------------------ evaluated fields
+
+// sphere parameters whose gradients one field backward accumulates (per-warp
+// partials in shared memory)
+constexpr int FIELD_BWD_MAX_SPHERES = 64;
+
+template <class S, int METHOD>
+__host__ __device__ constexpr size_t field_bwd_smem(int K) {
+  return (sizeof(FusedShared<S, METHOD>) + 15) / 16 * 16 + (size_t)(NTHREADS / 32) * K * 4 * sizeof(double);
+}
+
+// The backward of an evaluated union of spheres (diso_backward_field): CTA b takes
+// point tiles b, b + gridDim.x, ... (a fixed assignment, so that the sums repeat);
+// active tiles as fused_tile, with the point gradients going to the spheres'
+// parameters; the deform's gradient written, zeros in the inactive tiles.  Each
+// CTA's sums (per sphere: dL/dc, dL/dr) go to cta_part[b][K][4] in a fixed order.
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS, 2)
+    field_backward_kernel(SphereField<S> f, Geom g, const uint64_t* __restrict__ seg, const S* __restrict__ gv,
+                          int normalize, int exact, S* __restrict__ gdef, double* __restrict__ cta_part,
+                          Stats* stats) {
+  extern __shared__ __align__(16) unsigned char fb_smem[];
+  FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
+  double* part = reinterpret_cast<double*>(fb_smem + (sizeof(FusedShared<S, METHOD>) + 15) / 16 * 16);
+  const int K = f.K, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < (NTHREADS / 32) * K * 4; i += blockDim.x) part[i] = 0.0;
+  if constexpr (METHOD == DMC) sh.cases[threadIdx.x & 255] = dmc_case(threadIdx.x & 255);
+  if (threadIdx.x < 24) sh.edge_of[threadIdx.x] = __ldg(g_edge_of + threadIdx.x);
+  __syncthreads();
+  const uint8_t* tile_flag = reinterpret_cast<const uint8_t*>(seg + g.nseg + 1);
+  const uint64_t tot = seg[g.nseg];
+  const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
+  S scale[3];
+  grad_scale<S>(g, normalize, scale);
+  bool bad = false;
+#pragma unroll 1
+  for (int64_t t = blockIdx.x; t < g.nptiles(); t += gridDim.x) {
+    int x0, y0, z0;
+    ptile_coords(t, g, x0, y0, z0);
+    const int a = lane < 8 ? ptile_flag(g, tile_flag, x0, y0, z0, lane) : 0;
+    if (__any_sync(0xffffffffu, a)) {  // the same in every warp
+      fused_tile<S, METHOD, SphereField<S>>(sh, f, g, seg, t, gv, V, scale, exact, nullptr, gdef, bad, part);
+    } else if (gdef) {
+      const int nz = min(TZ, f.n2 - z0);
+      for (int q = warp; q < TX * TY; q += NTHREADS / 32) {
+        const int x = x0 + q / TY, y = y0 + q % TY;
+        if (x >= f.n0 || y >= f.n1) continue;
+        S* row = gdef + 3 * (((int64_t)x * f.n1 + y) * f.n2 + z0);
+        for (int k = lane; k < 3 * nz; k += 32) row[k] = S(0);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < K * 4; i += blockDim.x) {
+    double acc = 0.0;
+    for (int w = 0; w < NTHREADS / 32; ++w) acc += part[w * K * 4 + i];
+    cta_part[(int64_t)blockIdx.x * K * 4 + i] = acc;
+  }
+  if (bad) atomicOr(&stats->error, 8ull);
+}
+
+// out[i] = the sum of cta_part[b][i] over the n CTAs in order (i < k4)
+__global__ void __launch_bounds__(256) field_grad_final_kernel(const double* __restrict__ cta_part, int n, int k4,
+                                                               double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k4; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int b = 0; b < n; ++b) acc += cta_part[(int64_t)b * k4 + i];
+    out[i] = acc;
+  }
 }
 
 }  // namespace diso

@@ -18,6 +18,7 @@ template <class S>
 struct SphereField {
   static constexpr bool kDense = false;
   const S* __restrict__ sph;  // [K][4]: centre x, y, z, radius
+  const S* __restrict__ def;  // [N0][N1][N2][3] or null: the deform, a dense input as for Field
   int K;
   S lo[3], step[3];
   int n0, n1, n2;
@@ -40,7 +41,34 @@ struct SphereField {
   __device__ __forceinline__ S at(int X, int Y, int Z) const { return inside(X, Y, Z) ? value(X - 1, Y - 1, Z - 1) : pad; }
   // unpadded point (x, y, z) of a row in the grid (the row offset is not used)
   __device__ __forceinline__ S point(int64_t, int x, int y, int z) const { return value(x, y, z); }
-  __device__ __forceinline__ void deform(int, int, int, S d[3]) const { d[0] = d[1] = d[2] = S(0); }
+  // deform at padded point (zero in the pad)
+  __device__ __forceinline__ void deform(int X, int Y, int Z, S d[3]) const {
+    if (def && inside(X, Y, Z)) {
+      const S* p = def + 3 * (((int64_t)(X - 1) * n1 + (Y - 1)) * n2 + (Z - 1));
+      d[0] = __ldg(p); d[1] = __ldg(p + 1); d[2] = __ldg(p + 2);
+    } else {
+      d[0] = d[1] = d[2] = S(0);
+    }
+  }
+  // the sphere attaining value() at unpadded point (x, y, z) (the first of equal
+  // minima, as value() keeps it) and the point's offset from its centre
+  __device__ __forceinline__ int argmin(int x, int y, int z, S off[3]) const {
+    const S px = lo[0] + step[0] * (S)x, py = lo[1] + step[1] * (S)y, pz = lo[2] + step[2] * (S)z;
+    S m = S(INFINITY);
+    int best = 0;
+    for (int k = 0; k < K; ++k) {
+      const S dx = px - __ldg(sph + 4 * k), dy = py - __ldg(sph + 4 * k + 1), dz = pz - __ldg(sph + 4 * k + 2);
+      const S d = sqrt(dx * dx + dy * dy + dz * dz) - __ldg(sph + 4 * k + 3);
+      if (d < m) {
+        m = d;
+        best = k;
+        off[0] = dx;
+        off[1] = dy;
+        off[2] = dz;
+      }
+    }
+    return best;
+  }
 
   // value() over the spheres in `cand` only (bit k: sphere k; all of them when
   // `all`): the same value when the others cannot be the minimum (classify_warp)

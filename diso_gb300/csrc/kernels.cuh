@@ -1635,6 +1635,34 @@ __device__ __forceinline__ void load_grad(const S* __restrict__ gv, int64_t i, c
   for (int k = 0; k < 3; ++k) out[k] = mul_rn(__ldg(gv + 3 * i + k), scale[k]);
 }
 
+// the adjoint arithmetic of edge_adjoint2 from the end points' values d0, d1 and
+// deforms q0, q1
+template <class S>
+__device__ __forceinline__ void edge_adjoint_math(S iso, int X, int Y, int Z, int a, S d0, S d1, const S q0[3],
+                                                  const S q1[3], const S gvec[3], S c0[4], S c1[4]) {
+  const int ex = a == 0, ey = a == 1, ez = a == 2;
+  S t = S(0.5);
+  if (d1 != d0) {
+    S r = (iso - d0) / (d1 - d0);
+    r = S(0) > r ? S(0) : r;
+    t = r < S(1) ? r : S(1);
+  }
+  const S dp[3] = {(S(X + ex) + q1[0]) - (S(X) + q0[0]), (S(Y + ey) + q1[1]) - (S(Y) + q0[1]),
+                   (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
+  const S adj_t = fma_rn(dp[2], gvec[2], fma_rn(dp[1], gvec[1], mul_rn(dp[0], gvec[0])));
+  const S den = (d1 - d0) * (d1 - d0);
+  const S w0 = S(1) - t;
+  // rounded products: the backward's two forms (the adjoints stored, then added
+  // per point; or added where they are computed) must not fuse them into the sums
+  c0[0] = mul_rn((iso - d1) / den, adj_t);
+  c1[0] = mul_rn((d0 - iso) / den, adj_t);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    c0[k + 1] = mul_rn(w0, gvec[k]);
+    c1[k + 1] = mul_rn(t, gvec[k]);
+  }
+}
+
 // adjoint of edge_vertex (adjComputeMcVert, src/cumc.cu:412-453) for the edge from
 // padded point A along axis a: c0 = (dL/dsdf, dL/ddeform) at A, c1 at A + e_a
 template <class S>
@@ -1659,26 +1687,7 @@ __device__ __forceinline__ void edge_adjoint2(const Field<S>& f, int X, int Y, i
     }
   }
   const S d0 = in0 ? v0 : f.pad, d1 = in1 ? v1 : f.pad;
-  S t = S(0.5);
-  if (d1 != d0) {
-    S r = (f.iso - d0) / (d1 - d0);
-    r = S(0) > r ? S(0) : r;
-    t = r < S(1) ? r : S(1);
-  }
-  const S dp[3] = {(S(X + ex) + q1[0]) - (S(X) + q0[0]), (S(Y + ey) + q1[1]) - (S(Y) + q0[1]),
-                   (S(Z + ez) + q1[2]) - (S(Z) + q0[2])};
-  const S adj_t = fma_rn(dp[2], gvec[2], fma_rn(dp[1], gvec[1], mul_rn(dp[0], gvec[0])));
-  const S den = (d1 - d0) * (d1 - d0);
-  const S w0 = S(1) - t;
-  // rounded products: the backward's two forms (the adjoints stored, then added
-  // per point; or added where they are computed) must not fuse them into the sums
-  c0[0] = mul_rn((f.iso - d1) / den, adj_t);
-  c1[0] = mul_rn((d0 - f.iso) / den, adj_t);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    c0[k + 1] = mul_rn(w0, gvec[k]);
-    c1[k + 1] = mul_rn(t, gvec[k]);
-  }
+  edge_adjoint_math<S>(f.iso, X, Y, Z, a, d0, d1, q0, q1, gvec, c0, c1);
 }
 
 // whether forward tile k = (dx, dy, dz) of point tile (x0, y0, z0) (the tile one step

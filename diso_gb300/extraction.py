@@ -221,12 +221,13 @@ class DiffMC(nn.Module):
     def forward(self, grid, deform=None, isovalue=0.0, normalize=True):
         return extract(self._ex, grid, deform, isovalue, normalize, recompute=self.recompute)
 
-    def forward_field(self, field, shape, isovalue=0.0, normalize=True):
+    def forward_field(self, field, shape, isovalue=0.0, normalize=True, deform=None):
         """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,
-        without a dense grid in memory; forward only."""
+        without a dense grid in memory; differentiable with respect to the field's
+        parameters and the deform."""
         from .fields import extract_field
 
-        return extract_field(self._ex, field, shape, isovalue, normalize)
+        return extract_field(self._ex, field, shape, isovalue, normalize, deform=deform)
 
 
 class DiffDMC(nn.Module):
@@ -247,9 +248,10 @@ class DiffDMC(nn.Module):
     def forward(self, grid, deform=None, isovalue=0.0, return_quads=False, normalize=True):
         return extract(self._ex, grid, deform, isovalue, normalize, return_quads, self.exact_grad, self.recompute)
 
-    def forward_field(self, field, shape, isovalue=0.0, return_quads=False, normalize=True):
+    def forward_field(self, field, shape, isovalue=0.0, return_quads=False, normalize=True, deform=None):
         """The mesh of an evaluated field (diso_gb300.fields) on a grid of `shape`,
-        without a dense grid in memory; forward only."""
+        without a dense grid in memory; differentiable with respect to the field's
+        parameters and the deform."""
         from .fields import extract_field
 
-        return extract_field(self._ex, field, shape, isovalue, normalize, return_quads)
+        return extract_field(self._ex, field, shape, isovalue, normalize, return_quads, deform, self.exact_grad)

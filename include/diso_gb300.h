@@ -293,13 +293,15 @@ int diso_timing_read(diso_extractor* ex, diso_kernel_time* out, int max, int* n)
  * emit evaluates the end points of the crossing edges.  The field: a union of spheres,
  * value(p) = min_k (|p - c_k| - r_k) at grid point p = lo + (hi - lo) * i / (n - 1)
  * (per axis; step computed in double, then in the dtype), spheres [count][4] (x, y,
- * z, r) in device memory in the extractor's dtype.  Forward only (no deform, no
- * gradients). */
+ * z, r) in device memory in the extractor's dtype, and optionally a dense deform of
+ * the grid's points.  diso_backward_field gives the gradients with respect to the
+ * spheres (and the deform). */
 typedef struct diso_sphere_field {
   const void* spheres;
   int count;
   double lo[3];
   double hi[3];
+  const void* deform; /* [nx][ny][nz][3] in the dtype, or NULL: the vertices' deform, as for a dense grid */
 } diso_sphere_field;
 
 /* As diso_forward for an evaluated field: count, scan and emit in one call into
@@ -309,6 +311,20 @@ typedef struct diso_sphere_field {
 int diso_forward_field(diso_extractor* ex, const diso_sphere_field* field, int nx, int ny, int nz, double isovalue,
                        double padval, uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces,
                        int64_t fcap, void* stream, diso_counts* counts);
+
+/* Backward of diso_forward_field (its `seg` record; the field unchanged since), without
+ * a dense grid of the field's values: from dL/dverts [n_verts][3], the gradients of
+ * the spheres' parameters as doubles grad_spheres [count][4] (dL/dx, dL/dy, dL/dz of
+ * the centre, dL/dr), and, when the field has a deform, dL/ddeform [nx][ny][nz][3].
+ * A point's dL/d(value) (the crossing edges' lerp adjoints, as diso_backward forms
+ * them, flags as there) goes to the sphere attaining the minimum there: d(|p - c| -
+ * r)/dc = -(p - c) / |p - c|, d/dr = -1.  Deterministic (fixed reduction orders); at
+ * most 64 spheres.  The reference's example differentiates its analytic sphere
+ * through PyTorch on a dense grid (test/example.py:8-16, 33-54, 75-81); no
+ * counterpart in its library. */
+int diso_backward_field(diso_extractor* ex, const diso_sphere_field* field, int nx, int ny, int nz, double isovalue,
+                        double padval, const uint64_t* seg, int normalize, int flags, const void* grad_verts,
+                        double* grad_spheres, void* grad_deform, void* stream);
 
 /* The field's dense grid [nx][ny][nz] (the same values the fused forward evaluates). */
 int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, int ny, int nz, void* sdf,
