@@ -154,7 +154,7 @@ def test_field_gradients_match_the_dense_path(cuda_device, method, rq, dtype, wi
     """The fused field backward against the dense path on the field's grid
     (field.materialize, the same values bit for bit): dL/ddeform equal bit for bit,
     dL/d(centres, radii) equal to the dense dL/dsdf carried to the spheres by the
-    chain rule (double sums in another order: within 1e-10 relative)."""
+    chain rule in float64 (within 1e-10 relative in float64, 1e-6 in float32)."""
     from diso_gb300 import DiffDMC, DiffMC
 
     dt = DT[dtype]
@@ -178,8 +178,11 @@ def test_field_gradients_match_the_dense_path(cuda_device, method, rq, dtype, wi
         assert torch.equal(dfm.grad, d2.grad)
     gc, gr = _chain_rule(field, shape, s.grad)
     scale = max(float(gc.abs().max()), float(gr.abs().max()))
-    assert float((c.grad.double() - gc).abs().max()) <= 1e-10 * scale
-    assert float((r.grad.double() - gr).abs().max()) <= 1e-10 * scale
+    # float32: the offsets from the centres are taken in float32, as the field's values
+    # are, and the gradients are returned in float32
+    rtol = 1e-10 if dtype == "float64" else 1e-6
+    assert float((c.grad.double() - gc).abs().max()) <= rtol * scale
+    assert float((r.grad.double() - gr).abs().max()) <= rtol * scale
 
 
 @pytest.mark.parametrize("method", ["mc", "dmc"])
