@@ -639,7 +639,8 @@ def run_ours(args, rank, world, device):
     ext = DiffDMC(torch.float32, recompute=True)
     # launch widths from the package's autotuner (timed on a synthetic field of this
     # size, outside the timed region; cached per GPU, method, dtype, size and mode)
-    tuned = tune.tune_module(ext, (n, n, n), retune=args.retune)
+    tuned = (tune.tune_module(ext, (n, n, n), retune=args.retune) if not args.no_tune else
+             {"params": {}, "ms": 0.0, "default_ms": 0.0, "trials": 0})
     s = sdf.clone().requires_grad_(True)
     d = deform.clone().requires_grad_(True)
     v, f = ext(s, d, return_quads=True)
@@ -653,7 +654,7 @@ def run_ours(args, rank, world, device):
     # the same workload with the forward's edge record and gradient buffers kept for
     # the backward (stored mode), for comparison
     stored = DiffDMC(torch.float32)
-    tuned_st = tune.tune_module(stored, (n, n, n), retune=args.retune)
+    tuned_st = tune.tune_module(stored, (n, n, n), retune=args.retune) if not args.no_tune else {"params": {}}
     ms_st, k_st, ph_st, _ = time_steps(stored, s, d, w, args.steps, args.warmup, world)
     mem_st = peak_memory(stored, s, d, w)
     del stored
@@ -889,6 +890,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--retune", action="store_true", help="time the launch widths again instead of the cached ones")
+    ap.add_argument("--no-tune", action="store_true", help="the library's default launch widths (for profiling)")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     args = ap.parse_args()
