@@ -682,10 +682,15 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
   int rc;
   if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
-  // two zero CTAs per SM, launched first: fewer warps make the zeros (and the fused
-  // pass beside them, measured) slower
-  if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
-  {
+  // The zeros of the point tiles with no crossing nearby: bulk copies issued from
+  // inside the fused pass when the gradients' rows are whole 16-byte units at
+  // 16-byte aligned addresses (they then take no warps from it); otherwise a zero
+  // kernel on the second stream, two CTAs per SM launched first (fewer warps make
+  // the zeros, and the fused pass beside them, slower: measured).
+  const bool zbulk = ((int64_t)nz * (int64_t)sizeof(S)) % 16 == 0 && ((uintptr_t)gsdf & 15u) == 0 &&
+                     ((uintptr_t)gdef & 15u) == 0;
+  if (!zbulk) {
+    if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
     zero_tiles_kernel<S><<<per_sm_ctas(ex, DISO_TUNE_ZERO_CTAS, 2), 256, 0, ex->side>>>(f, g, tile_flags(seg, g),
                                                                                         (S*)gsdf, (S*)gdef);
@@ -702,14 +707,17 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
     KernelTimer kt(ex, K_FUSED_BWD, s);
     if (ex->method == DISO_MC)
       fused_backward_kernel<S, MC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
-                                     (size_t)ex->fused_smem, s>>>(
-          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gsdf, (S*)gdef, ex->stats);
+                                     (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
+                                                                  normalize, 0, (S*)gsdf, (S*)gdef, ex->stats,
+                                                                  zbulk ? 1 : 0);
     else
       fused_backward_kernel<S, DMC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
-                                      (size_t)ex->fused_smem, s>>>(
-          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats);
+                                      (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
+                                                                   normalize, exact, (S*)gsdf, (S*)gdef, ex->stats,
+                                                                   zbulk ? 1 : 0);
   }
   CUDA_TRY(cudaGetLastError());
+  if (zbulk) return DISO_OK;
   return side_join(ex, s);
 }
 

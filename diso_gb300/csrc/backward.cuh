@@ -41,6 +41,8 @@ __host__ __device__ constexpr int fb_cap() {
   return sizeof(S) == 4 ? 1664 : 832;
 }
 
+constexpr int FB_ZBLOCK = 2048;  // bytes of the zeroed block the bulk zero copies read
+
 template <class S, int METHOD>
 struct FusedShared {
   // mask rows start at (X0 - LO, Y0 - LO): MC, the edge rows' points; DMC, two rows
@@ -67,6 +69,7 @@ struct FusedShared {
   // dependent chains of the code and adjoint phases
   uint64_t cases[METHOD == DMC ? 256 : 1];
   uint8_t edge_of[24];
+  __align__(16) uint4 zblock[FB_ZBLOCK / 16];  // zeros, the source of the bulk zero copies
   __align__(16) S adj[fb_cap<S>()][8];
 };
 
@@ -466,11 +469,60 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
+// Zeros of column `col` of point tiles (the 4 x 8 rows of points (x0.., y0..) along the
+// whole z extent) where its tiles have no crossing nearby, by the calling warp: lane
+// l takes row (x0 + l / 8, y0 + l % 8); each run of such z tiles becomes bulk copies
+// of at most FB_ZBLOCK bytes from the zeroed block to the row's dL/dsdf and dL/ddeform
+// (rows of a multiple of 16 bytes at 16-byte aligned addresses, checked by the host).
+// The copies run on the TMA unit beside the fused pass; the lane commits them.
+template <class S>
+__device__ __forceinline__ void zero_column(const Geom& g, const uint8_t* __restrict__ tile_flag, int64_t col,
+                                            S* __restrict__ gsdf, S* __restrict__ gdef, const void* zblock) {
+  const int lane = threadIdx.x & 31;
+  const int x0 = (int)(col / g.ptiles_y()) * TX, y0 = (int)(col % g.ptiles_y()) * TY;
+  const int x = x0 + lane / TY, y = y0 + lane % TY;
+  const bool row = x < g.n[0] && y < g.n[1];
+  const int pz = g.ptiles_z();
+  char* srow = reinterpret_cast<char*>(gsdf + ((int64_t)x * g.n[1] + y) * g.n[2]);
+  char* drow = gdef ? reinterpret_cast<char*>(gdef + 3 * (((int64_t)x * g.n[1] + y) * g.n[2])) : nullptr;
+  bool any = false;
+  for (int base = 0; base < pz; base += 32) {
+    const int tz = base + lane;
+    bool act = true;
+    if (tz < pz) {
+      act = false;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) act = act || ptile_flag(g, tile_flag, x0, y0, tz * TZ, k) != 0;
+    }
+    uint32_t idle = __ballot_sync(0xffffffffu, !act);
+    while (idle) {
+      const int a = __ffs(idle) - 1;
+      const uint32_t rest = ~(idle >> a);
+      const int len = rest ? __ffs(rest) - 1 : 32 - a;  // idle tiles a .. a + len - 1
+      idle &= len >= 32 ? 0u : ~(((1u << len) - 1u) << a);
+      if (a + len >= 32) idle &= (1u << a) - 1u;
+      const int z0 = (base + a) * TZ, z1 = min((base + a + len) * TZ, g.n[2]);
+      if (!row || z1 <= z0) continue;
+      const int64_t sb = (int64_t)z0 * sizeof(S), se = (int64_t)z1 * sizeof(S);
+      for (int64_t o = sb; o < se; o += FB_ZBLOCK)
+        bulk_store(srow + o, zblock, (uint32_t)(se - o < FB_ZBLOCK ? se - o : FB_ZBLOCK));
+      if (drow)
+        for (int64_t o = 3 * sb; o < 3 * se; o += FB_ZBLOCK)
+          bulk_store(drow + o, zblock, (uint32_t)(3 * se - o < FB_ZBLOCK ? 3 * se - o : FB_ZBLOCK));
+      any = true;
+    }
+  }
+  if (any) bulk_commit();
+}
+
 // Persistent over the active point tiles in list[0 .. *count) (active_ptiles_kernel
-// in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...; the zeros of the
-// other tiles are written beside it (zero_tiles_kernel).  Bit 3 of stats->error is
-// set when an index derived from the grid falls outside the forward's counts (the
-// grid no longer matches the forward's record); no access leaves its buffer.
+// in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...  With zbulk, warp 0
+// also zeroes the point tiles with no crossing nearby, column b, b + gridDim.x, ...
+// of point tiles before each of its active tiles and the rest after the last (bulk
+// copies, zero_column); otherwise zero_tiles_kernel writes them beside it.  Bit 3 of
+// stats->error is set when an index derived from the grid falls outside the
+// forward's counts (the grid no longer matches the forward's record); no access
+// leaves its buffer.
 template <class S, int METHOD>
 __host__ __device__ constexpr size_t fused_smem() {
   return sizeof(FusedShared<S, METHOD>);
@@ -480,9 +532,16 @@ template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3)
     fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
-                          S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats) {
+                          S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats, int zbulk) {
   extern __shared__ __align__(16) unsigned char fb_smem[];
   FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
+  const uint8_t* tile_flag = reinterpret_cast<const uint8_t*>(seg + g.nseg + 1);
+  const int64_t ncol = (int64_t)g.ptiles_x() * g.ptiles_y();
+  int64_t col = blockIdx.x;  // the next column of point tiles this CTA zeroes
+  if (zbulk) {
+    for (int i = threadIdx.x; i < FB_ZBLOCK / 16; i += blockDim.x) sh.zblock[i] = make_uint4(0u, 0u, 0u, 0u);
+    fence_proxy_async();  // the zeros are read by the bulk copies
+  }
   const uint64_t tot = seg[g.nseg];
   const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
   S scale[3];
@@ -492,9 +551,19 @@ __global__ void __launch_bounds__(NTHREADS, 3)
   __syncthreads();
   const unsigned n = *count;
   bool bad = false;
+  const int warp = threadIdx.x >> 5;
 #pragma unroll 1
-  for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+    if (zbulk && warp == 0 && col < ncol) {
+      zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
+      col += gridDim.x;
+    }
     fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad);
+  }
+  if (zbulk && warp == 0) {
+    for (; col < ncol; col += gridDim.x) zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
+    bulk_wait_all();  // the copies read shared memory: the CTA stays until they have
+  }
   if (bad) atomicOr(&stats->error, 8ull);
 }
 

@@ -62,19 +62,23 @@ def _dense(shape, dtype, dev, seed):
                                              ("dmc", {"return_quads": True}, True)])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("shape,field", [((37, 50, 70), "dense"), ((65, 33, 97), "sphere"),
-                                         ((96, 96, 96), "dense")])
+                                         ((96, 96, 96), "dense"), ((72, 40, 200), "sphere")])
 def test_fused_backward_equals_stored(cuda_device, method, kw, exact, dtype, shape, field):
     """Dense U(-1, 1) fields put thousands of crossing edges in a tile's window (the
     uncached path); odd sizes leave partial tiles on every axis and rows that are no
-    multiple of four values (the scalar zero path); exact_grad takes each patch's own
-    gradient."""
+    multiple of 16 bytes (the zeros by a kernel on the second stream); rows of whole
+    16-byte units get their zeros as bulk copies from inside the fused pass, the long
+    z extent of (72, 40, 200) with runs of idle tiles; exact_grad takes each patch's
+    own gradient."""
     from diso_gb300 import DiffDMC, DiffMC
 
     if field == "dense":
         sdf, deform = _dense(shape, dtype, cuda_device, 5)
     else:
-        sdf, deform = _inputs(shape[0], dtype, cuda_device, 6)
-        sdf, deform = sdf[:, :shape[1], :shape[2]].contiguous(), deform[:, :shape[1], :shape[2]].contiguous()
+        big = max(shape)
+        sdf, deform = _inputs(big, dtype, cuda_device, 6)
+        sdf = sdf[:shape[0], :shape[1], :shape[2]].contiguous()
+        deform = deform[:shape[0], :shape[1], :shape[2]].contiguous()
     res = []
     for recompute in (False, True):
         mod = (DiffMC(dtype, recompute=recompute) if method == "mc"
