@@ -75,10 +75,12 @@ def test_fused_backward_equals_stored(cuda_device, method, kw, exact, dtype, sha
     if field == "dense":
         sdf, deform = _dense(shape, dtype, cuda_device, 5)
     else:
-        big = max(shape)
-        sdf, deform = _inputs(big, dtype, cuda_device, 6)
-        sdf = sdf[:shape[0], :shape[1], :shape[2]].contiguous()
-        deform = deform[:shape[0], :shape[1], :shape[2]].contiguous()
+        rng = np.random.default_rng(6)
+        X, Y, Z = np.meshgrid(*[np.linspace(-1, 1, n) for n in shape], indexing="ij")
+        npdt = np.float32 if dtype == torch.float32 else np.float64
+        sdf = torch.tensor((np.sqrt(X * X + Y * Y + Z * Z) - 0.55 + 0.03 * rng.standard_normal(shape)).astype(npdt),
+                           device=cuda_device)
+        deform = torch.tensor(rng.uniform(-0.3, 0.3, shape + (3,)).astype(npdt), device=cuda_device)
     res = []
     for recompute in (False, True):
         mod = (DiffMC(dtype, recompute=recompute) if method == "mc"
