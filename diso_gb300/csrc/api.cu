@@ -72,6 +72,9 @@ struct diso_extractor {
   uint8_t* mesh = nullptr;       // mesh consumers' scratch (normals, weld, OBJ), bytes
   int64_t mesh_cap = 0;
   int64_t last_active = 0;       // from the last forward count
+  // the `seg` and grid of the last dense DMC count, whose cell records `codes` holds
+  const uint64_t* codes_seg = nullptr;
+  int codes_dims[3] = {0, 0, 0};
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
   int tma_ctas = 0;              // the same for the TMA count kernel
   int gather_ctas = 0;           // the same for the point gather
@@ -458,6 +461,10 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   if (scan_tiles == 0) return DISO_ERR_CUDA;
   count_prep_kernel<<<1, 256, 0, s>>>(ex->stats, ex->scan_flag, scan_tiles);
   CUDA_TRY(cudaGetLastError());
+  ex->codes_seg = seg;
+  ex->codes_dims[0] = nx;
+  ex->codes_dims[1] = ny;
+  ex->codes_dims[2] = nz;
   CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
@@ -689,6 +696,12 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   // the zeros, and the fused pass beside them, slower: measured).
   const bool zbulk = ((int64_t)nz * (int64_t)sizeof(S)) % 16 == 0 && ((uintptr_t)gsdf & 15u) == 0 &&
                      ((uintptr_t)gdef & 15u) == 0;
+  // DMC: the cell records of the extractor's last count are this forward's when that
+  // count wrote this `seg` for a grid of these sizes (no other forward ran since);
+  // then the fused pass reads the window cells' codes and patch offsets from them
+  // instead of running the ambiguity test again
+  const bool records = ex->method == DISO_DMC && ex->codes && ex->codes_seg == seg && ex->codes_dims[0] == nx &&
+                       ex->codes_dims[1] == ny && ex->codes_dims[2] == nz;
   if (!zbulk) {
     if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
@@ -709,12 +722,12 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
       fused_backward_kernel<S, MC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
                                      (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
                                                                   normalize, 0, (S*)gsdf, (S*)gdef, ex->stats,
-                                                                  zbulk ? 1 : 0);
+                                                                  zbulk ? 1 : 0, nullptr);
     else
       fused_backward_kernel<S, DMC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
                                       (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
                                                                    normalize, exact, (S*)gsdf, (S*)gdef, ex->stats,
-                                                                   zbulk ? 1 : 0);
+                                                                   zbulk ? 1 : 0, records ? ex->codes : nullptr);
   }
   CUDA_TRY(cudaGetLastError());
   if (zbulk) return DISO_OK;
@@ -887,6 +900,7 @@ int64_t batch_record_slots(const diso_grid* grids, int n, int64_t* seg_total, in
 
 template <class S>
 int batch_prepare(diso_extractor* ex, const diso_grid* grids, int n, uint64_t* record, cudaStream_t s) {
+  ex->codes_seg = nullptr;  // the batch's records replace the last single grid's
   if (!ex->bdesc) {
     CUDA_TRY(cudaMalloc(&ex->bdesc, sizeof(BatchGrid<double>) * MAX_BATCH));
     CUDA_TRY(cudaMallocHost(&ex->bdesc_host, sizeof(BatchGrid<double>) * MAX_BATCH + sizeof(int64_t) * (MAX_BATCH + 1)));
@@ -1124,6 +1138,7 @@ int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint6
   if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
   const int64_t scan_tiles = scan_reserve(ex, g.nseg);
   if (scan_tiles == 0) return DISO_ERR_CUDA;
+  ex->codes_seg = nullptr;  // the field's records are not those of a dense grid
   ex->zpend.set = ex->zemit_set = false;  // gradient zeros belong to a dense forward
   count_prep_kernel<<<1, 256, 0, s>>>(ex->stats, ex->scan_flag, scan_tiles);
   CUDA_TRY(cudaGetLastError());

@@ -57,6 +57,7 @@ struct FusedShared {
   RowBits wb[CX][CY];
   uint32_t eb[CX][CY][2];          // scanned crossing counts of chunks zc, zc + 1 (MC vertex ids)
   uint32_t pb[KX][KY][2];          // scanned patch counts of chunks zc, zc + 1 (DMC)
+  uint8_t busy[KX][KY];            // DMC: bit 0/1/2: chunk zc-1 / zc / zc+1 of the row has a non-zero count
   uint16_t wcell[CX][CY][TZ + 1];  // per edge-row cell: its first window slot | crossing flags << 13
   uint16_t witems[fb_cap<S>()];
   uint8_t w32[CX][CY];
@@ -271,7 +272,8 @@ template <class S, int METHOD, class F = Field<S>>
 __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& f, const Geom& g,
                                            const uint64_t* __restrict__ seg, int64_t ptile, const S* __restrict__ gv,
                                            int64_t V, const S scale[3], int exact, S* __restrict__ gsdf,
-                                           S* __restrict__ gdef, bool& bad, double* __restrict__ part = nullptr) {
+                                           S* __restrict__ gdef, bool& bad, double* __restrict__ part = nullptr,
+                                           const CellRec* __restrict__ codes = nullptr) {
   using SH = FusedShared<S, METHOD>;
   constexpr int LO = SH::LO, CX = SH::CX, CY = SH::CY, KX = SH::KX, KY = SH::KY;
   constexpr int CAP = fb_cap<S>();
@@ -280,15 +282,22 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
   ptile_coords(ptile, g, X0, Y0, Z0);
   const int zc = Z0 / TZ;
   // segment values first, so that their loads overlap the mask loads: MC, the
-  // crossing counts of the edge rows; DMC, the patch counts of the window cell rows
-  constexpr int RY = METHOD == MC ? CY : KY, SLO = METHOD == MC ? 0 : 1;
-  constexpr int NSV = (METHOD == MC ? CX * CY : KX * KY) * 2;
+  // crossing counts of chunks zc, zc + 1 of the edge rows; DMC, the scanned values of
+  // chunks zc - 1 .. zc + 2 of the window cell rows (patch bases, and which chunks
+  // have a non-zero count)
+  constexpr int RY = METHOD == MC ? CY : KY, SLO = METHOD == MC ? 0 : 1, NSEG = METHOD == MC ? 2 : 4;
+  constexpr int NSV = (METHOD == MC ? CX * CY : KX * KY) * NSEG;
   static_assert(NSV <= NTHREADS, "one segment value per thread");
   uint64_t sv = 0;
-  const int si = threadIdx.x, sk = si & 1, sy = (si >> 1) % RY, sx = (si >> 1) / RY;
+  const int si = threadIdx.x, sk = si % NSEG, sy = (si / NSEG) % RY, sx = (si / NSEG) / RY;
+  const int sc = zc + (METHOD == MC ? sk : sk - 1);
+  bool sin = false;
   if (si < NSV) {
-    const int X = X0 - SLO + sx, Y = Y0 - SLO + sy, c = zc + sk;
-    if (X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && c < g.nzc) sv = seg[g.seg(X, Y, c)];
+    const int X = X0 - SLO + sx, Y = Y0 - SLO + sy;
+    // the value after a row's last chunk is the next row's first (the scan is
+    // global); after the grid's last chunk, the total
+    sin = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1] && sc >= 0 && sc <= g.nzc && (sc < g.nzc || sk >= 2);
+    if (sin) sv = seg[g.seg(X, Y, 0) + sc];
   }
   S dmn, dmx;
   bool dseen = false;
@@ -296,11 +305,19 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
   constexpr int ROWS_PW = (SH::WX * SH::WY + NTHREADS / 32 - 1) / (NTHREADS / 32);
   constexpr int MBATCH = ROWS_PW <= 10 ? ROWS_PW : (ROWS_PW + 1) / 2;
   load_masks<S, SH::WX, SH::WY, false, F, MBATCH>(sh.m, f, X0 - LO, Y0 - LO, Z0, dmn, dmx, dseen);
-  if (si < NSV) {
-    if constexpr (METHOD == MC)
-      sh.eb[sx][sy][sk] = Counts::lo(sv);
-    else
-      sh.pb[sx][sy][sk] = Counts::hi(sv);
+  if constexpr (METHOD == MC) {
+    if (si < NSV) sh.eb[sx][sy][sk] = Counts::lo(sv);
+  } else {
+    // chunk zc - 1 + k is busy when the scanned values at it and after it differ (the
+    // four values of a row sit in four consecutive lanes; every lane shuffles)
+    const uint64_t nxt = __shfl_down_sync(0xffffffffu, sv, 1, 4);
+    const bool nin = __shfl_down_sync(0xffffffffu, sin ? 1 : 0, 1, 4) != 0;
+    const uint32_t b = (sk < 3 && sin && nin && nxt != sv) ? (1u << sk) : 0u;
+    const uint32_t bits = b | __shfl_down_sync(0xffffffffu, b, 1, 4) | __shfl_down_sync(0xffffffffu, b, 2, 4);
+    if (si < NSV) {
+      if (sk == 1 || sk == 2) sh.pb[sx][sy][sk - 1] = Counts::hi(sv);
+      if (sk == 0) sh.busy[sx][sy] = (uint8_t)bits;
+    }
   }
   __syncthreads();
   // edge rows: crossing bits and the crossing flags of cell Z0 + TZ, one warp per row
@@ -321,6 +338,31 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
     }
   }
   if constexpr (METHOD == DMC) {
+   if (codes) {
+    // window cells from the forward count's cell records (resolved code, first patch
+    // inside the segment), as the emit reads them; segments with a zero count hold
+    // trivial cells only and have no records
+    for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+      const int rec = (busy & 2) && Z0 + lane < g.c[2] ? codes[g.code(X, Y, Z0 + lane)] : 0;
+      sh.rc[wx][wy][lane + 1] = (uint8_t)(rec & 0xff);
+      sh.first[wx][wy][lane + 1] = (int32_t)(sh.pb[wx][wy][0] + (uint32_t)(rec >> 9));
+    }
+    if (threadIdx.x < 2 * KX * KY) {
+      const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+      const int Z = end ? Z0 + TZ : Z0 - 1;
+      const int rec = (busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2] ? codes[g.code(X, Y, Z)] : 0;
+      const int rc = rec & 0xff;
+      sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
+      sh.first[wx][wy][end ? TZ + 1 : 0] =
+          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
+    }
+   } else {
     // window cells: codes after the ambiguity test and first patch ids.  One warp per
     // cell row, lane j for cell Z0 + j (rows without a non-trivial cell need no test
     // and no scan); then one thread per row end for cells Z0 - 1 and Z0 + TZ.
@@ -358,6 +400,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
       sh.first[wx][wy][end ? TZ + 1 : 0] =
           (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
     }
+   }
   }
   __syncthreads();
   // window slots: rows' bases by a block scan; slots in (row, cell, axis) order
@@ -516,7 +559,9 @@ __device__ __forceinline__ void zero_column(const Geom& g, const uint8_t* __rest
 }
 
 // Persistent over the active point tiles in list[0 .. *count) (active_ptiles_kernel
-// in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...  With zbulk, warp 0
+// in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...  DMC: `codes`, when
+// given, are the forward count's cell records of this grid (read instead of
+// recomputing the window cells' codes).  With zbulk, warp 0
 // also zeroes the point tiles with no crossing nearby, column b, b + gridDim.x, ...
 // of point tiles before each of its active tiles and the rest after the last (bulk
 // copies, zero_column); otherwise zero_tiles_kernel writes them beside it.  Bit 3 of
@@ -532,7 +577,8 @@ template <class S, int METHOD>
 __global__ void __launch_bounds__(NTHREADS, 3)
     fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
-                          S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats, int zbulk) {
+                          S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats, int zbulk,
+                          const CellRec* __restrict__ codes) {
   extern __shared__ __align__(16) unsigned char fb_smem[];
   FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
   const uint8_t* tile_flag = reinterpret_cast<const uint8_t*>(seg + g.nseg + 1);
@@ -558,7 +604,7 @@ __global__ void __launch_bounds__(NTHREADS, 3)
       zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
       col += gridDim.x;
     }
-    fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad);
+    fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad, nullptr, codes);
   }
   if (zbulk && warp == 0) {
     for (; col < ncol; col += gridDim.x) zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
