@@ -136,10 +136,28 @@ __device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>&
                                                    int64_t V, const S scale[3], int exact, S c0[4], S c1[4],
                                                    bool& bad) {
   S gvec[3];
-  fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
   if constexpr (F::kDense) {
-    edge_adjoint2<S>(f, X0 + x, Y0 + y, Z0 + j, a, gvec, c0, c1);
+    // the end points' loads first, so that they overlap the patches' gradient loads
+    const int X = X0 + x, Y = Y0 + y, Z = Z0 + j, ex = a == 0, ey = a == 1, ez = a == 2;
+    const bool in0 = f.inside(X, Y, Z), in1 = f.inside(X + ex, Y + ey, Z + ez);
+    const int64_t i0 = ((int64_t)min(max(X - 1, 0), f.n0 - 1) * f.n1 + min(max(Y - 1, 0), f.n1 - 1)) * f.n2 +
+                       min(max(Z - 1, 0), f.n2 - 1);
+    const int64_t i1 = ((int64_t)min(max(X - 1 + ex, 0), f.n0 - 1) * f.n1 + min(max(Y - 1 + ey, 0), f.n1 - 1)) * f.n2 +
+                       min(max(Z - 1 + ez, 0), f.n2 - 1);
+    const S v0 = __ldg(f.sdf + i0), v1 = __ldg(f.sdf + i1);
+    S q0[3] = {S(0), S(0), S(0)}, q1[3] = {S(0), S(0), S(0)};
+    if (f.def) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const S u0 = __ldg(f.def + 3 * i0 + k), u1 = __ldg(f.def + 3 * i1 + k);
+        q0[k] = in0 ? u0 : S(0);
+        q1[k] = in1 ? u1 : S(0);
+      }
+    }
+    fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
+    edge_adjoint_math<S>(f.iso, X, Y, Z, a, in0 ? v0 : f.pad, in1 ? v1 : f.pad, q0, q1, gvec, c0, c1);
   } else {
+    fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
     // an evaluated field: its values where the edge's ends lie, the same arithmetic
     const int X = X0 + x, Y = Y0 + y, Z = Z0 + j, ex = a == 0, ey = a == 1, ez = a == 2;
     S q0[3], q1[3];
@@ -342,13 +360,28 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
     // window cells from the forward count's cell records (resolved code, first patch
     // inside the segment), as the emit reads them; segments with a zero count hold
     // trivial cells only and have no records
-    for (int r = warp; r < KX * KY; r += NTHREADS / 32) {
-      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
-      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
-      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
-      const int rec = (busy & 2) && Z0 + lane < g.c[2] ? codes[g.code(X, Y, Z0 + lane)] : 0;
-      sh.rc[wx][wy][lane + 1] = (uint8_t)(rec & 0xff);
-      sh.first[wx][wy][lane + 1] = (int32_t)(sh.pb[wx][wy][0] + (uint32_t)(rec >> 9));
+    // a warp's rows' records are loaded together, then stored
+    constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32);
+    int rec[RPW];
+#pragma unroll
+    for (int k = 0; k < RPW; ++k) {
+      const int r = warp + (NTHREADS / 32) * k;
+      rec[k] = 0;
+      if (r < KX * KY) {
+        const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+        const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+        const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+        if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[g.code(X, Y, Z0 + lane)];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RPW; ++k) {
+      const int r = warp + (NTHREADS / 32) * k;
+      if (r < KX * KY) {
+        const int wx = r / KY, wy = r % KY;
+        sh.rc[wx][wy][lane + 1] = (uint8_t)(rec[k] & 0xff);
+        sh.first[wx][wy][lane + 1] = (int32_t)(sh.pb[wx][wy][0] + (uint32_t)(rec[k] >> 9));
+      }
     }
     if (threadIdx.x < 2 * KX * KY) {
       const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
@@ -448,12 +481,18 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
   const uint32_t nwi = sh.nwi;
   const bool cached = nwi <= (uint32_t)CAP;
   if (cached) {
-    for (uint32_t i = threadIdx.x; i < nwi; i += blockDim.x) {
-      int x, y, j, a;
+    // two edges per thread and pass, so that their loads are in flight together
+    for (uint32_t i = threadIdx.x; i < nwi; i += 2 * blockDim.x) {
+      const uint32_t i2 = i + blockDim.x;
+      int x, y, j, a, x2 = 0, y2 = 0, j2 = 0, a2 = 0;
       item_decode(sh.witems[i], x, y, j, a);
-      S c0[4], c1[4];
+      const bool two = i2 < nwi;
+      if (two) item_decode(sh.witems[i2], x2, y2, j2, a2);
+      S c0[4], c1[4], d0[4], d1[4];
       fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
+      if (two) fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x2, y2, j2, a2, gv, V, scale, exact, d0, d1, bad);
       store_adj<S>(&sh.adj[0][0], i, c0, c1);
+      if (two) store_adj<S>(&sh.adj[0][0], i2, d0, d1);
     }
     __syncthreads();
   }
