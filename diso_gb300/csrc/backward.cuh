@@ -481,18 +481,12 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
   const uint32_t nwi = sh.nwi;
   const bool cached = nwi <= (uint32_t)CAP;
   if (cached) {
-    // two edges per thread and pass, so that their loads are in flight together
-    for (uint32_t i = threadIdx.x; i < nwi; i += 2 * blockDim.x) {
-      const uint32_t i2 = i + blockDim.x;
-      int x, y, j, a, x2 = 0, y2 = 0, j2 = 0, a2 = 0;
+    for (uint32_t i = threadIdx.x; i < nwi; i += blockDim.x) {
+      int x, y, j, a;
       item_decode(sh.witems[i], x, y, j, a);
-      const bool two = i2 < nwi;
-      if (two) item_decode(sh.witems[i2], x2, y2, j2, a2);
-      S c0[4], c1[4], d0[4], d1[4];
+      S c0[4], c1[4];
       fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
-      if (two) fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x2, y2, j2, a2, gv, V, scale, exact, d0, d1, bad);
       store_adj<S>(&sh.adj[0][0], i, c0, c1);
-      if (two) store_adj<S>(&sh.adj[0][0], i2, d0, d1);
     }
     __syncthreads();
   }
