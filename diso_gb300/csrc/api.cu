@@ -81,6 +81,7 @@ struct diso_extractor {
   int emit_ctas = 0;             // the same for the emit
   int fused_ctas = 0;            // the same for the fused backward
   int fused_smem = 0;            // its dynamic shared memory per CTA
+  int fused_smem_rec = 0;        // the same for its variant that reads the DMC cell records
   int per_sm[4] = {1, 1, 1, 1};  // resident CTAs per SM of the count (TMA), emit, gather, fused backward
   // launch widths set by diso_tune_set (0: the default), and the zeros' count share
   int tune[DISO_TUNE_N] = {};
@@ -344,15 +345,21 @@ int bind_device(diso_extractor* ex) {
     ex->per_sm[1] = std::max(per_e, 1);
     int per_f = 0;
     const void* fk = ex->dtype == DISO_F32
-                         ? (ex->method == DISO_MC ? (const void*)fused_backward_kernel<float, MC>
-                                                  : (const void*)fused_backward_kernel<float, DMC>)
-                         : (ex->method == DISO_MC ? (const void*)fused_backward_kernel<double, MC>
-                                                  : (const void*)fused_backward_kernel<double, DMC>);
+                         ? (ex->method == DISO_MC ? (const void*)fused_backward_kernel<float, MC, false>
+                                                  : (const void*)fused_backward_kernel<float, DMC, false>)
+                         : (ex->method == DISO_MC ? (const void*)fused_backward_kernel<double, MC, false>
+                                                  : (const void*)fused_backward_kernel<double, DMC, false>);
     ex->fused_smem = (int)(ex->dtype == DISO_F32
                                ? (ex->method == DISO_MC ? fused_smem<float, MC>() : fused_smem<float, DMC>())
                                : (ex->method == DISO_MC ? fused_smem<double, MC>() : fused_smem<double, DMC>()));
     CUDA_TRY(cudaFuncSetAttribute(fk, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, fk, NTHREADS, ex->fused_smem));
+    if (ex->method == DISO_DMC) {  // the variant that reads the count's cell records
+      const void* fr = ex->dtype == DISO_F32 ? (const void*)fused_backward_kernel<float, DMC, true>
+                                             : (const void*)fused_backward_kernel<double, DMC, true>;
+      ex->fused_smem_rec = (int)(ex->dtype == DISO_F32 ? fused_smem<float, DMC, true>() : fused_smem<double, DMC, true>());
+      CUDA_TRY(cudaFuncSetAttribute(fr, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem_rec));
+    }
     ex->fused_ctas = sms * std::max(per_f, 1);
     ex->per_sm[3] = std::max(per_f, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
@@ -719,15 +726,20 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   {
     KernelTimer kt(ex, K_FUSED_BWD, s);
     if (ex->method == DISO_MC)
-      fused_backward_kernel<S, MC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
+      fused_backward_kernel<S, MC, false><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
                                      (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
                                                                   normalize, 0, (S*)gsdf, (S*)gdef, ex->stats,
                                                                   zbulk ? 1 : 0, nullptr);
+    else if (records)
+      fused_backward_kernel<S, DMC, true><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]),
+                                            NTHREADS, (size_t)ex->fused_smem_rec, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats,
+          zbulk ? 1 : 0, ex->codes);
     else
-      fused_backward_kernel<S, DMC><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]), NTHREADS,
-                                      (size_t)ex->fused_smem, s>>>(f, g, seg, ex->plist, ex->plist_n, (const S*)gv,
-                                                                   normalize, exact, (S*)gsdf, (S*)gdef, ex->stats,
-                                                                   zbulk ? 1 : 0, records ? ex->codes : nullptr);
+      fused_backward_kernel<S, DMC, false><<<tuned_ctas(ex, DISO_TUNE_FUSED_CTAS, ex->fused_ctas, ex->per_sm[3]),
+                                             NTHREADS, (size_t)ex->fused_smem, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gsdf, (S*)gdef, ex->stats,
+          zbulk ? 1 : 0, nullptr);
   }
   CUDA_TRY(cudaGetLastError());
   if (zbulk) return DISO_OK;

@@ -43,14 +43,17 @@ __host__ __device__ constexpr int fb_cap() {
 
 constexpr int FB_ZBLOCK = 2048;  // bytes of the zeroed block the bulk zero copies read
 
-template <class S, int METHOD>
+// REC: the DMC window cells' codes come from the forward count's cell records
+template <class S, int METHOD, bool REC = false>
 struct FusedShared {
-  // mask rows start at (X0 - LO, Y0 - LO): MC, the edge rows' points; DMC, two rows
-  // further, so that the ambiguity test of every window cell finds its neighbour's
-  // code in the masks (on the noisy surfaces of dense fields most window rows hold
-  // ambiguous cells, and a neighbour from global memory stalls the row's warp)
-  static constexpr int LO = METHOD == DMC ? 2 : 0;
-  static constexpr int WX = TX + 2 + (METHOD == DMC ? 3 : 0), WY = TY + 2 + (METHOD == DMC ? 3 : 0);
+  // mask rows start at (X0 - LO, Y0 - LO): the edge rows' points; for DMC codes
+  // computed here two rows further, so that the ambiguity test of every window cell
+  // finds its neighbour's code in the masks (on the noisy surfaces of dense fields
+  // most window rows hold ambiguous cells, and a neighbour from global memory stalls
+  // the row's warp)
+  static constexpr bool WIDE = METHOD == DMC && !REC;
+  static constexpr int LO = WIDE ? 2 : 0;
+  static constexpr int WX = TX + 2 + (WIDE ? 3 : 0), WY = TY + 2 + (WIDE ? 3 : 0);
   static constexpr int CX = TX + 1, CY = TY + 1;  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
   static constexpr int KX = METHOD == DMC ? TX + 2 : 1, KY = METHOD == DMC ? TY + 2 : 1;  // DMC window cell rows
   uint64_t m[WX][WY];
@@ -78,8 +81,8 @@ struct FusedShared {
 // (X0 + x, Y0 + y, Z0 + j), x in [0, TX], y in [0, TY], j in [0, TZ]), in padded
 // coordinates (the chain rule of the shift and the normalisation in `scale`), as
 // the stored backward's edge pass forms it (edge_adjoint_at in kernels.cuh).
-template <class S, int METHOD>
-__device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh, int x, int y, int j, int a,
+template <class S, int METHOD, class SH>
+__device__ __forceinline__ void fused_edge_grad(const SH& sh, int x, int y, int j, int a,
                                                 const S* __restrict__ gv, int64_t V, const S scale[3], int exact,
                                                 S gvec[3], bool& bad) {
   if constexpr (METHOD == MC) {
@@ -130,8 +133,8 @@ __device__ __forceinline__ void fused_edge_grad(const FusedShared<S, METHOD>& sh
 }
 
 // adjoints (c0 at the edge's first point, c1 at its second) of window edge (x, y, j, a)
-template <class S, int METHOD, class F>
-__device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>& sh, const F& f, int X0, int Y0,
+template <class S, int METHOD, class F, class SH>
+__device__ __forceinline__ void fused_edge_adjoint(const SH& sh, const F& f, int X0, int Y0,
                                                    int Z0, int x, int y, int j, int a, const S* __restrict__ gv,
                                                    int64_t V, const S scale[3], int exact, S c0[4], S c1[4],
                                                    bool& bad) {
@@ -154,10 +157,10 @@ __device__ __forceinline__ void fused_edge_adjoint(const FusedShared<S, METHOD>&
         q1[k] = in1 ? u1 : S(0);
       }
     }
-    fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
+    fused_edge_grad<S, METHOD, SH>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
     edge_adjoint_math<S>(f.iso, X, Y, Z, a, in0 ? v0 : f.pad, in1 ? v1 : f.pad, q0, q1, gvec, c0, c1);
   } else {
-    fused_edge_grad<S, METHOD>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
+    fused_edge_grad<S, METHOD, SH>(sh, x, y, j, a, gv, V, scale, exact, gvec, bad);
     // an evaluated field: its values where the edge's ends lie, the same arithmetic
     const int X = X0 + x, Y = Y0 + y, Z = Z0 + j, ex = a == 0, ey = a == 1, ez = a == 2;
     S q0[3], q1[3];
@@ -176,8 +179,8 @@ struct Adj4 {
 // the uncached path's per-point call, kept out of line (it runs only for tiles with
 // more window edges than the cache holds): the adjoint at end k of window edge
 // (x, y, j, a)
-template <class S, int METHOD, class F>
-__device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METHOD>& sh, const F& f, int X0,
+template <class S, int METHOD, class F, class SH>
+__device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const SH& sh, const F& f, int X0,
                                                        int Y0, int Z0, int x, int y, int j, int a,
                                                        const S* __restrict__ gv, int64_t V, S sx, S sy, S sz,
                                                        int exact, int k) {
@@ -185,7 +188,7 @@ __device__ __noinline__ Adj4<S> fused_edge_adjoint_far(const FusedShared<S, METH
   const S scale[3] = {sx, sy, sz};
   Adj4<S> r;
   r.bad = false;
-  fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, r.bad);
+  fused_edge_adjoint<S, METHOD, F, SH>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, r.bad);
 #pragma unroll
   for (int i = 0; i < 4; ++i) r.v[i] = k ? c1[i] : c0[i];
   return r;
@@ -286,13 +289,13 @@ __device__ __forceinline__ void field_param_add(const SphereField<S>& f, double*
 // one active point tile (see the top of this file); for an evaluated field the
 // point gradients go to the spheres' parameters (field_param_add into `part`) and
 // only the deform's gradient is written
-template <class S, int METHOD, class F = Field<S>>
-__device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& f, const Geom& g,
+template <class S, int METHOD, class F = Field<S>, bool REC = false>
+__device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, const F& f, const Geom& g,
                                            const uint64_t* __restrict__ seg, int64_t ptile, const S* __restrict__ gv,
                                            int64_t V, const S scale[3], int exact, S* __restrict__ gsdf,
                                            S* __restrict__ gdef, bool& bad, double* __restrict__ part = nullptr,
                                            const CellRec* __restrict__ codes = nullptr) {
-  using SH = FusedShared<S, METHOD>;
+  using SH = FusedShared<S, METHOD, REC>;
   constexpr int LO = SH::LO, CX = SH::CX, CY = SH::CY, KX = SH::KX, KY = SH::KY;
   constexpr int CAP = fb_cap<S>();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -356,7 +359,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
     }
   }
   if constexpr (METHOD == DMC) {
-   if (codes) {
+   if constexpr (REC) {
     // window cells from the forward count's cell records (resolved code, first patch
     // inside the segment), as the emit reads them; segments with a zero count hold
     // trivial cells only and have no records
@@ -485,7 +488,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
       int x, y, j, a;
       item_decode(sh.witems[i], x, y, j, a);
       S c0[4], c1[4];
-      fused_edge_adjoint<S, METHOD, F>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
+      fused_edge_adjoint<S, METHOD, F, SH>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
       store_adj<S>(&sh.adj[0][0], i, c0, c1);
     }
     __syncthreads();
@@ -520,7 +523,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD>& sh, const F& 
       for (int e = 0; e < 6; ++e)
         if ((on >> e) & 1) {
           const Adj4<S> o =
-              fused_edge_adjoint_far<S, METHOD, F>(sh, f, X0, Y0, Z0, x - (e == 1), y - (e == 3), j - (e == 5), e >> 1,
+              fused_edge_adjoint_far<S, METHOD, F, SH>(sh, f, X0, Y0, Z0, x - (e == 1), y - (e == 3), j - (e == 5), e >> 1,
                                                 gv, V, scale[0], scale[1], scale[2], exact, e & 1);
           acc[0] += o.v[0];
           acc[1] += o.v[1];
@@ -601,19 +604,19 @@ __device__ __forceinline__ void zero_column(const Geom& g, const uint8_t* __rest
 // stats->error is set when an index derived from the grid falls outside the
 // forward's counts (the grid no longer matches the forward's record); no access
 // leaves its buffer.
-template <class S, int METHOD>
+template <class S, int METHOD, bool REC = false>
 __host__ __device__ constexpr size_t fused_smem() {
-  return sizeof(FusedShared<S, METHOD>);
+  return sizeof(FusedShared<S, METHOD, REC>);
 }
 
-template <class S, int METHOD>
+template <class S, int METHOD, bool REC>
 __global__ void __launch_bounds__(NTHREADS, 3)
     fused_backward_kernel(Field<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
                           S* __restrict__ gsdf, S* __restrict__ gdef, Stats* stats, int zbulk,
                           const CellRec* __restrict__ codes) {
   extern __shared__ __align__(16) unsigned char fb_smem[];
-  FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
+  FusedShared<S, METHOD, REC>& sh = *reinterpret_cast<FusedShared<S, METHOD, REC>*>(fb_smem);
   const uint8_t* tile_flag = reinterpret_cast<const uint8_t*>(seg + g.nseg + 1);
   const int64_t ncol = (int64_t)g.ptiles_x() * g.ptiles_y();
   int64_t col = blockIdx.x;  // the next column of point tiles this CTA zeroes
@@ -637,7 +640,8 @@ __global__ void __launch_bounds__(NTHREADS, 3)
       zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
       col += gridDim.x;
     }
-    fused_tile<S, METHOD>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad, nullptr, codes);
+    fused_tile<S, METHOD, Field<S>, REC>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad, nullptr,
+                                         codes);
   }
   if (zbulk && warp == 0) {
     for (; col < ncol; col += gridDim.x) zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
