@@ -363,21 +363,18 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
     // window cells from the forward count's cell records (resolved code, first patch
     // inside the segment), as the emit reads them; segments with a zero count hold
     // trivial cells only and have no records
-    // a warp's rows' records are loaded together (lane 0 also that of the row's cell
-    // Z0 - 1, lane 31 that of cell Z0 + TZ), then stored
+    // a warp's rows' records are loaded together, then stored
     constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32);
-    int rec[RPW], ext[RPW];
+    int rec[RPW];
 #pragma unroll
     for (int k = 0; k < RPW; ++k) {
       const int r = warp + (NTHREADS / 32) * k;
-      rec[k] = ext[k] = 0;
+      rec[k] = 0;
       if (r < KX * KY) {
         const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
         const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
         const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
         if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[g.code(X, Y, Z0 + lane)];
-        if (lane == 0 && (busy & 1) && Z0 >= 1) ext[k] = codes[g.code(X, Y, Z0 - 1)];
-        if (lane == 31 && (busy & 4) && Z0 + TZ < g.c[2]) ext[k] = codes[g.code(X, Y, Z0 + TZ)];
       }
     }
 #pragma unroll
@@ -387,17 +384,19 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
         const int wx = r / KY, wy = r % KY;
         sh.rc[wx][wy][lane + 1] = (uint8_t)(rec[k] & 0xff);
         sh.first[wx][wy][lane + 1] = (int32_t)(sh.pb[wx][wy][0] + (uint32_t)(rec[k] >> 9));
-        if (lane == 0) {
-          // cell Z0 - 1 is the previous segment's last: its patches end at this one's base
-          const int rc = ext[k] & 0xff;
-          sh.rc[wx][wy][0] = (uint8_t)rc;
-          sh.first[wx][wy][0] = (int32_t)(sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
-        }
-        if (lane == 31) {  // cell Z0 + TZ is the next segment's first
-          sh.rc[wx][wy][TZ + 1] = (uint8_t)(ext[k] & 0xff);
-          sh.first[wx][wy][TZ + 1] = (int32_t)sh.pb[wx][wy][1];
-        }
       }
+    }
+    if (threadIdx.x < 2 * KX * KY) {
+      const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+      const int Z = end ? Z0 + TZ : Z0 - 1;
+      const int rec = (busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2] ? codes[g.code(X, Y, Z)] : 0;
+      const int rc = rec & 0xff;
+      sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
+      sh.first[wx][wy][end ? TZ + 1 : 0] =
+          (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
     }
    } else {
     // window cells: codes after the ambiguity test and first patch ids.  One warp per
