@@ -41,7 +41,10 @@ import torch  # noqa: E402
 
 SEED = 2
 DEFORM = 0.45
-METRIC = "fwd+bwd grids/s @512^3 (DiffDMC, fp32, deform, return_quads)"
+
+
+def metric_name(n):
+    return f"fwd+bwd grids/s @{n}^3 (DiffDMC, fp32, deform, return_quads)"
 
 
 def spheres_field(n, device, dtype=torch.float32, seed=SEED):
@@ -459,7 +462,7 @@ class PhaseEvents:
         return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in self.done.items()}
 
 
-def kernel_bytes(vol, nseg, nv, nq, s, zshare, active_pts):
+def kernel_bytes(vol, nseg, nv, nq, s, zshare, active_pts, zeros_in_fused=True):
     """Algorithmic bytes per launch of each kernel of the 512^3 DMC step: what the
     kernel's function must read and write at least (nq crossing edges = quads, nv
     patches = vertices, s bytes per scalar, active_pts = points of the point tiles
@@ -470,7 +473,9 @@ def kernel_bytes(vol, nseg, nv, nq, s, zshare, active_pts):
     "zero_grads", when the buffers do not allow it) and the emit the edge record;
     the backward's edge pass and gather read it.  Recompute mode: the forward writes
     no zeros and no record; the backward zeroes the point tiles with no crossing
-    nearby (zero_tiles) and recomputes the rest in one pass (fused_bwd)."""
+    nearby and recomputes the rest in one pass (fused_bwd); the zeros are bulk copies
+    issued by the fused pass itself (zeros_in_fused) or, for grids whose rows are no
+    multiple of 16 bytes, a kernel of their own (zero_tiles)."""
     zeros = vol * 4 * s
     return {
         # the SDF once; the per-segment counts out; its share of the zeros (stored mode)
@@ -490,8 +495,9 @@ def kernel_bytes(vol, nseg, nv, nq, s, zshare, active_pts):
         # the gradients of the point tiles with no crossing nearby
         "zero_tiles": (vol - active_pts) * 4 * s,
         # the SDF of the active tiles in, their gradients out; the deform at both ends of
-        # every crossing edge and dL/dverts in
-        "fused_bwd": active_pts * 5 * s + nq * 2 * 3 * s + nv * 3 * s,
+        # every crossing edge and dL/dverts in; the other tiles' zeros when it writes them
+        "fused_bwd": active_pts * 5 * s + nq * 2 * 3 * s + nv * 3 * s
+        + ((vol - active_pts) * 4 * s if zeros_in_fused else 0),
     }
 
 
@@ -738,7 +744,7 @@ def run_ours(args, rank, world, device):
     vol = n ** 3
     nseg = (n + 1) ** 2 * ((n + 1 + 31) // 32)
     act_pts = active_points(sdf)
-    algo = kernel_bytes(vol, nseg, nv, nq, s_b, 0.0, act_pts)
+    algo = kernel_bytes(vol, nseg, nv, nq, s_b, 0.0, act_pts, zeros_in_fused="zero_tiles" not in kernels)
     zshare = 0.0 if "zero_grads" in k_st else float(N.lib().diso_zero_count_share())
     algo_st = kernel_bytes(vol, nseg, nv, nq, s_b, zshare, act_pts)
     per_launch = {k: ms / max(cnt, 1) for k, (cnt, ms) in kernels.items()}
@@ -750,7 +756,7 @@ def run_ours(args, rank, world, device):
     step_bytes = vol * s_b * (3 + 3) + 4 * nq * 3 * s_b + 2 * nv * 3 * s_b + 8 * nq * 4
     ms_step = ms_max / args.steps
     res = {
-        "metric": METRIC,
+        "metric": metric_name(n),
         "value": job_throughput(world, args.steps, ms_max),
         "unit": "grids/s",
         "n_gpus": world,
@@ -761,7 +767,7 @@ def run_ours(args, rank, world, device):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic: min of 16 seeded spheres + 0.01*N(0,1) noise at 512^3, deform U(-0.45,0.45)",
+        "data": f"synthetic: min of 16 seeded spheres + 0.01*N(0,1) noise at {n}^3, deform U(-0.45,0.45)",
         "config": {"workload": f"dmc_fwd_bwd_{n}_spheres16", "n": n, "method": "DiffDMC", "return_quads": True,
                    "deform": True, "normalize": True, "backward": "recompute", "verts": nv, "quads": nq,
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
@@ -906,7 +912,7 @@ def main():
         # each step a bounded sample, sized so that the whole run stays within ~3 minutes
         budget = min(20.0, max(0.1, 180.0 / max(1, steps + warmup)))
         value, planes, cores, sec = run_cpu(args, steps, warmup, budget_s=budget)
-        out = {"metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": args.gpus, "steps": steps,
+        out = {"metric": metric_name(args.n), "value": value, "unit": "grids/s", "n_gpus": args.gpus, "steps": steps,
                "warmup": warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (same field as ours)",
                "config": {"workload": f"dmc_fwd_bwd_{args.n}_spheres16", "n": args.n, "method": "DiffDMC",
