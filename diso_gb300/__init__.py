@@ -10,10 +10,11 @@ The compute path is hand-written sm_103a CUDA behind the C ABI of
 include/diso_gb300.h; there is no CPU path.
 """
 from .batch import BatchPlan, DiffDMCBatch, DiffMCBatch, extract_batch  # noqa: F401
+from .bricks import BrickGrid, extract_bricks  # noqa: F401
 from .extraction import DiffDMC, DiffMC, extract  # noqa: F401
 from .fields import SphereUnion, extract_field  # noqa: F401
 from . import tune  # noqa: F401
 
 __all__ = ["DiffMC", "DiffDMC", "extract", "DiffMCBatch", "DiffDMCBatch", "extract_batch", "BatchPlan", "SphereUnion",
-           "extract_field", "tune"]
+           "extract_field", "BrickGrid", "extract_bricks", "tune"]
 __version__ = "0.1.0"

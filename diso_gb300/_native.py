@@ -56,6 +56,22 @@ class SphereFieldDesc(ctypes.Structure):
     ]
 
 
+BRICK = 8
+BRICK_OUTSIDE, BRICK_INSIDE = -1, -2
+
+
+class BrickGridDesc(ctypes.Structure):
+    """diso_brick_grid: dims, index [ceil(n/8)]^3 int32, values [count][8][8][8], deform or NULL, background."""
+    _fields_ = [
+        ("dims", ctypes.c_int * 3),
+        ("index", ctypes.c_void_p),
+        ("count", ctypes.c_int),
+        ("values", ctypes.c_void_p),
+        ("deform", ctypes.c_void_p),
+        ("background", ctypes.c_double),
+    ]
+
+
 EXPORTS = {
     # name: (restype, argtypes)
     "diso_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
@@ -101,6 +117,15 @@ EXPORTS = {
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_field_materialize": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(SphereFieldDesc), ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_forward_bricks": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BrickGridDesc), ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                           ctypes.POINTER(Counts)]),
+    "diso_backward_bricks": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BrickGridDesc), ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "diso_bricks_materialize": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(BrickGridDesc), ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p]),
     "diso_mesh_normals": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                          ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "diso_mesh_weld": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
@@ -185,6 +210,7 @@ class Extractor:
         # (dense grids and evaluated fields), for the single-call forward
         self.size_hints = {}
         self.field_hints = {}
+        self.brick_hints = {}
         self._h = ctypes.c_void_p()
         check(lib().diso_create(method, dtype_tag(dtype), ctypes.byref(self._h)), "create")
 
@@ -290,6 +316,20 @@ class Extractor:
         check(lib().diso_backward_field(self._h, ctypes.byref(desc), *shape, iso, pad, ptr(seg), int(bool(normalize)),
                                         GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_spheres),
                                         ptr(grad_deform), stream_of(grad_verts.device)), "backward of a field")
+
+    def forward_bricks(self, desc, iso, pad, seg, normalize, verts, faces) -> Counts:
+        """The forward of a narrow band in one call (see diso_forward_bricks)."""
+        c = Counts()
+        check(lib().diso_forward_bricks(self._h, ctypes.byref(desc), iso, pad, ptr(seg), int(bool(normalize)),
+                                        ptr(verts), verts.shape[0], ptr(faces), faces.shape[0],
+                                        stream_of(verts.device), ctypes.byref(c)), "forward of a narrow band")
+        return c
+
+    def backward_bricks(self, desc, iso, pad, seg, normalize, grad_verts, grad_values, grad_deform, exact=False):
+        """Gradients of a narrow band's slots (see diso_backward_bricks)."""
+        check(lib().diso_backward_bricks(self._h, ctypes.byref(desc), iso, pad, ptr(seg), int(bool(normalize)),
+                                         GRAD_EXACT if exact else 0, ptr(grad_verts), ptr(grad_values),
+                                         ptr(grad_deform), stream_of(grad_verts.device)), "backward of a narrow band")
 
     # mesh consumers (diso_mesh_*): the extractor supplies the dtype and the scratch
     def mesh_normals(self, verts, faces, out):

@@ -108,6 +108,11 @@ struct diso_extractor {
   int64_t isog_cap = 0;
   double* fpart = nullptr;       // per-CTA sums of a field backward's sphere gradients
   int64_t fpart_cap = 0;
+  int* buses = nullptr;          // narrow band: uses of each brick slot (brick_check_kernel)
+  int64_t buses_cap = 0;
+  unsigned long long* bcheck = nullptr;  // its results (bad bits, present, border bricks)
+  int64_t bcheck_cap = 0;
+  int brick_ctas = 0;            // resident CTAs of the narrow band's backward
 
   // batch state (diso_batch_*): descriptors, per-grid status, layout of the record
   void* bdesc = nullptr;         // device BatchGrid<S>[MAX_BATCH]
@@ -176,6 +181,12 @@ struct diso_extractor {
     cudaFree(fpart);
     fpart = nullptr;
     fpart_cap = 0;
+    cudaFree(buses);
+    buses = nullptr;
+    buses_cap = 0;
+    cudaFree(bcheck);
+    bcheck = nullptr;
+    bcheck_cap = 0;
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -362,6 +373,16 @@ int bind_device(diso_extractor* ex) {
     }
     ex->fused_ctas = sms * std::max(per_f, 1);
     ex->per_sm[3] = std::max(per_f, 1);
+    // the narrow band's backward: the fused tile with the same shared memory
+    const void* bk = ex->dtype == DISO_F32
+                         ? (ex->method == DISO_MC ? (const void*)brick_backward_kernel<float, MC>
+                                                  : (const void*)brick_backward_kernel<float, DMC>)
+                         : (ex->method == DISO_MC ? (const void*)brick_backward_kernel<double, MC>
+                                                  : (const void*)brick_backward_kernel<double, DMC>);
+    int per_b = 0;
+    CUDA_TRY(cudaFuncSetAttribute(bk, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, bk, NTHREADS, ex->fused_smem));
+    ex->brick_ctas = sms * std::max(per_b, 1);
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
@@ -1137,11 +1158,12 @@ SphereField<S> make_sphere_field(const diso_sphere_field* d, int nx, int ny, int
   return f;
 }
 
-// The forward of an evaluated field in one call, as forward_all without deform or
-// edge record: the count evaluates the chunks near the surface (the others it
-// classifies whole), the emit evaluates the end points of the crossing edges.
-template <class S>
-int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint64_t* seg, int normalize,
+// The forward of an evaluated field (a union of spheres, a narrow band of bricks) in
+// one call, as forward_all without edge record: the count evaluates the chunks near
+// the surface (the others it classifies whole), the emit evaluates the end points of
+// the crossing edges.
+template <class S, class F>
+int forward_field(diso_extractor* ex, const F& f, double iso, uint64_t* seg, int normalize,
                   void* verts, int64_t vcap, int64_t* faces, int64_t fcap, cudaStream_t s, diso_counts* out) {
   Geom g;
   g.init(f.n0, f.n1, f.n2);
@@ -1162,11 +1184,9 @@ int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint6
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     KernelTimer kt(ex, K_COUNT, s);
     if (ex->method == DISO_MC)
-      count_kernel<S, MC, SphereField<S>><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
-                                                                    ex->active);
+      count_kernel<S, MC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
     else
-      count_kernel<S, DMC, SphereField<S>><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
-                                                                     ex->active);
+      count_kernel<S, DMC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
   }
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->total))) != DISO_OK)
@@ -1177,10 +1197,10 @@ int forward_field(diso_extractor* ex, const SphereField<S>& f, double iso, uint6
     const ZeroJob zj{};
     KernelTimer kt(ex, K_EMIT, s);
     if (ex->method == DISO_MC)
-      mc_emit_kernel<S, SphereField<S>><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
+      mc_emit_kernel<S, F><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
           f, g, seg, ex->active, &ex->stats->n_active, (S*)verts, faces, normalize, nullptr, vcap, fcap, ex->stats, zj);
     else
-      dmc_emit_kernel<S, SphereField<S>><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
+      dmc_emit_kernel<S, F><<<(unsigned)ex->emit_ctas, NTHREADS, 0, s>>>(
           f, g, seg, codes, ex->active, &ex->stats->n_active, (S*)verts, faces, normalize, nullptr, vcap, fcap,
           ex->stats, zj);
   }
@@ -1229,6 +1249,105 @@ int check_field(const diso_sphere_field* field, int nx, int ny, int nz) {
   if (3.0 * cells >= 2147483647.0) return fail(DISO_ERR_ARG, "grid too large: %d x %d x %d", nx, ny, nz);
   for (int a = 0; a < 3; ++a)
     if (!std::isfinite(field->lo[a]) || !std::isfinite(field->hi[a])) return fail(DISO_ERR_ARG, "non-finite bounds");
+  return DISO_OK;
+}
+
+// ------------------------------------------------------------------ narrow band
+
+template <class S>
+BrickField<S> make_brick_field(const diso_brick_grid* b, double iso, double padval) {
+  BrickField<S> f;
+  f.index = b->index;
+  f.val = (const S*)b->values;
+  f.def = (const S*)b->deform;
+  f.nb1 = (b->dims[1] + BRICK - 1) / BRICK;
+  f.nb2 = (b->dims[2] + BRICK - 1) / BRICK;
+  f.K = b->count;
+  f.n0 = b->dims[0];
+  f.n1 = b->dims[1];
+  f.n2 = b->dims[2];
+  f.iso = (S)iso;
+  f.pad = (S)padval;
+  f.bg = (S)b->background;
+  return f;
+}
+
+// the arguments of a narrow band, before any CUDA call
+int check_bricks(const diso_brick_grid* b) {
+  if (!b || !b->index) return fail(DISO_ERR_ARG, "null brick grid or index");
+  const int nx = b->dims[0], ny = b->dims[1], nz = b->dims[2];
+  if (nx < 1 || ny < 1 || nz < 1) return fail(DISO_ERR_ARG, "grid dims must be >= 1 (got %d x %d x %d)", nx, ny, nz);
+  if (nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30)) return fail(DISO_ERR_ARG, "grid dims above 2^30");
+  if (b->count < 0) return fail(DISO_ERR_ARG, "negative brick count %d", b->count);
+  if (b->count > 0 && !b->values) return fail(DISO_ERR_ARG, "null brick values");
+  if (!std::isfinite(b->background) || !(b->background > 0.0))
+    return fail(DISO_ERR_ARG, "background must be finite and > 0 (got %g)", b->background);
+  return DISO_OK;
+}
+
+// One pass over the index (brick_check_kernel), read back: slots and tags valid, no
+// slot used twice, and the crossings that the bricks allow fit the 32-bit counts
+template <class S>
+int validate_bricks(diso_extractor* ex, const diso_brick_grid* b, double iso, double padval, cudaStream_t s) {
+  const int nb0 = (b->dims[0] + BRICK - 1) / BRICK, nb1 = (b->dims[1] + BRICK - 1) / BRICK,
+            nb2 = (b->dims[2] + BRICK - 1) / BRICK;
+  const int64_t nb = (int64_t)nb0 * nb1 * nb2;
+  int rc;
+  if ((rc = grow(ex->buses, ex->buses_cap, std::max(b->count, 1))) != DISO_OK) return rc;
+  if ((rc = grow(ex->bcheck, ex->bcheck_cap, 4)) != DISO_OK) return rc;
+  if (b->count) CUDA_TRY(cudaMemsetAsync(ex->buses, 0, sizeof(int) * (size_t)b->count, s));
+  CUDA_TRY(cudaMemsetAsync(ex->bcheck, 0, 4 * sizeof(unsigned long long), s));
+  const S bg = (S)b->background, isoS = (S)iso;
+  brick_check_kernel<<<stride_ctas(nb, ex->sms * 8), 256, 0, s>>>(b->index, nb0, nb1, nb2, b->count, bg >= isoS ? 1 : 0,
+                                                                  -bg >= isoS ? 1 : 0, (S)padval >= isoS ? 1 : 0,
+                                                                  ex->buses, ex->bcheck);
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long h[4] = {0, 0, 0, 0};
+  CUDA_TRY(cudaMemcpyAsync(h, ex->bcheck, sizeof(h), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (h[0] & 1ull) return fail(DISO_ERR_ARG, "brick index: an entry is neither a slot in [0, %d) nor -1 / -2", b->count);
+  if (h[0] & 2ull) return fail(DISO_ERR_ARG, "brick index: a slot is used by two bricks");
+  // crossings are counted in 32 bits per half of the scan value: at most 3 per cell,
+  // and only cells touching a present or a border brick can cross
+  const double cells = std::min((double)(b->dims[0] + 1) * (b->dims[1] + 1) * (b->dims[2] + 1),
+                                729.0 * (double)(h[1] + h[2]));
+  if (3.0 * cells >= 2147483647.0)
+    return fail(DISO_ERR_ARG, "narrow band too wide for 32-bit counts: %llu present and %llu border bricks", h[1],
+                h[2]);
+  return DISO_OK;
+}
+
+// the backward of a narrow band: its gradient slots zeroed, then the fused tile over
+// the active point tiles with the gradients going to the slots
+template <class S>
+int backward_bricks(diso_extractor* ex, const BrickField<S>& f, int K, const uint64_t* seg, int normalize, int flags,
+                    const void* gv, void* gval, void* gdef, cudaStream_t s) {
+  Geom g;
+  g.init(f.n0, f.n1, f.n2);
+  int rc;
+  if ((rc = grow(ex->plist, ex->plist_cap, g.nptiles())) != DISO_OK) return rc;
+  if (K) {
+    CUDA_TRY(cudaMemsetAsync(gval, 0, (size_t)K * BRICK_PTS * sizeof(S), s));
+    if (gdef) CUDA_TRY(cudaMemsetAsync(gdef, 0, (size_t)K * BRICK_PTS * 3 * sizeof(S), s));
+  }
+  CUDA_TRY(cudaMemsetAsync(ex->plist_n, 0, sizeof(unsigned), s));
+  {
+    KernelTimer kt(ex, K_ACTIVE_PTILES, s);
+    active_ptiles_kernel<<<stride_ctas(g.nptiles(), ex->sms * 8), 256, 0, s>>>(g, tile_flags(seg, g), ex->plist,
+                                                                               ex->plist_n);
+  }
+  CUDA_TRY(cudaGetLastError());
+  const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  {
+    KernelTimer kt(ex, K_FUSED_BWD, s);
+    if (ex->method == DISO_MC)
+      brick_backward_kernel<S, MC><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gval, (S*)gdef, ex->stats);
+    else
+      brick_backward_kernel<S, DMC><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gval, (S*)gdef, ex->stats);
+  }
+  CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }
 
@@ -1801,6 +1920,64 @@ int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, in
   else
     field_materialize_kernel<double><<<blocks, 256, 0, s>>>(make_sphere_field<double>(field, nx, ny, nz, 0.0, 1.0),
                                                            (double*)sdf);
+  CUDA_TRY(cudaGetLastError());
+  return DISO_OK;
+}
+
+int diso_forward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
+                        uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                        void* stream, diso_counts* out) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  int rc = check_bricks(bricks);
+  if (rc) return rc;
+  if (!seg || !out) return fail(DISO_ERR_ARG, "null seg or counts");
+  if (vcap < 0 || fcap < 0 || (vcap && !verts) || (fcap && !faces)) return fail(DISO_ERR_ARG, "bad output buffers");
+  if ((rc = bind_device(ex)) != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ex->dtype == DISO_F32) {
+    if ((rc = validate_bricks<float>(ex, bricks, isovalue, padval, s)) != DISO_OK) return rc;
+    return forward_field<float>(ex, make_brick_field<float>(bricks, isovalue, padval), isovalue, seg, normalize,
+                                verts, vcap, faces, fcap, s, out);
+  }
+  if ((rc = validate_bricks<double>(ex, bricks, isovalue, padval, s)) != DISO_OK) return rc;
+  return forward_field<double>(ex, make_brick_field<double>(bricks, isovalue, padval), isovalue, seg, normalize,
+                               verts, vcap, faces, fcap, s, out);
+}
+
+int diso_backward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
+                         const uint64_t* seg, int normalize, int flags, const void* grad_verts, void* grad_values,
+                         void* grad_deform, void* stream) {
+  if (!ex) return fail(DISO_ERR_ARG, "null extractor");
+  int rc = check_bricks(bricks);
+  if (rc) return rc;
+  if (!seg || !grad_verts) return fail(DISO_ERR_ARG, "null seg or grad_verts");
+  if (bricks->count && !grad_values) return fail(DISO_ERR_ARG, "null grad_values");
+  if (bricks->deform && !grad_deform) return fail(DISO_ERR_ARG, "a band with a deform needs grad_deform");
+  if ((rc = bind_device(ex)) != DISO_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  void* gd = bricks->deform ? grad_deform : nullptr;
+  return ex->dtype == DISO_F32
+             ? backward_bricks<float>(ex, make_brick_field<float>(bricks, isovalue, padval), bricks->count, seg,
+                                      normalize, flags, grad_verts, grad_values, gd, s)
+             : backward_bricks<double>(ex, make_brick_field<double>(bricks, isovalue, padval), bricks->count, seg,
+                                       normalize, flags, grad_verts, grad_values, gd, s);
+}
+
+int diso_bricks_materialize(int dtype, const diso_brick_grid* bricks, void* sdf, void* deform, void* stream) {
+  if (dtype != DISO_F32 && dtype != DISO_F64) return fail(DISO_ERR_ARG, "unknown dtype %d", dtype);
+  int rc = check_bricks(bricks);
+  if (rc) return rc;
+  if (!sdf) return fail(DISO_ERR_ARG, "null output grid");
+  if (deform && !bricks->deform) return fail(DISO_ERR_ARG, "a dense deform asked of a band without one");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = (int64_t)bricks->dims[0] * bricks->dims[1] * bricks->dims[2];
+  const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 65536);
+  if (dtype == DISO_F32)
+    bricks_materialize_kernel<float><<<blocks, 256, 0, s>>>(make_brick_field<float>(bricks, 0.0, 1.0), (float*)sdf,
+                                                            (float*)deform);
+  else
+    bricks_materialize_kernel<double><<<blocks, 256, 0, s>>>(make_brick_field<double>(bricks, 0.0, 1.0),
+                                                             (double*)sdf, (double*)deform);
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;
 }

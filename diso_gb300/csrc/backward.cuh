@@ -535,15 +535,26 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
     const int X = X0 + 1 + ix, Y = Y0 + 1 + warp, Z = Z0 + 1 + lane;
     const bool in = f.inside(X, Y, Z);
     const int64_t i = ((int64_t)(X - 1) * f.n1 + (Y - 1)) * f.n2 + (Z - 1);
-    if (in) {
-      if constexpr (F::kDense) gsdf[i] = acc[0];
+    if constexpr (F::kGrad == 2) {
+      // a narrow band: the point's slot in the bricks (none in an absent brick)
+      const int64_t b = in ? f.slot_point(X - 1, Y - 1, Z - 1) : -1;
+      if (b >= 0) {
+        gsdf[b] = acc[0];
+        if (gdef) {
+          gdef[3 * b + 0] = acc[1];
+          gdef[3 * b + 1] = acc[2];
+          gdef[3 * b + 2] = acc[3];
+        }
+      }
+    } else if (in) {
+      if constexpr (F::kGrad == 0) gsdf[i] = acc[0];
       if (gdef) {
         gdef[3 * i + 0] = acc[1];
         gdef[3 * i + 1] = acc[2];
         gdef[3 * i + 2] = acc[3];
       }
     }
-    if constexpr (!F::kDense) field_param_add<S>(f, part, in && acc[0] != S(0), X - 1, Y - 1, Z - 1, acc[0]);
+    if constexpr (F::kGrad == 1) field_param_add<S>(f, part, in && acc[0] != S(0), X - 1, Y - 1, Z - 1, acc[0]);
   }
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
@@ -647,6 +658,32 @@ __global__ void __launch_bounds__(NTHREADS, 3)
     for (; col < ncol; col += gridDim.x) zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
     bulk_wait_all();  // the copies read shared memory: the CTA stays until they have
   }
+  if (bad) atomicOr(&stats->error, 8ull);
+}
+
+// The backward of a narrow band (diso_backward_bricks): as fused_backward_kernel
+// over the active point tiles in list[0 .. *count), the point gradients written to
+// the bricks' slots (gval [K][512], gdef [K][512][3] or null; the caller zeroed them,
+// points of tiles with no crossing nearby keep the zeros).
+template <class S, int METHOD>
+__global__ void __launch_bounds__(NTHREADS, 3)
+    brick_backward_kernel(BrickField<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
+                          const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
+                          S* __restrict__ gval, S* __restrict__ gdef, Stats* stats) {
+  extern __shared__ __align__(16) unsigned char fb_smem[];
+  FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
+  const uint64_t tot = seg[g.nseg];
+  const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
+  S scale[3];
+  grad_scale<S>(g, normalize, scale);
+  if constexpr (METHOD == DMC) sh.cases[threadIdx.x & 255] = dmc_case(threadIdx.x & 255);
+  if (threadIdx.x < 24) sh.edge_of[threadIdx.x] = __ldg(g_edge_of + threadIdx.x);
+  __syncthreads();
+  const unsigned n = *count;
+  bool bad = false;
+#pragma unroll 1
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
+    fused_tile<S, METHOD, BrickField<S>>(sh, f, g, seg, list[i], gv, V, scale, exact, gval, gdef, bad);
   if (bad) atomicOr(&stats->error, 8ull);
 }
 

@@ -66,6 +66,7 @@ struct Geom {
 template <class S>
 struct Field {
   static constexpr bool kDense = true;  // a grid in memory (fields.cuh has evaluated ones)
+  static constexpr int kGrad = 0;       // the backward writes dense dL/dsdf (fields.cuh: 1 spheres, 2 bricks)
   const S* __restrict__ sdf;
   const S* __restrict__ def;  // [N0][N1][N2][3] or null
   int n0, n1, n2;

@@ -17,6 +17,7 @@ namespace diso {
 template <class S>
 struct SphereField {
   static constexpr bool kDense = false;
+  static constexpr int kGrad = 1;  // point gradients go to the spheres' parameters
   const S* __restrict__ sph;  // [K][4]: centre x, y, z, radius
   const S* __restrict__ def;  // [N0][N1][N2][3] or null: the deform, a dense input as for Field
   int K;
@@ -153,6 +154,184 @@ struct SphereField {
     return -1;
   }
 };
+
+// ------------------------------------------------------------------ narrow band
+
+constexpr int BRICK = 8;                          // points per brick edge
+constexpr int BRICK_PTS = BRICK * BRICK * BRICK;  // 512
+constexpr int BRICK_OUT = -1, BRICK_IN = -2;      // index entries of absent bricks
+
+// A narrow band: the grid's values only in the 8^3-point bricks near the surface.
+// index[bx][by][bz] (ceil(n / 8) bricks per axis) is the brick's slot in
+// val [K][8][8][8] (z fastest), or BRICK_OUT / BRICK_IN for an absent brick, whose
+// points read +bg / -bg.  Its values are those of the dense grid with those numbers
+// in the absent bricks (bricks_materialize_kernel writes it), and so are its meshes.
+// The deform, when given, is [K][8][8][8][3] (zero in absent bricks).  The backward's
+// point gradients go to the slots' points (kGrad 2), none to absent points.
+template <class S>
+struct BrickField {
+  static constexpr bool kDense = false;
+  static constexpr int kGrad = 2;
+  const int* __restrict__ index;
+  const S* __restrict__ val;
+  const S* __restrict__ def;
+  int nb1, nb2;  // bricks along y and z
+  int K;         // slots; an entry at or above K reads as absent (the forward rejects it)
+  int n0, n1, n2;
+  S iso, pad, bg;
+
+  __device__ __forceinline__ int entry(int x, int y, int z) const {
+    const int e = __ldg(index + ((int64_t)(x >> 3) * nb1 + (y >> 3)) * nb2 + (z >> 3));
+    return e < K ? e : BRICK_OUT;
+  }
+  __device__ __forceinline__ static int local(int x, int y, int z) {
+    return ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+  }
+  // position of unpadded point (x, y, z) in the slot arrays, -1 in an absent brick
+  __device__ __forceinline__ int64_t slot_point(int x, int y, int z) const {
+    const int e = entry(x, y, z);
+    return e >= 0 ? (int64_t)e * BRICK_PTS + local(x, y, z) : -1;
+  }
+  __device__ __forceinline__ S value(int x, int y, int z) const {
+    const int e = entry(x, y, z);
+    if (e >= 0) return __ldg(val + (int64_t)e * BRICK_PTS + local(x, y, z));
+    return e == BRICK_IN ? -bg : bg;
+  }
+  __device__ __forceinline__ bool inside(int X, int Y, int Z) const {
+    return (unsigned)(X - 1) < (unsigned)n0 && (unsigned)(Y - 1) < (unsigned)n1 && (unsigned)(Z - 1) < (unsigned)n2;
+  }
+  __device__ __forceinline__ S at(int X, int Y, int Z) const { return inside(X, Y, Z) ? value(X - 1, Y - 1, Z - 1) : pad; }
+  __device__ __forceinline__ S point(int64_t, int x, int y, int z) const { return value(x, y, z); }
+  __device__ __forceinline__ S value_of(int x, int y, int z, uint64_t, bool) const { return value(x, y, z); }
+  __device__ __forceinline__ void deform(int X, int Y, int Z, S d[3]) const {
+    d[0] = d[1] = d[2] = S(0);
+    if (def && inside(X, Y, Z)) {
+      const int64_t p = slot_point(X - 1, Y - 1, Z - 1);
+      if (p >= 0) {
+        d[0] = __ldg(def + 3 * p);
+        d[1] = __ldg(def + 3 * p + 1);
+        d[2] = __ldg(def + 3 * p + 2);
+      }
+    }
+  }
+
+  // As SphereField::classify_warp, from the index entries of the bricks that the box
+  // [x0, x1] x [y0, y1] x [z0, z1] (unpadded, in the grid) touches: -1 when one is
+  // present (the box is evaluated), else the class of the absent bricks' values
+  // (+bg, -bg) when they agree, with `bound` the value farthest from iso on that side.
+  // Every lane of the calling warp takes part.
+  __device__ __forceinline__ int classify_warp(int x0, int x1, int y0, int y1, int z0, int z1, bool pads, S& bound,
+                                               uint64_t& cand, bool& all) const {
+    const int lane = threadIdx.x & 31;
+    cand = 0;
+    all = true;
+    if (x0 > x1 || y0 > y1 || z0 > z1) return 1;  // only pad points
+    const int bx0 = x0 >> 3, by0 = y0 >> 3, bz0 = z0 >> 3;
+    const int nx = (x1 >> 3) - bx0 + 1, ny = (y1 >> 3) - by0 + 1, nz = (z1 >> 3) - bz0 + 1;
+    bool present = false, in = false, out = false;
+    for (int k = lane; k < nx * ny * nz; k += 32) {
+      const int bz = bz0 + k % nz, r = k / nz;
+      const int e = __ldg(index + ((int64_t)(bx0 + r / ny) * nb1 + (by0 + r % ny)) * nb2 + bz);
+      present = present || e >= 0;
+      in = in || e == BRICK_IN;
+      out = out || (e < 0 && e != BRICK_IN);
+    }
+    if (__any_sync(0xffffffffu, present)) return -1;
+    in = __any_sync(0xffffffffu, in);
+    out = __any_sync(0xffffffffu, out);
+    const bool out_hi = bg >= iso, in_hi = -bg >= iso;
+    const bool above = (out && out_hi) || (in && in_hi), below = (out && !out_hi) || (in && !in_hi);
+    if (above && below) return -1;
+    if (above) {
+      bound = out ? bg : -bg;
+      return 1;
+    }
+    if (pads) return -1;  // pad points (>= iso) beside values below it
+    bound = in ? -bg : bg;
+    return 0;
+  }
+};
+
+// Checks of a brick index before a forward (one pass over the entries): bit 0 of
+// out[0] for an entry that is neither a slot in [0, K) nor an absent tag, bit 1 for a
+// slot used twice (uses[K], zeroed by the caller, counts them); out[1] += present
+// bricks; out[2] += absent bricks with a 26-neighbour of the other class (value at or
+// above iso / below it: an absent brick of the other tag, or the pad beyond the grid's
+// edge).  A cell can cross the surface only if a corner lies in a present brick or in
+// such a border brick, and 9^3 cells touch a brick, so 729 (out[1] + out[2]) bounds the
+// non-trivial cells (the host checks it against the 32-bit counts).
+__global__ void __launch_bounds__(256) brick_check_kernel(const int* __restrict__ index, int nb0, int nb1, int nb2,
+                                                          int K, int out_hi, int in_hi, int pad_hi,
+                                                          int* __restrict__ uses,
+                                                          unsigned long long* __restrict__ out) {
+  const int64_t n = (int64_t)nb0 * nb1 * nb2;
+  unsigned long long present = 0, border = 0;
+  unsigned bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int e = index[i];
+    if (e >= 0) {
+      if (e >= K) {
+        bad |= 1u;
+      } else {
+        if (atomicAdd(uses + e, 1) != 0) bad |= 2u;
+        ++present;
+      }
+      continue;
+    }
+    if (e != BRICK_OUT && e != BRICK_IN) {
+      bad |= 1u;
+      continue;
+    }
+    const int hi = e == BRICK_IN ? in_hi : out_hi;
+    const int bz = (int)(i % nb2);
+    const int64_t r = i / nb2;
+    const int by = (int)(r % nb1), bx = (int)(r / nb1);
+    bool edge = false;
+    for (int d = 0; d < 27 && !edge; ++d) {
+      const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+      const int x = bx + dx, y = by + dy, z = bz + dz;
+      if (x < 0 || y < 0 || z < 0 || x >= nb0 || y >= nb1 || z >= nb2) {
+        edge = pad_hi != hi;
+      } else {
+        const int f = index[((int64_t)x * nb1 + y) * nb2 + z];
+        if (f < 0) edge = (f == BRICK_IN ? in_hi : out_hi) != hi;
+      }
+    }
+    border += edge ? 1 : 0;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    present += __shfl_xor_sync(0xffffffffu, present, o);
+    border += __shfl_xor_sync(0xffffffffu, border, o);
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicOr(out, (unsigned long long)bad);
+    if (present) atomicAdd(out + 1, present);
+    if (border) atomicAdd(out + 2, border);
+  }
+}
+
+// the dense grid [n0][n1][n2] of a narrow band (and its dense deform, zero in absent
+// bricks, when both are given)
+template <class S>
+__global__ void __launch_bounds__(256) bricks_materialize_kernel(BrickField<S> f, S* __restrict__ out,
+                                                                 S* __restrict__ dout) {
+  const int64_t n = (int64_t)f.n0 * f.n1 * f.n2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(i % f.n2);
+    const int64_t r = i / f.n2;
+    const int x = (int)(r / f.n1), y = (int)(r % f.n1);
+    out[i] = f.value(x, y, z);
+    if (dout) {
+      S d[3];
+      f.deform(x + 1, y + 1, z + 1, d);
+      dout[3 * i] = d[0];
+      dout[3 * i + 1] = d[1];
+      dout[3 * i + 2] = d[2];
+    }
+  }
+}
 
 // the dense grid of a field (for callers that want it, and for checking the
 // fused path against the dense one on the same values)

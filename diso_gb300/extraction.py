@@ -229,6 +229,14 @@ class DiffMC(nn.Module):
 
         return extract_field(self._ex, field, shape, isovalue, normalize, deform=deform)
 
+    def forward_bricks(self, grid, isovalue=0.0, normalize=True):
+        """The mesh of a narrow band (diso_gb300.bricks.BrickGrid): that of its dense
+        grid, without the dense grid in memory; differentiable with respect to
+        grid.values and grid.deform."""
+        from .bricks import extract_bricks
+
+        return extract_bricks(self._ex, grid, isovalue, normalize)
+
 
 class DiffDMC(nn.Module):
     """Differentiable dual marching cubes (diso/__init__.py:63-147).
@@ -255,3 +263,9 @@ class DiffDMC(nn.Module):
         from .fields import extract_field
 
         return extract_field(self._ex, field, shape, isovalue, normalize, return_quads, deform, self.exact_grad)
+
+    def forward_bricks(self, grid, isovalue=0.0, return_quads=False, normalize=True):
+        """The mesh of a narrow band (diso_gb300.bricks.BrickGrid), as DiffMC.forward_bricks."""
+        from .bricks import extract_bricks
+
+        return extract_bricks(self._ex, grid, isovalue, normalize, return_quads, self.exact_grad)

@@ -330,6 +330,54 @@ int diso_backward_field(diso_extractor* ex, const diso_sphere_field* field, int 
 int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, int ny, int nz, void* sdf,
                            void* stream);
 
+/* ---- Narrow-band input ----
+ * A grid whose values are stored only in 8 x 8 x 8-point bricks near the surface, for
+ * grids whose dense arrays (and the dense path's 32-bit limit of about 890^3 points)
+ * are out of reach.  index [ceil(nx/8)][ceil(ny/8)][ceil(nz/8)] (int32, device)
+ * holds each brick's slot in values [count][8][8][8] (the dtype, z fastest), or
+ * DISO_BRICK_OUTSIDE / DISO_BRICK_INSIDE for an absent brick, whose points read
+ * +background / -background.  The band's meshes are exactly those of the dense grid
+ * with those values in the absent bricks (diso_bricks_materialize writes it): the same
+ * vertices, faces and order.  The deform, when given, is [count][8][8][8][3] (zero in
+ * absent bricks).  The reference takes only dense [N, N, N] grids
+ * (diso/__init__.py:48, 102); no counterpart in its library. */
+#define DISO_BRICK_OUTSIDE (-1)
+#define DISO_BRICK_INSIDE (-2)
+typedef struct diso_brick_grid {
+  int dims[3];          /* nx, ny, nz: points per axis of the grid the band lies in */
+  const int32_t* index; /* [ceil(nx/8)][ceil(ny/8)][ceil(nz/8)] */
+  int count;            /* slots */
+  const void* values;   /* [count][8][8][8] in the extractor's dtype */
+  const void* deform;   /* [count][8][8][8][3] in the dtype, or NULL */
+  double background;    /* > 0 */
+} diso_brick_grid;
+
+/* As diso_forward_field for a narrow band (count, scan and emit in one call into
+ * outputs of capacities vcap / fcap; counts->emitted says whether they fitted).  A
+ * first pass checks the index (synchronising the stream): an entry that is neither a
+ * slot in [0, count) nor an absent tag, a slot used twice, or a band whose present
+ * bricks and absent bricks beside an absent brick of the other side (or the grid's
+ * edge) allow more crossings than the 32-bit counts hold is DISO_ERR_ARG.  The count
+ * classifies chunks whose bricks are all absent from the index alone.  The `seg`
+ * record has the dense grid's size (8 bytes per 32-cell row segment); DMC also keeps
+ * the dense cell records in the extractor's scratch (2 bytes per cell). */
+int diso_forward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
+                        uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
+                        void* stream, diso_counts* counts);
+
+/* Backward of diso_forward_bricks (its `seg`; the band unchanged since): from
+ * dL/dverts [n_verts][3], dL/dvalues [count][8][8][8] and, for a band with a deform,
+ * dL/ddeform [count][8][8][8][3], every element written (zero where no crossing edge
+ * ends), flags as for diso_backward.  Equal to the dense backward's gradients at the
+ * bricks' points; absent points have none. */
+int diso_backward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
+                         const uint64_t* seg, int normalize, int flags, const void* grad_verts, void* grad_values,
+                         void* grad_deform, void* stream);
+
+/* The band's dense grid [nx][ny][nz] and, when `deform` is not NULL (the band has a
+ * deform), its dense deform [nx][ny][nz][3]. */
+int diso_bricks_materialize(int dtype, const diso_brick_grid* bricks, void* sdf, void* deform, void* stream);
+
 /* ---- Mesh consumers on the device ----
  * For the meshes the extractor returns: vertices [n_verts][3] in the extractor's
  * dtype, faces [n_faces][corners] int64 (corners 3 or 4).  Each call runs on
