@@ -347,6 +347,132 @@ def run_field(device, n=512, steps=10, warmup=3):
             "dense_ms": ms_d, "fused_ms": ms_f, "speedup": ms_d / ms_f}
 
 
+def sphere_band(n, device, dtype=torch.float32, seed=SEED, halo=12.0, deform=True):
+    """The benchmark's 16 spheres (without the noise) as a narrow band at n^3 on
+    [-1, 1]^3, built brick by brick without a dense grid: bricks whose centre lies
+    within `halo` grid steps of the surface are present (the union's distance is
+    1-Lipschitz, so the others, more than their half diagonal from it, lie on one side
+    and are tagged by it); deform U(-0.45, 0.45) at the bricks' points."""
+    from diso_gb300 import BrickGrid
+
+    g = torch.Generator().manual_seed(seed)
+    c = (torch.rand(16, 3, generator=g, dtype=torch.float64) * 1.6 - 0.8).to(device)
+    r = (torch.rand(16, generator=g, dtype=torch.float64) * 0.25 + 0.05).to(device)
+    step = 2.0 / (n - 1)
+    nb = (n + 7) // 8
+
+    def dist(p):  # p [..., 3] float64 -> min_k |p - c_k| - r_k
+        out = None
+        for k in range(16):
+            d = (p - c[k]).norm(dim=-1) - r[k]
+            out = d if out is None else torch.minimum(out, d)
+        return out
+
+    ax = -1.0 + (torch.arange(nb, device=device, dtype=torch.float64) * 8 + 3.5) * step
+    dc = torch.empty((nb, nb, nb), dtype=torch.float64, device=device)
+    for i in range(nb):
+        P = torch.stack(torch.meshgrid(ax[i:i + 1], ax, ax, indexing="ij"), -1)
+        dc[i] = dist(P)[0]
+    present = dc.abs() <= halo * step
+    k = int(present.sum())
+    index = torch.where(dc > 0, -1, -2).to(torch.int32)
+    index[present] = torch.arange(k, dtype=torch.int32, device=device)
+    bricks = torch.nonzero(present)  # slot order: x-major, as the index numbers them
+    lr = torch.arange(8, device=device, dtype=torch.float64)
+    loc = torch.stack(torch.meshgrid(lr, lr, lr, indexing="ij"), -1).reshape(1, 512, 3)
+    values = torch.empty((k, 8, 8, 8), dtype=dtype, device=device)
+    for a in range(0, k, 32768):
+        b = bricks[a:a + 32768].to(torch.float64)
+        P = -1.0 + (b[:, None, :] * 8 + loc) * step
+        values[a:a + 32768] = dist(P).reshape(-1, 8, 8, 8).to(dtype)
+    dfm = None
+    if deform:
+        gg = torch.Generator(device=device).manual_seed(seed + 100)
+        dfm = torch.rand((k, 8, 8, 8, 3), device=device, dtype=dtype, generator=gg) * (2 * DEFORM) - DEFORM
+    return BrickGrid((n, n, n), index, values, dfm, background=1.0)
+
+
+def run_band(device, n=2048, steps=10, warmup=3, dense_n=512):
+    """Narrow-band extraction.  (1) The benchmark's spheres as a band at n^3 (built
+    without a dense grid, sphere_band), DiffDMC forward + backward with quads and deform:
+    its dense grids (SDF, deform and their gradients, 32 B per point) would not fit in
+    HBM at 2048^3.  (2) The headline's own grid at dense_n^3 cut to a band
+    (BrickGrid.from_dense: every brick with an end of a crossing edge), the same step on
+    the band and on the dense grid (recompute backward): the same mesh, and the time of
+    each."""
+    from diso_gb300 import BrickGrid, DiffDMC
+
+    def step_fn(mod, band):
+        v, q = mod.forward_bricks(band, return_quads=True)
+        w = loss_weights(v.shape[0], device, v.dtype)
+        (v * w).sum().backward()
+        return v, q
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, out
+
+    out = {}
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    band = sphere_band(n, device)
+    band.values.requires_grad_(True)
+    band.deform.requires_grad_(True)
+    mod = DiffDMC(torch.float32)
+    band_bytes = sum(t.numel() * t.element_size() for t in (band.index, band.values, band.deform))
+    torch.cuda.reset_peak_memory_stats(device)
+
+    def big():
+        band.values.grad = None
+        band.deform.grad = None
+        return step_fn(mod, band)
+
+    ms, (v, q) = timed(big)
+    out["band"] = {"n": n, "bricks": band.count, "verts": v.shape[0], "quads": q.shape[0], "ms_per_step": ms,
+                   "grids_s": 1e3 / ms, "band_gb": round(band_bytes / 1e9, 3),
+                   "peak_hbm_gb": round(torch.cuda.max_memory_allocated(device) / 1e9, 3),
+                   "extractor_scratch_gb": round(mod._ex.scratch_bytes() / 1e9, 3),
+                   "dense_equivalent_gb": round(n ** 3 * 4 * (1 + 3) * 2 / 1e9, 1)}
+    del band, v, q, mod
+    torch.cuda.empty_cache()
+    # the headline grid as a band
+    sdf = spheres_field(dense_n, device)
+    dfm = deform_field(dense_n, device)
+    cut = BrickGrid.from_dense(sdf, 0.0, deform=dfm)
+    cut.values.requires_grad_(True)
+    cut.deform.requires_grad_(True)
+    mod = DiffDMC(torch.float32, recompute=True)
+    s_req, d_req = sdf.clone().requires_grad_(True), dfm.clone().requires_grad_(True)
+
+    def dense_step():
+        s_req.grad = None
+        d_req.grad = None
+        v, q = mod(s_req, d_req, return_quads=True)
+        (v * loss_weights(v.shape[0], device, v.dtype)).sum().backward()
+        return v, q
+
+    def band_step():
+        cut.values.grad = None
+        cut.deform.grad = None
+        return step_fn(mod, cut)
+
+    ms_d, (vd, qd) = timed(dense_step)
+    ms_b, (vb, qb) = timed(band_step)
+    out["headline_grid_as_band"] = {"n": dense_n, "bricks": cut.count,
+                                    "bricks_share": round(cut.count / ((dense_n + 7) // 8) ** 3, 4),
+                                    "same_mesh": bool(torch.equal(vd, vb) and torch.equal(qd, qb)),
+                                    "dense_ms": ms_d, "band_ms": ms_b}
+    return out
+
+
 def run_served(device, nreq=20000, rate=2000.0, plain_sample=4000):
     """The served stream: p50 / p99 latency and grids/s of the continuous-batching
     server on the Poisson trace in real time, and its capacity (the whole trace
@@ -899,6 +1025,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="the library's default launch widths (for profiling)")
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
+    ap.add_argument("--band-n", type=int, default=2048, help="grid size of the narrow-band measurement")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -937,7 +1064,8 @@ def main():
         for name, fn in (("batched_mc", lambda: run_batched(device, 0)), ("batched_dmc", lambda: run_batched(device, 1)),
                          ("served", lambda: run_served(device, args.requests)),
                          ("mesh_consumers", lambda: run_mesh(device, args.n)),
-                         ("fused_field", lambda: run_field(device, args.n))):
+                         ("fused_field", lambda: run_field(device, args.n)),
+                         ("narrow_band", lambda: run_band(device, args.band_n))):
             try:
                 res[name] = fn()
             except Exception as e:  # report, but keep the headline line

@@ -42,10 +42,11 @@ int fail(int code, const char* fmt, ...) {
 // kernels timed by diso_timing
 enum KernelId {
   K_COUNT, K_SCAN, K_EMIT, K_ZERO_GRADS, K_ZERO_TILES, K_ACTIVE_PTILES, K_EDGE, K_GATHER, K_SPLIT, K_FUSED_BWD,
-  K_NKERNELS
+  K_BRICK_CHECK, K_NKERNELS
 };
 static const char* const kKernelNames[K_NKERNELS] = {"count",       "scan", "emit",   "zero_grads", "zero_tiles",
-                                                      "active_list", "edge", "gather", "split",     "fused_bwd"};
+                                                      "active_list", "edge", "gather", "split",     "fused_bwd",
+                                                      "brick_check"};
 
 struct diso_extractor {
   int method = 0, dtype = 0, device = -1;
@@ -75,6 +76,7 @@ struct diso_extractor {
   // the `seg` and grid of the last dense DMC count, whose cell records `codes` holds
   const uint64_t* codes_seg = nullptr;
   int codes_dims[3] = {0, 0, 0};
+  bool codes_band = false;       // they are a narrow band's (else a dense grid's)
   int resident_ctas = 0;         // count-kernel CTAs that fit on the device at once
   int tma_ctas = 0;              // the same for the TMA count kernel
   int gather_ctas = 0;           // the same for the point gather
@@ -101,6 +103,8 @@ struct diso_extractor {
   cudaStream_t zemit_stream = nullptr;
   bool zemit_set = false;
   cudaEvent_t ev_counts = nullptr;  // the count's results are on the host
+  int* ulist = nullptr;          // an evaluated field's count units that hold the surface (count, then ids)
+  int64_t ulist_cap = 0;
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
   unsigned* plist_n = nullptr;
@@ -184,6 +188,9 @@ struct diso_extractor {
     cudaFree(buses);
     buses = nullptr;
     buses_cap = 0;
+    cudaFree(ulist);
+    ulist = nullptr;
+    ulist_cap = 0;
     cudaFree(bcheck);
     bcheck = nullptr;
     bcheck_cap = 0;
@@ -375,14 +382,19 @@ int bind_device(diso_extractor* ex) {
     ex->per_sm[3] = std::max(per_f, 1);
     // the narrow band's backward: the fused tile with the same shared memory
     const void* bk = ex->dtype == DISO_F32
-                         ? (ex->method == DISO_MC ? (const void*)brick_backward_kernel<float, MC>
-                                                  : (const void*)brick_backward_kernel<float, DMC>)
-                         : (ex->method == DISO_MC ? (const void*)brick_backward_kernel<double, MC>
-                                                  : (const void*)brick_backward_kernel<double, DMC>);
+                         ? (ex->method == DISO_MC ? (const void*)brick_backward_kernel<float, MC, false>
+                                                  : (const void*)brick_backward_kernel<float, DMC, false>)
+                         : (ex->method == DISO_MC ? (const void*)brick_backward_kernel<double, MC, false>
+                                                  : (const void*)brick_backward_kernel<double, DMC, false>);
     int per_b = 0;
     CUDA_TRY(cudaFuncSetAttribute(bk, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, bk, NTHREADS, ex->fused_smem));
     ex->brick_ctas = sms * std::max(per_b, 1);
+    if (ex->method == DISO_DMC) {  // the variant that reads the forward's cell records
+      const void* br = ex->dtype == DISO_F32 ? (const void*)brick_backward_kernel<float, DMC, true>
+                                             : (const void*)brick_backward_kernel<double, DMC, true>;
+      CUDA_TRY(cudaFuncSetAttribute(br, cudaFuncAttributeMaxDynamicSharedMemorySize, ex->fused_smem_rec));
+    }
     CUDA_TRY(cudaStreamCreateWithFlags(&ex->side, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&ex->ev_join, cudaEventDisableTiming));
@@ -493,6 +505,7 @@ int count_launch(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, do
   ex->codes_dims[0] = nx;
   ex->codes_dims[1] = ny;
   ex->codes_dims[2] = nz;
+  ex->codes_band = false;
   CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   Field<S> f = make_field<S>(sdf, nullptr, nx, ny, nz, iso, padval);
   // persistent grids: enough CTAs to fill the GPU, and at most COUNT_LIST tiles each
@@ -728,8 +741,8 @@ int backward_fused(diso_extractor* ex, const void* sdf, const void* deform, int 
   // count wrote this `seg` for a grid of these sizes (no other forward ran since);
   // then the fused pass reads the window cells' codes and patch offsets from them
   // instead of running the ambiguity test again
-  const bool records = ex->method == DISO_DMC && ex->codes && ex->codes_seg == seg && ex->codes_dims[0] == nx &&
-                       ex->codes_dims[1] == ny && ex->codes_dims[2] == nz;
+  const bool records = ex->method == DISO_DMC && ex->codes && ex->codes_seg == seg && !ex->codes_band &&
+                       ex->codes_dims[0] == nx && ex->codes_dims[1] == ny && ex->codes_dims[2] == nz;
   if (!zbulk) {
     if ((rc = side_fork(ex, s)) != DISO_OK) return rc;
     KernelTimer kt(ex, K_ZERO_TILES, ex->side);
@@ -1172,21 +1185,35 @@ int forward_field(diso_extractor* ex, const F& f, double iso, uint64_t* seg, int
   if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
   const int64_t scan_tiles = scan_reserve(ex, g.nseg);
   if (scan_tiles == 0) return DISO_ERR_CUDA;
-  ex->codes_seg = nullptr;  // the field's records are not those of a dense grid
+  // a narrow band's records serve its backward (brick_backward_kernel); a sphere
+  // union's backward recomputes its cells
+  ex->codes_seg = F::kGrad == 2 ? seg : nullptr;
+  ex->codes_dims[0] = f.n0;
+  ex->codes_dims[1] = f.n1;
+  ex->codes_dims[2] = f.n2;
+  ex->codes_band = true;
   ex->zpend.set = ex->zemit_set = false;  // gradient zeros belong to a dense forward
   count_prep_kernel<<<1, 256, 0, s>>>(ex->stats, ex->scan_flag, scan_tiles);
   CUDA_TRY(cudaGetLastError());
+  // the count leaves the units that field_units_kernel classifies whole unwritten
+  CUDA_TRY(cudaMemsetAsync(seg, 0, (size_t)(g.nseg + 1 + (2 * g.ntiles() + 7) / 8) * sizeof(uint64_t), s));
   CellRec* codes = ex->method == DISO_DMC ? ex->codes : nullptr;
   {
     const int64_t units = count_units(g);
+    if ((rc = grow(ex->ulist, ex->ulist_cap, units + 1)) != DISO_OK) return rc;
+    CUDA_TRY(cudaMemsetAsync(ex->ulist, 0, sizeof(int), s));
     const int64_t want =
         std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
     KernelTimer kt(ex, K_COUNT, s);
+    field_units_kernel<S, F><<<stride_ctas(units * 32, (unsigned)ex->sms * 16), 256, 0, s>>>(f, g, ex->stats,
+                                                                                              ex->ulist);
     if (ex->method == DISO_MC)
-      count_kernel<S, MC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
+      field_count_kernel<S, MC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
+                                                             ex->active, ex->ulist);
     else
-      count_kernel<S, DMC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats, ex->active);
+      field_count_kernel<S, DMC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
+                                                              ex->active, ex->ulist);
   }
   CUDA_TRY(cudaGetLastError());
   if ((rc = run_scan(ex, seg, g.nseg, s, true, reinterpret_cast<uint64_t*>(&ex->stats->total))) != DISO_OK)
@@ -1298,9 +1325,12 @@ int validate_bricks(diso_extractor* ex, const diso_brick_grid* b, double iso, do
   if (b->count) CUDA_TRY(cudaMemsetAsync(ex->buses, 0, sizeof(int) * (size_t)b->count, s));
   CUDA_TRY(cudaMemsetAsync(ex->bcheck, 0, 4 * sizeof(unsigned long long), s));
   const S bg = (S)b->background, isoS = (S)iso;
-  brick_check_kernel<<<stride_ctas(nb, ex->sms * 8), 256, 0, s>>>(b->index, nb0, nb1, nb2, b->count, bg >= isoS ? 1 : 0,
-                                                                  -bg >= isoS ? 1 : 0, (S)padval >= isoS ? 1 : 0,
-                                                                  ex->buses, ex->bcheck);
+  {
+    KernelTimer kt(ex, K_BRICK_CHECK, s);
+    brick_check_kernel<<<stride_ctas(nb, ex->sms * 8), 256, 0, s>>>(b->index, nb0, nb1, nb2, b->count,
+                                                                    bg >= isoS ? 1 : 0, -bg >= isoS ? 1 : 0,
+                                                                    (S)padval >= isoS ? 1 : 0, ex->buses, ex->bcheck);
+  }
   CUDA_TRY(cudaGetLastError());
   unsigned long long h[4] = {0, 0, 0, 0};
   CUDA_TRY(cudaMemcpyAsync(h, ex->bcheck, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -1338,14 +1368,23 @@ int backward_bricks(diso_extractor* ex, const BrickField<S>& f, int K, const uin
   }
   CUDA_TRY(cudaGetLastError());
   const int exact = (flags & DISO_GRAD_EXACT) ? 1 : 0;
+  // DMC: the cell records of the extractor's last forward are this band's when that
+  // forward wrote this `seg` for a band of these sizes
+  const bool records = ex->method == DISO_DMC && ex->codes && ex->codes_seg == seg && ex->codes_band &&
+                       ex->codes_dims[0] == f.n0 && ex->codes_dims[1] == f.n1 && ex->codes_dims[2] == f.n2;
   {
     KernelTimer kt(ex, K_FUSED_BWD, s);
     if (ex->method == DISO_MC)
-      brick_backward_kernel<S, MC><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
-          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gval, (S*)gdef, ex->stats);
+      brick_backward_kernel<S, MC, false><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, 0, (S*)gval, (S*)gdef, ex->stats, nullptr);
+    else if (records)
+      brick_backward_kernel<S, DMC, true><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem_rec, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gval, (S*)gdef, ex->stats,
+          ex->codes);
     else
-      brick_backward_kernel<S, DMC><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
-          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gval, (S*)gdef, ex->stats);
+      brick_backward_kernel<S, DMC, false><<<(unsigned)ex->brick_ctas, NTHREADS, (size_t)ex->fused_smem, s>>>(
+          f, g, seg, ex->plist, ex->plist_n, (const S*)gv, normalize, exact, (S*)gval, (S*)gdef, ex->stats,
+          nullptr);
   }
   CUDA_TRY(cudaGetLastError());
   return DISO_OK;

@@ -664,14 +664,16 @@ __global__ void __launch_bounds__(NTHREADS, 3)
 // The backward of a narrow band (diso_backward_bricks): as fused_backward_kernel
 // over the active point tiles in list[0 .. *count), the point gradients written to
 // the bricks' slots (gval [K][512], gdef [K][512][3] or null; the caller zeroed them,
-// points of tiles with no crossing nearby keep the zeros).
-template <class S, int METHOD>
+// points of tiles with no crossing nearby keep the zeros).  DMC with REC: the band's
+// forward's cell records (`codes`).
+template <class S, int METHOD, bool REC>
 __global__ void __launch_bounds__(NTHREADS, 3)
     brick_backward_kernel(BrickField<S> f, Geom g, const uint64_t* __restrict__ seg, const int* __restrict__ list,
                           const unsigned* __restrict__ count, const S* __restrict__ gv, int normalize, int exact,
-                          S* __restrict__ gval, S* __restrict__ gdef, Stats* stats) {
+                          S* __restrict__ gval, S* __restrict__ gdef, Stats* stats,
+                          const CellRec* __restrict__ codes) {
   extern __shared__ __align__(16) unsigned char fb_smem[];
-  FusedShared<S, METHOD>& sh = *reinterpret_cast<FusedShared<S, METHOD>*>(fb_smem);
+  FusedShared<S, METHOD, REC>& sh = *reinterpret_cast<FusedShared<S, METHOD, REC>*>(fb_smem);
   const uint64_t tot = seg[g.nseg];
   const int64_t V = METHOD == MC ? (int64_t)Counts::lo(tot) : (int64_t)Counts::hi(tot);
   S scale[3];
@@ -683,7 +685,8 @@ __global__ void __launch_bounds__(NTHREADS, 3)
   bool bad = false;
 #pragma unroll 1
   for (unsigned i = blockIdx.x; i < n; i += gridDim.x)
-    fused_tile<S, METHOD, BrickField<S>>(sh, f, g, seg, list[i], gv, V, scale, exact, gval, gdef, bad);
+    fused_tile<S, METHOD, BrickField<S>, REC>(sh, f, g, seg, list[i], gv, V, scale, exact, gval, gdef, bad, nullptr,
+                                              codes);
   if (bad) atomicOr(&stats->error, 8ull);
 }
 

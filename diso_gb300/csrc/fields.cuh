@@ -228,13 +228,35 @@ struct BrickField {
     if (x0 > x1 || y0 > y1 || z0 > z1) return 1;  // only pad points
     const int bx0 = x0 >> 3, by0 = y0 >> 3, bz0 = z0 >> 3;
     const int nx = (x1 >> 3) - bx0 + 1, ny = (y1 >> 3) - by0 + 1, nz = (z1 >> 3) - bz0 + 1;
+    const int nbk = nx * ny * nz;
     bool present = false, in = false, out = false;
-    for (int k = lane; k < nx * ny * nz; k += 32) {
+    // the boxes of a count unit touch at most 2 x 5 x 18 bricks: six entries per lane,
+    // loaded together (a loop takes any rest)
+    constexpr int PER = 6;
+    int e[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int k = lane + 32 * j;
+      e[j] = BRICK_OUT;
+      if (k < nbk) {
+        const int bz = bz0 + k % nz, r = k / nz;
+        e[j] = __ldg(index + ((int64_t)(bx0 + r / ny) * nb1 + (by0 + r % ny)) * nb2 + bz);
+      }
+    }
+    for (int k = lane + 32 * PER; k < nbk; k += 32) {
       const int bz = bz0 + k % nz, r = k / nz;
-      const int e = __ldg(index + ((int64_t)(bx0 + r / ny) * nb1 + (by0 + r % ny)) * nb2 + bz);
-      present = present || e >= 0;
-      in = in || e == BRICK_IN;
-      out = out || (e < 0 && e != BRICK_IN);
+      const int v = __ldg(index + ((int64_t)(bx0 + r / ny) * nb1 + (by0 + r % ny)) * nb2 + bz);
+      present = present || v >= 0;
+      in = in || v == BRICK_IN;
+      out = out || (v < 0 && v != BRICK_IN);
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      if (lane + 32 * j < nbk) {
+        present = present || e[j] >= 0;
+        in = in || e[j] == BRICK_IN;
+        out = out || (e[j] < 0 && e[j] != BRICK_IN);
+      }
     }
     if (__any_sync(0xffffffffu, present)) return -1;
     in = __any_sync(0xffffffffu, in);
@@ -286,15 +308,18 @@ __global__ void __launch_bounds__(256) brick_check_kernel(const int* __restrict_
     const int bz = (int)(i % nb2);
     const int64_t r = i / nb2;
     const int by = (int)(r % nb1), bx = (int)(r / nb1);
+    // the 26 neighbours' loads issued together
     bool edge = false;
-    for (int d = 0; d < 27 && !edge; ++d) {
+#pragma unroll
+    for (int d = 0; d < 27; ++d) {
       const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+      if (d == 13) continue;
       const int x = bx + dx, y = by + dy, z = bz + dz;
       if (x < 0 || y < 0 || z < 0 || x >= nb0 || y >= nb1 || z >= nb2) {
-        edge = pad_hi != hi;
+        edge = edge || pad_hi != hi;
       } else {
-        const int f = index[((int64_t)x * nb1 + y) * nb2 + z];
-        if (f < 0) edge = (f == BRICK_IN ? in_hi : out_hi) != hi;
+        const int f = __ldg(index + ((int64_t)x * nb1 + y) * nb2 + z);
+        edge = edge || (f < 0 && (f == BRICK_IN ? in_hi : out_hi) != hi);
       }
     }
     border += edge ? 1 : 0;

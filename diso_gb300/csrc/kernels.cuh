@@ -469,23 +469,28 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
       __syncwarp();
       return;
     }
-    // evaluated one row at a time (compute, not loads, is what takes the time)
+    if constexpr (F::kGrad == 1) {
+      // a union of spheres, evaluated one row at a time (compute, not loads, is what
+      // takes the time)
 #pragma unroll 1
-    for (int i = 0; i < CRPW; ++i) {
-      const int r = warp + 8 * i;
-      if (r >= CROWS) break;
-      const bool in = zin && sh.rowoff[r] >= 0;
-      const S v = in ? f.value_of(X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z, cand, all) : f.pad;
-      const uint32_t b = __ballot_sync(0xffffffffu, v >= f.iso);
-      if (lane == 0) sh.bal[r] = b;
-      if (in) {
-        mn = smin(mn, v);
-        mx = smax(mx, v);
+      for (int i = 0; i < CRPW; ++i) {
+        const int r = warp + 8 * i;
+        if (r >= CROWS) break;
+        const bool in = zin && sh.rowoff[r] >= 0;
+        const S v = in ? f.value_of(X0 + r / (CR + 1) - 1, Y0 + r % (CR + 1) - 1, z, cand, all) : f.pad;
+        const uint32_t b = __ballot_sync(0xffffffffu, v >= f.iso);
+        if (lane == 0) sh.bal[r] = b;
+        if (in) {
+          mn = smin(mn, v);
+          mx = smax(mx, v);
+        }
       }
+      __syncwarp();
+      return;
     }
-    __syncwarp();
-    return;
-  } else {
+  }
+  {
+    // a grid in memory, or a narrow band's chunk that holds bricks: loads in batches
 #pragma unroll
     for (int h = 0; h < NB; ++h) {
       S v[HALF];
@@ -747,6 +752,59 @@ __global__ void __launch_bounds__(NTHREADS, F::kDense ? 3 : 2) count_kernel(F f,
 #pragma unroll 1
   for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x)
     count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, u, 0, ck);
+  count_flush<S, METHOD>(sh, &stats->n_active, active);
+}
+
+// ------------------------------------------------------------------ evaluated fields
+
+// The units of an evaluated field's count that may hold both sides of iso: one warp
+// per unit classifies the unit's box (every point its chunks' masks read; pads: part
+// of it lies outside the grid); a unit wholly on one side publishes its bound and is
+// left out (its record stays as the host zeroed it), the others are appended to
+// units[1 ..] (units[0] counts them) for field_count_kernel.
+template <class S, class F>
+__global__ void __launch_bounds__(256) field_units_kernel(F f, Geom g, Stats* stats, int* __restrict__ units) {
+  const int lane = threadIdx.x & 31;
+  const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
+  const int64_t nunits = count_units(g), step = ((int64_t)gridDim.x * blockDim.x) >> 5;
+#pragma unroll 1
+  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += step) {
+    const int tz0 = (int)(u % nbz) * kz, tz1 = min(tz0 + kz, g.nzc);
+    const int64_t col = u / nbz;
+    const int X0 = (int)(col / nby) * CP, Y0 = (int)(col % nby) * CR;
+    const int xa = max(X0 - 1, 0), xb = min(X0 + CP - 1, f.n0 - 1);
+    const int ya = max(Y0 - 1, 0), yb = min(Y0 + CR - 1, f.n1 - 1);
+    const int za = max(32 * tz0 - 2, 0), zb = min(32 * tz1, f.n2 - 1);
+    const bool pads = X0 - 1 < 0 || X0 + CP - 1 >= f.n0 || Y0 - 1 < 0 || Y0 + CR - 1 >= f.n1 || 32 * tz0 - 2 < 0 ||
+                      32 * tz1 >= f.n2;
+    S bound = S(0);
+    uint64_t cand = 0;
+    bool all = true;
+    if (f.classify_warp(xa, xb, ya, yb, za, zb, pads, bound, cand, all) >= 0) {
+      if (xa <= xb && ya <= yb && za <= zb) publish_minmax<S>(stats, bound, bound);
+    } else if (lane == 0) {
+      units[1 + atomicAdd(units, 1)] = (int)u;
+    }
+  }
+}
+
+// count_kernel over the units that field_units_kernel listed
+template <class S, int METHOD, class F>
+__global__ void __launch_bounds__(NTHREADS, 2) field_count_kernel(F f, Geom g, uint64_t* __restrict__ seg,
+                                                                  uint8_t* __restrict__ tile_flag,
+                                                                  CellRec* __restrict__ codes, Stats* stats,
+                                                                  int* __restrict__ active,
+                                                                  const int* __restrict__ units) {
+  __shared__ CountShared<S, METHOD> sh;
+  if (threadIdx.x == 0) {
+    sh.nlist = 0;
+    sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
+  }
+  const int n = units[0];
+  int64_t ck = 0;
+#pragma unroll 1
+  for (int i = blockIdx.x; i < n; i += gridDim.x)
+    count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, units[1 + i], 0, ck);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
 }
 
