@@ -436,7 +436,15 @@ def run_band(device, n=2048, steps=10, warmup=3, dense_n=512):
         return step_fn(mod, band)
 
     ms, (v, q) = timed(big)
+    # per-kernel times of the same step (CUDA events around every launch)
+    mod._ex.timing(True)
+    for _ in range(steps):
+        big()
+    torch.cuda.synchronize()
+    kern = {k: round(t / steps, 4) for k, (c, t) in mod._ex.timing_read().items()}
+    mod._ex.timing(False)
     out["band"] = {"n": n, "bricks": band.count, "verts": v.shape[0], "quads": q.shape[0], "ms_per_step": ms,
+                   "kernel_ms_per_step": kern,
                    "grids_s": 1e3 / ms, "band_gb": round(band_bytes / 1e9, 3),
                    "peak_hbm_gb": round(torch.cuda.max_memory_allocated(device) / 1e9, 3),
                    "extractor_scratch_gb": round(mod._ex.scratch_bytes() / 1e9, 3),
@@ -1026,6 +1034,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     ap.add_argument("--band-n", type=int, default=2048, help="grid size of the narrow-band measurement")
+    ap.add_argument("--only", choices=["narrow_band", "fused_field", "mesh_consumers"],
+                    help="run one side measurement alone and print it (for profiling)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1053,6 +1063,13 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
+    if args.only:
+        device = torch.device("cuda", torch.cuda.current_device())
+        fn = {"narrow_band": lambda: run_band(device, args.band_n, steps=args.steps, warmup=args.warmup),
+              "fused_field": lambda: run_field(device, args.n, steps=args.steps, warmup=args.warmup),
+              "mesh_consumers": lambda: run_mesh(device, args.n, steps=args.steps, warmup=args.warmup)}[args.only]
+        print(json.dumps({args.only: fn()}), flush=True)
+        return
     if world > 1:
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
