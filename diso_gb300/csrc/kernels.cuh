@@ -489,7 +489,7 @@ __device__ __forceinline__ void count_ballots(CountShared<S, METHOD>& sh, const 
       return;
     }
   }
-  {
+  if constexpr (F::kGrad != 1) {
     // a grid in memory, or a narrow band's chunk that holds bricks: loads in batches
 #pragma unroll
     for (int h = 0; h < NB; ++h) {
