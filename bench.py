@@ -184,9 +184,44 @@ def served_trace(nreq=2000, rate=2000.0, seed=3, pool=None):
             make = (lambda n_, k_, v_: (lambda dev: pool.get(n_, k_, v_)))(n, kind, rs % pool.variants)
         else:
             make = request_inputs(rs, shape, kind)
-        out.append(Request(rid=i, method=method, shape=shape, arrival=t, make_inputs=make,
-                           est_bytes=estimate_bytes(shape, dense=kind == "random")))
+        req = Request(rid=i, method=method, shape=shape, arrival=t, make_inputs=make,
+                      est_bytes=estimate_bytes(shape, dense=kind == "random"))
+        req.kind = kind
+        out.append(req)
     return out
+
+
+def device_bound(trace, pool, device, reps=3):
+    """grids/s of the trace if the GPU did nothing but the requests' kernels: per
+    (N, kind, method) the extractor's kernel time of one request (CUDA events around
+    every launch, the plain per-request call), summed over the trace.  No scheduler
+    can serve the trace faster than this."""
+    from diso_gb300 import _native as N
+    from diso_gb300.extraction import extract
+
+    ex = {m: N.Extractor(m, torch.float32) for m in (N.MC, N.DMC)}
+    per = {}
+    for key in sorted({(r.shape[0], r.kind, r.method) for r in trace}):
+        n, kind, m = key
+        e = ex[m]
+
+        def one():
+            sdf, dfm, grad = pool.get(n, kind, 0)
+            sdf.requires_grad_(True)
+            dfm.requires_grad_(True)
+            v, _ = extract(e, sdf, dfm, 0.0, True, True)
+            torch.autograd.backward(v, grad(v.shape[0]))
+
+        one()
+        torch.cuda.synchronize()
+        e.timing(True)
+        for _ in range(reps):
+            one()
+        torch.cuda.synchronize()
+        per[key] = sum(ms for _, ms in e.timing_read().values()) / reps
+        e.timing(False)
+    total_ms = sum(per[(r.shape[0], r.kind, r.method)] for r in trace)
+    return len(trace) / (total_ms * 1e-3), per
 
 
 def run_batched(device, method, steps=10, warmup=3, ngrids=64):
@@ -506,8 +541,12 @@ def run_served(device, nreq=20000, rate=2000.0, plain_sample=4000):
     plain_trace = served_trace(nreq, rate, pool=pool)[:plain_sample]
     serve_plain(plain_trace, device, realtime=False)
     plain = {k: v for k, v in summarize(plain_trace, t_first=0.0).items() if not k.startswith("p")}
+    bound, per = device_bound(trace, pool, device)
+    heavy = sorted(per.items(), key=lambda kv: -kv[1])[:3]
     return {"requests": nreq, "rate_per_s": rate, "server_realtime": realtime, "server_capacity": capacity,
             "plain_per_request_capacity": plain, "plain_sample": plain_sample,
+            "device_bound_grids_s": bound,
+            "device_ms_heaviest": {f"{n}^3 {k} {'mc' if m == 0 else 'dmc'}": round(v, 3) for (n, k, m), v in heavy},
             "grids_s_speedup": capacity["grids_per_s"] / plain["grids_per_s"], "peak_budget_gb": peak / 1e9,
             "inputs": "device-resident pool: 4 grids per (N, kind), one N(0,1) gradient buffer",
             "workers": 4, "max_batch": 64}
@@ -793,7 +832,7 @@ def run_ours(args, rank, world, device):
 
     # the same workload with the forward's edge record and gradient buffers kept for
     # the backward (stored mode), for comparison
-    stored = DiffDMC(torch.float32)
+    stored = DiffDMC(torch.float32, recompute=False)
     tuned_st = tune.tune_module(stored, (n, n, n), retune=args.retune) if not args.no_tune else {"params": {}}
     ms_st, k_st, ph_st, _ = time_steps(stored, s, d, w, args.steps, args.warmup, world)
     mem_st = peak_memory(stored, s, d, w)

@@ -19,12 +19,16 @@ Differences that are invisible to callers of the reference API:
 * an isovalue given as a tensor that requires grad gets dL/d(isovalue), minus
   the sum of dL/dsdf (the reference's isovalue is a plain scalar).
 
-With recompute=True the forward keeps nothing for the backward but the inputs
-and its segment record (the scanned output counts per 32-cell row segment, 8
-bytes per 32 cells): no edge record and no gradient buffers.  The backward
-recomputes the crossings, the DMC cell codes and patch ids and every edge's
-adjoint per point tile in one pass that writes each gradient element once
-(diso_backward_recompute); the gradients are the stored mode's bit for bit.
+By default (recompute=True, as the reference, which re-runs its forward in its
+backward, diso/__init__.py:32, 86) the forward keeps nothing for the backward but
+the inputs and its segment record (the scanned output counts per 32-cell row
+segment, 8 bytes per 32 cells): no edge record and no gradient buffers.  The
+backward recomputes the crossings, the DMC cell codes and patch ids and every
+edge's adjoint per point tile in one pass that writes each gradient element once
+(diso_backward_recompute).  recompute=False keeps the edge record and the zeroed
+gradient buffers from the forward instead (a faster backward for 2.4 GB more
+device memory between the two at 512^3 with deform); the gradients are the same
+bit for bit.
 
 The outputs are the reference's: the same vertex, face and quad order, the same
 dtypes, including the int32 empty faces of the guard.
@@ -132,15 +136,15 @@ def _capacity(n):
 
 
 def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, return_quads=False,
-            exact_grad=False, recompute=False):
+            exact_grad=False, recompute=True):
     """One differentiable extraction with the reference's semantics.
 
     An isovalue given as a tensor that requires grad (a one-element tensor, not in
     the reference) receives dL/d(isovalue) in the backward.
 
-    recompute=True keeps no edge record and no gradient buffers between the
-    forward and the backward, only the segment record; the backward recomputes
-    the crossing lists per point tile.
+    recompute=True (the default) keeps no edge record and no gradient buffers
+    between the forward and the backward, only the segment record; the backward
+    recomputes the crossing lists per point tile.  recompute=False keeps them.
 
     exact_grad (DMC only) replaces the reference's backward in cells with several
     patches, where every patch receives the first patch's gradient
@@ -208,11 +212,12 @@ def extract(ex: N.Extractor, grid, deform=None, isovalue=0.0, normalize=True, re
 class DiffMC(nn.Module):
     """Differentiable marching cubes (diso/__init__.py:9-61).
 
-    ``recompute=True`` (keyword only, not in the reference) keeps nothing between
-    the forward and the backward but the inputs and the segment record; the
-    backward recomputes the crossing lists."""
+    ``recompute`` (keyword only, not in the reference): True (the default) keeps
+    nothing between the forward and the backward but the inputs and the segment
+    record, and the backward recomputes the crossing lists; False keeps the edge
+    record and the gradient buffers (a faster backward, more memory held)."""
 
-    def __init__(self, dtype=torch.float32, *, recompute=False):
+    def __init__(self, dtype=torch.float32, *, recompute=True):
         super().__init__()
         self.dtype = dtype
         self.recompute = recompute
@@ -246,7 +251,7 @@ class DiffDMC(nn.Module):
     reference's gradient there (every patch gets the first patch's gradient).
     ``recompute=True`` as for DiffMC."""
 
-    def __init__(self, dtype=torch.float32, *, exact_grad=False, recompute=False):
+    def __init__(self, dtype=torch.float32, *, exact_grad=False, recompute=True):
         super().__init__()
         self.dtype = dtype
         self.exact_grad = exact_grad
