@@ -516,6 +516,79 @@ def run_band(device, n=2048, steps=10, warmup=3, dense_n=512):
     return out
 
 
+def octahedron_mlp(device, width=64, seed=SEED):
+    """A ReLU MLP SDF: |x| + |y| + |z| - 0.8 (|t| = relu(t) + relu(-t)) plus a seeded
+    random ReLU branch of `width` units scaled by 0.05."""
+    from torch import nn
+
+    g = torch.Generator().manual_seed(seed)
+    net = nn.Sequential(nn.Linear(3, 6 + width), nn.ReLU(), nn.Linear(6 + width, 1 + width), nn.ReLU(),
+                        nn.Linear(1 + width, 1))
+    with torch.no_grad():
+        for m in net:
+            if isinstance(m, nn.Linear):
+                m.weight.zero_()
+                m.bias.zero_()
+        net[0].weight[:3] = torch.eye(3)
+        net[0].weight[3:6] = -torch.eye(3)
+        net[0].weight[6:] = torch.randn((width, 3), generator=g) * 0.7
+        net[0].bias[6:] = torch.randn(width, generator=g) * 0.2
+        net[2].weight[0, :6] = 1.0
+        net[2].weight[1:, 6:] = torch.randn((width, width), generator=g) * (0.3 * (32 / width) ** 0.5)
+        net[4].weight[0, 0] = 1.0
+        net[4].weight[0, 1:] = torch.randn(width, generator=g) * 0.05
+        net[4].bias.fill_(-0.8)
+    return net.to(device)
+
+
+def run_mlp(device, n=256, steps=5, warmup=2):
+    """An MLP SDF (octahedron_mlp, fp32) on an n^3 grid, DiffDMC quads, forward +
+    backward to the network's parameters: from its narrow band (MLPField: interval
+    bounds per brick, the network evaluated at the band's points only) against the
+    network evaluated on the whole grid and the dense path.  The same mesh (up to the
+    rounding of evaluating a point inside one batch or another).  The dense path keeps
+    the network's activations at every grid point for its backward (about 1 KB per
+    point), hence the moderate default size."""
+    from diso_gb300 import DiffDMC, MLPField
+
+    net = octahedron_mlp(device)
+    field = MLPField(net)
+    mod = DiffDMC(torch.float32)
+
+    def band_step():
+        net.zero_grad(set_to_none=True)
+        v, q = mod.forward_mlp(field, (n, n, n), return_quads=True)
+        (v * loss_weights(v.shape[0], device, v.dtype)).sum().backward()
+        return v, q
+
+    def dense_step():
+        net.zero_grad(set_to_none=True)
+        v, q = mod(field.dense((n, n, n)), return_quads=True)
+        (v * loss_weights(v.shape[0], device, v.dtype)).sum().backward()
+        return v, q
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, out
+
+    ms_b, (vb, qb) = timed(band_step)
+    ms_d, (vd, qd) = timed(dense_step)
+    band = field.band((n, n, n), 0.0)
+    return {"field": f"ReLU MLP 3-70-65-1 (octahedron + random branch) at {n}^3, DiffDMC quads, fwd+bwd to the weights",
+            "bricks": band.count, "bricks_share": round(band.count / band.index.numel(), 4),
+            "verts": vb.shape[0], "same_faces": bool(torch.equal(qb, qd)),
+            "max_vertex_diff": float((vb - vd).detach().abs().max()) if vb.shape == vd.shape else None,
+            "dense_ms": ms_d, "band_ms": ms_b, "speedup": ms_d / ms_b}
+
+
 def run_served(device, nreq=20000, rate=2000.0, plain_sample=4000):
     """The served stream: p50 / p99 latency and grids/s of the continuous-batching
     server on the Poisson trace in real time, and its capacity (the whole trace
@@ -1073,7 +1146,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     ap.add_argument("--band-n", type=int, default=2048, help="grid size of the narrow-band measurement")
-    ap.add_argument("--only", choices=["narrow_band", "fused_field", "mesh_consumers"],
+    ap.add_argument("--only", choices=["narrow_band", "fused_field", "mesh_consumers", "mlp_field"],
                     help="run one side measurement alone and print it (for profiling)")
     args = ap.parse_args()
 
@@ -1106,7 +1179,8 @@ def main():
         device = torch.device("cuda", torch.cuda.current_device())
         fn = {"narrow_band": lambda: run_band(device, args.band_n, steps=args.steps, warmup=args.warmup),
               "fused_field": lambda: run_field(device, args.n, steps=args.steps, warmup=args.warmup),
-              "mesh_consumers": lambda: run_mesh(device, args.n, steps=args.steps, warmup=args.warmup)}[args.only]
+              "mesh_consumers": lambda: run_mesh(device, args.n, steps=args.steps, warmup=args.warmup),
+              "mlp_field": lambda: run_mlp(device, args.n, steps=args.steps, warmup=args.warmup)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
     if world > 1:
@@ -1121,7 +1195,8 @@ def main():
                          ("served", lambda: run_served(device, args.requests)),
                          ("mesh_consumers", lambda: run_mesh(device, args.n)),
                          ("fused_field", lambda: run_field(device, args.n)),
-                         ("narrow_band", lambda: run_band(device, args.band_n))):
+                         ("narrow_band", lambda: run_band(device, args.band_n)),
+                         ("mlp_field", lambda: run_mlp(device, 256))):
             try:
                 res[name] = fn()
             except Exception as e:  # report, but keep the headline line

@@ -13,8 +13,9 @@ from .batch import BatchPlan, DiffDMCBatch, DiffMCBatch, extract_batch  # noqa: 
 from .bricks import BrickGrid, extract_bricks  # noqa: F401
 from .extraction import DiffDMC, DiffMC, extract  # noqa: F401
 from .fields import SphereUnion, extract_field  # noqa: F401
+from .neural import MLPField, extract_mlp  # noqa: F401
 from . import tune  # noqa: F401
 
 __all__ = ["DiffMC", "DiffDMC", "extract", "DiffMCBatch", "DiffDMCBatch", "extract_batch", "BatchPlan", "SphereUnion",
-           "extract_field", "BrickGrid", "extract_bricks", "tune"]
+           "extract_field", "BrickGrid", "extract_bricks", "MLPField", "extract_mlp", "tune"]
 __version__ = "0.1.0"

@@ -242,6 +242,14 @@ class DiffMC(nn.Module):
 
         return extract_bricks(self._ex, grid, isovalue, normalize)
 
+    def forward_mlp(self, field, shape, isovalue=0.0, normalize=True):
+        """The mesh of an MLP field (diso_gb300.neural.MLPField) on a grid of `shape`,
+        from the narrow band where the network can cross the isovalue; differentiable
+        with respect to the network's parameters."""
+        from .neural import extract_mlp
+
+        return extract_mlp(self._ex, field, shape, isovalue, normalize)
+
 
 class DiffDMC(nn.Module):
     """Differentiable dual marching cubes (diso/__init__.py:63-147).
@@ -274,3 +282,9 @@ class DiffDMC(nn.Module):
         from .bricks import extract_bricks
 
         return extract_bricks(self._ex, grid, isovalue, normalize, return_quads, self.exact_grad)
+
+    def forward_mlp(self, field, shape, isovalue=0.0, return_quads=False, normalize=True):
+        """The mesh of an MLP field (diso_gb300.neural.MLPField), as DiffMC.forward_mlp."""
+        from .neural import extract_mlp
+
+        return extract_mlp(self._ex, field, shape, isovalue, normalize, return_quads, self.exact_grad)
