@@ -192,10 +192,11 @@ def served_trace(nreq=2000, rate=2000.0, seed=3, pool=None):
 
 
 def device_bound(trace, pool, device, reps=3):
-    """grids/s of the trace if the GPU did nothing but the requests' kernels: per
-    (N, kind, method) the extractor's kernel time of one request (CUDA events around
-    every launch, the plain per-request call), summed over the trace.  No scheduler
-    can serve the trace faster than this."""
+    """grids/s of the trace if the GPU ran nothing but the plain per-request call's
+    kernels back to back: per (N, kind, method) the extractor's kernel time of one
+    request (CUDA events around every launch), summed over the trace.  The plain loop
+    cannot serve the trace faster than this; the server can, as far as its batched
+    kernels do less device work per grid."""
     from diso_gb300 import _native as N
     from diso_gb300.extraction import extract
 
@@ -618,8 +619,8 @@ def run_served(device, nreq=20000, rate=2000.0, plain_sample=4000):
     heavy = sorted(per.items(), key=lambda kv: -kv[1])[:3]
     return {"requests": nreq, "rate_per_s": rate, "server_realtime": realtime, "server_capacity": capacity,
             "plain_per_request_capacity": plain, "plain_sample": plain_sample,
-            "device_bound_grids_s": bound,
-            "device_ms_heaviest": {f"{n}^3 {k} {'mc' if m == 0 else 'dmc'}": round(v, 3) for (n, k, m), v in heavy},
+            "plain_kernel_bound_grids_s": bound,
+            "plain_kernel_ms_heaviest": {f"{n}^3 {k} {'mc' if m == 0 else 'dmc'}": round(v, 3) for (n, k, m), v in heavy},
             "grids_s_speedup": capacity["grids_per_s"] / plain["grids_per_s"], "peak_budget_gb": peak / 1e9,
             "inputs": "device-resident pool: 4 grids per (N, kind), one N(0,1) gradient buffer",
             "workers": 4, "max_batch": 64}
