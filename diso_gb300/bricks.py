@@ -2,8 +2,8 @@
 near the surface.
 
 The reference takes dense [N, N, N] grids only (diso/__init__.py:48, 102), so its
-grids stop where their dense arrays (and, here, the dense path's 32-bit counts, about
-890^3 points) stop.  A ``BrickGrid`` keeps
+grids stop where their dense arrays stop (32 B per point in fp32 with deform and both
+gradients: 275 GB at 2048^3).  A ``BrickGrid`` keeps
 
 * ``index`` [ceil(n0/8), ceil(n1/8), ceil(n2/8)] int32: each brick's slot, or
   BRICK_OUTSIDE (-1) / BRICK_INSIDE (-2) for an absent brick, whose points read

@@ -454,13 +454,27 @@ int run_scan(diso_extractor* ex, uint64_t* a, int64_t n, cudaStream_t s, bool pr
   return DISO_OK;
 }
 
+// A grid's counts are scanned in two 32-bit halves (crossings; triangles / patches),
+// and vertex ids are 32-bit in the records: with at most 3 crossings per cell, a grid
+// of fewer than 2^31 / 3 cells can never overflow them.  A larger grid (up to the
+// index limits below) is checked after its count instead: the count also sums both
+// halves in 64 bits (Stats::sum_lo / sum_hi), and count_read rejects counts that do
+// not fit, before anything reads the record (forward_all waits for that check before
+// its emit).
+constexpr int kMaxDim = 16384;
+constexpr double kMaxCells = 68719476736.0;  // 2^36
+inline bool counts_always_fit(int nx, int ny, int nz) {
+  return 3.0 * (double)(nx + 1) * (ny + 1) * (nz + 1) < 2147483647.0;
+}
+
 int check_common(diso_extractor* ex, const void* sdf, int nx, int ny, int nz) {
   if (!ex) return fail(DISO_ERR_ARG, "null extractor");
   if (!sdf) return fail(DISO_ERR_ARG, "null sdf");
   if (nx < 1 || ny < 1 || nz < 1) return fail(DISO_ERR_ARG, "grid dims must be >= 1 (got %d x %d x %d)", nx, ny, nz);
-  // crossings are counted in 32 bits per half of the scan value: at most 3 per cell
-  double cells = (double)(nx + 1) * (ny + 1) * (nz + 1);
-  if (3.0 * cells >= 2147483647.0) return fail(DISO_ERR_ARG, "grid too large: %d x %d x %d", nx, ny, nz);
+  const double cells = (double)(nx + 1) * (ny + 1) * (nz + 1);
+  if (nx > kMaxDim || ny > kMaxDim || nz > kMaxDim || cells >= kMaxCells)
+    return fail(DISO_ERR_ARG, "grid too large: %d x %d x %d (at most %d points per axis and 2^36 cells)", nx, ny,
+                nz, kMaxDim);
   return bind_device(ex);
 }
 
@@ -567,6 +581,11 @@ int count_read(diso_extractor* ex, int nx, int ny, int nz, double iso, const uin
   const uint64_t total = h.total;
   if (h.error & 1ull) return fail(DISO_ERR_SCAN, "segment scan: look-back wait gave up");
   if (h.error & 4ull) return fail(DISO_ERR_SCAN, "count: wait for a TMA copy gave up");
+  // the scanned 32-bit halves against the count's 64-bit sums
+  if (h.sum_lo != Counts::lo(total) || h.sum_hi != Counts::hi(total) || h.sum_lo >= (1ull << 31) ||
+      h.sum_hi >= (1ull << 31))
+    return fail(DISO_ERR_ARG, "%d x %d x %d: too many crossings for 32-bit counts (%llu and %llu)", nx, ny, nz,
+                (unsigned long long)h.sum_lo, (unsigned long long)h.sum_hi);
   // the low half counts crossings, the high half triangles (MC) or patches (DMC)
   if (ex->method == DISO_MC) {
     out->n_verts = Counts::lo(total);
@@ -642,12 +661,19 @@ int forward_all(diso_extractor* ex, const void* sdf, const void* deform, int nx,
   int rc;
   if ((rc = count_launch<S>(ex, sdf, nx, ny, nz, iso, padval, seg, s)) != DISO_OK) return rc;
   if ((rc = count_copy<S>(ex, g, seg, s)) != DISO_OK) return rc;
-  // the emit is queued before the host waits for the counts, and still runs when it returns
+  // a grid whose counts could overflow is checked before its emit reads the record
+  const bool checked = !counts_always_fit(nx, ny, nz);
+  if (checked) {
+    if ((rc = count_read<S>(ex, nx, ny, nz, iso, seg, s, out)) != DISO_OK) return rc;
+    if (out->empty) return DISO_OK;
+  }
+  // otherwise the emit is queued before the host waits for the counts, and still runs
+  // when it returns
   if ((rc = emit_launch<S>(ex, sdf, deform, nx, ny, nz, iso, padval, seg, normalize, verts, faces, record,
                            tuned_ctas(ex, DISO_TUNE_EMIT_CTAS, ex->emit_ctas, ex->per_sm[1]), vcap, fcap, s)) !=
       DISO_OK)
     return rc;
-  if ((rc = count_read<S>(ex, nx, ny, nz, iso, seg, s, out)) != DISO_OK) return rc;
+  if (!checked && (rc = count_read<S>(ex, nx, ny, nz, iso, seg, s, out)) != DISO_OK) return rc;
   out->emitted = (out->n_verts <= vcap && out->n_faces <= fcap) ? 1 : 0;
   return DISO_OK;
 }

@@ -183,6 +183,8 @@ struct Stats {
   unsigned long long emit_tile; // dynamic tile counter of the emit
   unsigned long long total;      // the segment scan's total (the forward's counts)
   unsigned long long units;      // next unit of the TMA count (a grid-wide counter)
+  unsigned long long sum_lo;     // the count's two halves summed in 64 bits (crossings; triangles /
+  unsigned long long sum_hi;     //   patches): the scan's 32-bit halves hold them only below 2^32
 };
 
 }  // namespace diso

@@ -381,10 +381,12 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 // walks only the segment's non-trivial cells for the case-table lookups (the DMC
 // ambiguity test reads a neighbour outside the unit's rows from global memory).
 //
-// Persistent: CTA b handles units b, b + gridDim.x, ...; it keeps the list of its
-// active tiles and publishes it with one atomic at the end (per-tile atomics on one
-// address serialise in L2).  At most COUNT_LIST tiles per CTA: launch at least
-// ntiles / COUNT_LIST CTAs.
+// Persistent: CTA b handles units b, b + gridDim.x, ... (the TMA count takes them
+// from a grid-wide counter); it keeps the list of its active tiles and publishes it
+// with one atomic at the end (per-tile atomics on one address serialise in L2).  The
+// launches size grids for at most COUNT_LIST tiles per CTA; tiles past that (a CTA
+// that took more units than its share, on grids where nearly every tile is active)
+// go to the global list with an atomic each.
 constexpr int CP = 8, CR = 32, KZ = 4;
 constexpr int CROWS = (CP + 1) * (CR + 1);  // point rows of a unit
 constexpr int CRPW = (CROWS + 7) / 8;       // point rows per warp
@@ -406,7 +408,21 @@ struct CountShared {
   __align__(16) CellRec code[CP][32][TZ];  // cell records of each lane's segment (staging)
   int list[COUNT_LIST];
   int nlist, base;
+  unsigned long long tot[2];  // the CTA's counts (both halves) in 64 bits, for Stats::sum_lo / sum_hi
+  // the global list and its counter: tiles past COUNT_LIST go there directly (a CTA
+  // that takes units from a grid-wide counter may meet more active tiles than its share)
+  int* spill;
+  unsigned long long* spill_n;
 };
+
+// the CTA's 64-bit count sums into the status words (after count_flush)
+template <class S, int METHOD>
+__device__ __forceinline__ void count_totals(CountShared<S, METHOD>& sh, Stats* stats) {
+  if (threadIdx.x == 0) {
+    if (sh.tot[0]) atomicAdd(&stats->sum_lo, sh.tot[0]);
+    if (sh.tot[1]) atomicAdd(&stats->sum_hi, sh.tot[1]);
+  }
+}
 
 __device__ __forceinline__ float smin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float smax(float a, float b) { return fmaxf(a, b); }
@@ -570,6 +586,19 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F&
       out[3] = stage[3];
     }
   }
+  // the warp's counts into the CTA's 64-bit sums (a warp's fit 32 bits)
+  {
+    uint32_t tv = nv, tf = nf;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      tv += __shfl_xor_sync(0xffffffffu, tv, o);
+      tf += __shfl_xor_sync(0xffffffffu, tf, o);
+    }
+    if (lane == 0 && (tv | tf)) {
+      atomicAdd(&sh.tot[0], (unsigned long long)tv);
+      atomicAdd(&sh.tot[1], (unsigned long long)tf);
+    }
+  }
   // a cell can emit faces / patches without owning a crossing edge (its
   // crossings may all sit on edges owned by its +1 neighbours)
   const uint32_t busy = __ballot_sync(0xffffffffu, (nv | nf) != 0);
@@ -599,7 +628,13 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F&
       const int64_t tile = ((int64_t)tx * g.tiles_y() + ty) * g.nzc + tz;
       tile_flag[tile] = any ? 1 : 0;
       tile_flag[g.ntiles() + tile] = (uint8_t)bw;
-      if (any) sh.list[atomicAdd(&sh.nlist, 1)] = (int)tile | tag;
+      if (any) {
+        const int at = atomicAdd(&sh.nlist, 1);
+        if (at < COUNT_LIST)
+          sh.list[at] = (int)tile | tag;
+        else
+          sh.spill[atomicAdd(sh.spill_n, 1ull)] = (int)tile | tag;
+      }
     }
   }
 }
@@ -732,9 +767,10 @@ template <class S, int METHOD>
 __device__ __forceinline__ void count_flush(CountShared<S, METHOD>& sh, unsigned long long* n_active,
                                             int* __restrict__ active) {
   __syncthreads();
-  if (threadIdx.x == 0) sh.base = sh.nlist ? (int)atomicAdd(n_active, (unsigned long long)sh.nlist) : 0;
+  const int n = min(sh.nlist, COUNT_LIST);  // the others went to the list directly
+  if (threadIdx.x == 0) sh.base = n ? (int)atomicAdd(n_active, (unsigned long long)n) : 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < sh.nlist; i += blockDim.x) active[sh.base + i] = sh.list[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) active[sh.base + i] = sh.list[i];
 }
 
 template <class S, int METHOD, class F = Field<S>>
@@ -745,6 +781,9 @@ __global__ void __launch_bounds__(NTHREADS, F::kDense ? 3 : 2) count_kernel(F f,
   __shared__ CountShared<S, METHOD> sh;
   if (threadIdx.x == 0) {
     sh.nlist = 0;
+    sh.tot[0] = sh.tot[1] = 0ull;
+    sh.spill = active;
+    sh.spill_n = &stats->n_active;
     sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
   }
   const int64_t nunits = count_units(g);
@@ -753,6 +792,7 @@ __global__ void __launch_bounds__(NTHREADS, F::kDense ? 3 : 2) count_kernel(F f,
   for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x)
     count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, u, 0, ck);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
+  count_totals<S, METHOD>(sh, stats);
 }
 
 // ------------------------------------------------------------------ evaluated fields
@@ -798,6 +838,9 @@ __global__ void __launch_bounds__(NTHREADS, 2) field_count_kernel(F f, Geom g, u
   __shared__ CountShared<S, METHOD> sh;
   if (threadIdx.x == 0) {
     sh.nlist = 0;
+    sh.tot[0] = sh.tot[1] = 0ull;
+    sh.spill = active;
+    sh.spill_n = &stats->n_active;
     sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
   }
   const int n = units[0];
@@ -806,6 +849,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) field_count_kernel(F f, Geom g, u
   for (int i = blockIdx.x; i < n; i += gridDim.x)
     count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, units[1 + i], 0, ck);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
+  count_totals<S, METHOD>(sh, stats);
 }
 
 // ------------------------------------------------------------------ count through TMA
@@ -989,6 +1033,9 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   if (zj.rounds) zero_block_init(zbuf);
   if (threadIdx.x == 0) {
     sh.nlist = 0;
+    sh.tot[0] = sh.tot[1] = 0ull;
+    sh.spill = active;
+    sh.spill_n = &stats->n_active;
     sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
 #pragma unroll
     for (int st = 0; st < TMA_STAGES; ++st) mbar_init(&full[st], 1);
@@ -1099,6 +1146,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) count_tma_kernel(const __grid_con
   if (warp == 1) zero_finish(zj, zbuf, k, lane);
   publish_minmax<S>(stats, mn, mx);
   count_flush<S, METHOD>(sh, &stats->n_active, active);
+  count_totals<S, METHOD>(sh, stats);
 }
 
 // ------------------------------------------------------------------ batches
@@ -1145,6 +1193,9 @@ __global__ void __launch_bounds__(NTHREADS, 3) batch_count_kernel(const BatchGri
   for (int i = threadIdx.x; i < ngrids; i += blockDim.x) start[i] = grids[i].cblk0;
   if (threadIdx.x == 0) {
     sh.nlist = 0;
+    sh.tot[0] = sh.tot[1] = 0ull;
+    sh.spill = active;
+    sh.spill_n = n_active;
     sh.mixed[0] = sh.mixed[1] = sh.mixed[2] = 0;
   }
   __syncthreads();

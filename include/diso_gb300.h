@@ -82,7 +82,13 @@ int64_t diso_segment_slots(int nx, int ny, int nz);
 /* Forward, phase 1: case codes, counts, scan and the empty-surface guard.
  * Replaces CuMC::forward / CUDualMC::forward up to their last scan
  * (src/cumc.cu:651-723, src/cudualmc.cu:1058-1122), the guard's min/max
- * (diso/__init__.py:49, 103) and the pad (diso/__init__.py:52-54). */
+ * (diso/__init__.py:49, 103) and the pad (diso/__init__.py:52-54).
+ *
+ * Sizes: at most 16384 points per axis and 2^36 cells.  The output counts are
+ * scanned in 32 bits: a grid of fewer than 2^31 / 3 cells (about 890^3) always fits;
+ * for a larger one the count's 64-bit sums are checked, and counts of 2^31 or more
+ * (crossings, or triangles / patches) are DISO_ERR_ARG.  diso_forward then waits for
+ * that check before its emit. */
 int diso_forward_count(diso_extractor* ex, const void* sdf, int nx, int ny, int nz, double isovalue, double padval,
                        uint64_t* seg, void* stream, diso_counts* out);
 
@@ -332,8 +338,8 @@ int diso_field_materialize(int dtype, const diso_sphere_field* field, int nx, in
 
 /* ---- Narrow-band input ----
  * A grid whose values are stored only in 8 x 8 x 8-point bricks near the surface, for
- * grids whose dense arrays (and the dense path's 32-bit limit of about 890^3 points)
- * are out of reach.  index [ceil(nx/8)][ceil(ny/8)][ceil(nz/8)] (int32, device)
+ * grids whose dense arrays are out of reach (32 B per point in fp32 with deform and
+ * both gradients: 275 GB at 2048^3).  index [ceil(nx/8)][ceil(ny/8)][ceil(nz/8)] (int32, device)
  * holds each brick's slot in values [count][8][8][8] (the dtype, z fastest), or
  * DISO_BRICK_OUTSIDE / DISO_BRICK_INSIDE for an absent brick, whose points read
  * +background / -background.  The band's meshes are exactly those of the dense grid

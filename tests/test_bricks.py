@@ -146,7 +146,9 @@ def test_brick_entry_points_check_their_arguments(lib):
     d.deform = None
     assert lib.diso_bricks_materialize(0, ctypes.byref(d), p, p, None) == 1
     assert b"without one" in lib.diso_last_error()
-    # the dense path's worst-case 32-bit limit, which the band lifts
-    assert lib.diso_forward_count(h, p, 1024, 1024, 1024, 0.0, 1.0, p, None, ctypes.byref(c)) == 1
+    # the dense path's index limits (counts of larger grids are checked after the count)
+    assert lib.diso_forward_count(h, p, 16385, 16, 16, 0.0, 1.0, p, None, ctypes.byref(c)) == 1
+    assert b"too large" in lib.diso_last_error()
+    assert lib.diso_forward_count(h, p, 8192, 8192, 2048, 0.0, 1.0, p, None, ctypes.byref(c)) == 1
     assert b"too large" in lib.diso_last_error()
     lib.diso_destroy(h)
