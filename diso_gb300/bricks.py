@@ -15,8 +15,8 @@ filled with +-background, zero deform there): the same vertices, faces and order
 ``extract_bricks`` runs the forward (diso_forward_bricks) and, through autograd, the
 backward (diso_backward_bricks) into the slots: dL/dvalues and dL/ddeform are the
 dense gradients at the bricks' points.  Memory grows with the bricks, the index (4 B
-per brick) and the segment record (8 B per 32-cell row segment); DMC also keeps its
-cell records dense in the extractor's scratch (2 B per cell).
+per brick) and the segment record (8 B per 32-cell row segment); DMC keeps its cell
+records in the extractor's scratch only for the count units that hold the surface.
 """
 from __future__ import annotations
 

@@ -105,6 +105,8 @@ struct diso_extractor {
   cudaEvent_t ev_counts = nullptr;  // the count's results are on the host
   int* ulist = nullptr;          // an evaluated field's count units that hold the surface (count, then ids)
   int64_t ulist_cap = 0;
+  int* umap = nullptr;           // a narrow band's unit -> block of DMC cell records (-1: none)
+  int64_t umap_cap = 0;
   int* plist = nullptr;          // active point tiles of the backward, and their count
   int64_t plist_cap = 0;
   unsigned* plist_n = nullptr;
@@ -191,6 +193,9 @@ struct diso_extractor {
     cudaFree(ulist);
     ulist = nullptr;
     ulist_cap = 0;
+    cudaFree(umap);
+    umap = nullptr;
+    umap_cap = 0;
     cudaFree(bcheck);
     bcheck = nullptr;
     bcheck_cap = 0;
@@ -1203,12 +1208,16 @@ SphereField<S> make_sphere_field(const diso_sphere_field* d, int nx, int ny, int
 // the crossing edges.
 template <class S, class F>
 int forward_field(diso_extractor* ex, const F& f, double iso, uint64_t* seg, int normalize,
-                  void* verts, int64_t vcap, int64_t* faces, int64_t fcap, cudaStream_t s, diso_counts* out) {
+                  void* verts, int64_t vcap, int64_t* faces, int64_t fcap, cudaStream_t s, diso_counts* out,
+                  int* umap = nullptr) {
   Geom g;
   g.init(f.n0, f.n1, f.n2);
   int rc;
+  // DMC cell records: dense, or (umap, a narrow band) one block per unit that holds
+  // the surface, grown once the units are listed
+  const bool blocks = umap != nullptr && ex->method == DISO_DMC;
   if ((rc = grow(ex->active, ex->active_cap, g.ntiles())) != DISO_OK) return rc;
-  if (ex->method == DISO_DMC && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
+  if (ex->method == DISO_DMC && !blocks && (rc = grow(ex->codes, ex->codes_cap, g.ncodes())) != DISO_OK) return rc;
   const int64_t scan_tiles = scan_reserve(ex, g.nseg);
   if (scan_tiles == 0) return DISO_ERR_CUDA;
   // a narrow band's records serve its backward (brick_backward_kernel); a sphere
@@ -1228,12 +1237,25 @@ int forward_field(diso_extractor* ex, const F& f, double iso, uint64_t* seg, int
     const int64_t units = count_units(g);
     if ((rc = grow(ex->ulist, ex->ulist_cap, units + 1)) != DISO_OK) return rc;
     CUDA_TRY(cudaMemsetAsync(ex->ulist, 0, sizeof(int), s));
+    if (blocks) CUDA_TRY(cudaMemsetAsync(umap, 0xff, sizeof(int) * (size_t)units, s));
     const int64_t want =
         std::max<int64_t>(ex->resident_ctas, (units * COUNT_TILES_PER_UNIT + COUNT_LIST - 1) / COUNT_LIST);
     const unsigned grid = (unsigned)std::min<int64_t>(want, units);
+    {
+      KernelTimer kt(ex, K_COUNT, s);
+      field_units_kernel<S, F><<<stride_ctas(units * 32, (unsigned)ex->sms * 16), 256, 0, s>>>(
+          f, g, ex->stats, ex->ulist, blocks ? umap : nullptr);
+    }
+    CUDA_TRY(cudaGetLastError());
+    if (blocks) {  // the listed units' record blocks (one host round trip)
+      int listed = 0;
+      CUDA_TRY(cudaMemcpyAsync(&listed, ex->ulist, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+      if ((rc = grow(ex->codes, ex->codes_cap, std::max(listed, 1) * BrickField<S>::UNIT_RECS)) != DISO_OK)
+        return rc;
+      codes = ex->codes;
+    }
     KernelTimer kt(ex, K_COUNT, s);
-    field_units_kernel<S, F><<<stride_ctas(units * 32, (unsigned)ex->sms * 16), 256, 0, s>>>(f, g, ex->stats,
-                                                                                              ex->ulist);
     if (ex->method == DISO_MC)
       field_count_kernel<S, MC, F><<<grid, NTHREADS, 0, s>>>(f, g, seg, tile_flags(seg, g), codes, ex->stats,
                                                              ex->active, ex->ulist);
@@ -1308,8 +1330,14 @@ int check_field(const diso_sphere_field* field, int nx, int ny, int nz) {
 // ------------------------------------------------------------------ narrow band
 
 template <class S>
-BrickField<S> make_brick_field(const diso_brick_grid* b, double iso, double padval) {
+BrickField<S> make_brick_field(const diso_brick_grid* b, double iso, double padval, const int* umap = nullptr) {
   BrickField<S> f;
+  Geom g;
+  g.init(b->dims[0], b->dims[1], b->dims[2]);
+  f.umap = umap;
+  f.unby = (g.c[1] + CR - 1) / CR;
+  f.unbz = (g.nzc + KZ - 1) / KZ;
+  f.ukz = (g.nzc + f.unbz - 1) / f.unbz;
   f.index = b->index;
   f.val = (const S*)b->values;
   f.def = (const S*)b->deform;
@@ -1999,14 +2027,18 @@ int diso_forward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, doubl
   if (vcap < 0 || fcap < 0 || (vcap && !verts) || (fcap && !faces)) return fail(DISO_ERR_ARG, "bad output buffers");
   if ((rc = bind_device(ex)) != DISO_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  Geom g;
+  g.init(bricks->dims[0], bricks->dims[1], bricks->dims[2]);
+  if (ex->method == DISO_DMC && (rc = grow(ex->umap, ex->umap_cap, count_units(g))) != DISO_OK) return rc;
+  int* umap = ex->method == DISO_DMC ? ex->umap : nullptr;
   if (ex->dtype == DISO_F32) {
     if ((rc = validate_bricks<float>(ex, bricks, isovalue, padval, s)) != DISO_OK) return rc;
-    return forward_field<float>(ex, make_brick_field<float>(bricks, isovalue, padval), isovalue, seg, normalize,
-                                verts, vcap, faces, fcap, s, out);
+    return forward_field<float>(ex, make_brick_field<float>(bricks, isovalue, padval, umap), isovalue, seg,
+                                normalize, verts, vcap, faces, fcap, s, out, umap);
   }
   if ((rc = validate_bricks<double>(ex, bricks, isovalue, padval, s)) != DISO_OK) return rc;
-  return forward_field<double>(ex, make_brick_field<double>(bricks, isovalue, padval), isovalue, seg, normalize,
-                               verts, vcap, faces, fcap, s, out);
+  return forward_field<double>(ex, make_brick_field<double>(bricks, isovalue, padval, umap), isovalue, seg,
+                               normalize, verts, vcap, faces, fcap, s, out, umap);
 }
 
 int diso_backward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
@@ -2022,9 +2054,10 @@ int diso_backward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, doub
   cudaStream_t s = (cudaStream_t)stream;
   void* gd = bricks->deform ? grad_deform : nullptr;
   return ex->dtype == DISO_F32
-             ? backward_bricks<float>(ex, make_brick_field<float>(bricks, isovalue, padval), bricks->count, seg,
+             ? backward_bricks<float>(ex, make_brick_field<float>(bricks, isovalue, padval, ex->umap), bricks->count, seg,
                                       normalize, flags, grad_verts, grad_values, gd, s)
-             : backward_bricks<double>(ex, make_brick_field<double>(bricks, isovalue, padval), bricks->count, seg,
+             : backward_bricks<double>(ex, make_brick_field<double>(bricks, isovalue, padval, ex->umap), bricks->count,
+                                       seg,
                                        normalize, flags, grad_verts, grad_values, gd, s);
 }
 

@@ -25,6 +25,8 @@
 namespace diso {
 
 constexpr int TZ = 32;        // cells per tile along z (one per lane)
+// count units: CP x CR rows of cells, runs of at most KZ 32-cell chunks
+constexpr int CP = 8, CR = 32, KZ = 4;
 constexpr int TY = 8;         // rows per tile along y (one per warp)
 constexpr int TX = 4;         // planes per tile along x (per-thread loop)
 constexpr int NTHREADS = 32 * TY;
@@ -83,6 +85,8 @@ struct Field {
   __device__ __forceinline__ int64_t lin(int X, int Y, int Z) const {
     return ((int64_t)(X - 1) * n1 + (Y - 1)) * n2 + (Z - 1);
   }
+  // position of cell (X, Y, Z)'s DMC record (rows padded to whole chunks)
+  __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const { return g.code(X, Y, Z); }
   // unpadded point (x, y, z) of a row in the grid whose first point is at `off`
   __device__ __forceinline__ S point(int64_t off, int, int, int z) const { return __ldg(sdf + off + z); }
   // deform at padded point (zero in the pad)

@@ -40,6 +40,7 @@ struct SphereField {
   }
   // value at padded point (X, Y, Z); the pad value outside the grid
   __device__ __forceinline__ S at(int X, int Y, int Z) const { return inside(X, Y, Z) ? value(X - 1, Y - 1, Z - 1) : pad; }
+  __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const { return g.code(X, Y, Z); }
   // unpadded point (x, y, z) of a row in the grid (the row offset is not used)
   __device__ __forceinline__ S point(int64_t, int x, int y, int z) const { return value(x, y, z); }
   // deform at padded point (zero in the pad)
@@ -179,6 +180,21 @@ struct BrickField {
   int K;         // slots; an entry at or above K reads as absent (the forward rejects it)
   int n0, n1, n2;
   S iso, pad, bg;
+  // DMC cell records, kept only for the count units that hold the surface: umap[unit]
+  // is the unit's block (UNIT_RECS records) in the records' array, -1 for the others
+  // (the units of field_count_kernel: unby x unbz runs of ukz chunks per row block)
+  const int* __restrict__ umap;
+  int unby, unbz, ukz;
+  static constexpr int64_t UNIT_RECS = (int64_t)CP * CR * KZ * TZ;
+
+  __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const {
+    (void)g;
+    const int tz = Z / TZ, uz = tz / ukz;
+    const int64_t unit = ((int64_t)(X / CP) * unby + Y / CR) * unbz + uz;
+    const int slot = umap[unit];
+    const int64_t off = ((int64_t)(X % CP) * CR + Y % CR) * (KZ * TZ) + (Z - uz * ukz * TZ);
+    return (int64_t)(slot < 0 ? 0 : slot) * UNIT_RECS + off;  // a listed unit's block (no other is read)
+  }
 
   __device__ __forceinline__ int entry(int x, int y, int z) const {
     const int e = __ldg(index + ((int64_t)(x >> 3) * nb1 + (y >> 3)) * nb2 + (z >> 3));

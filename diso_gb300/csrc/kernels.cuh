@@ -387,7 +387,6 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 // launches size grids for at most COUNT_LIST tiles per CTA; tiles past that (a CTA
 // that took more units than its share, on grids where nearly every tile is active)
 // go to the global list with an atomic each.
-constexpr int CP = 8, CR = 32, KZ = 4;
 constexpr int CROWS = (CP + 1) * (CR + 1);  // point rows of a unit
 constexpr int CRPW = (CROWS + 7) / 8;       // point rows per warp
 constexpr int COUNT_LIST = 2048;
@@ -579,7 +578,7 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F&
     }
     seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
     if (codes && nt) {
-      uint4* out = reinterpret_cast<uint4*>(codes + g.code(X, Y, Z0));
+      uint4* out = reinterpret_cast<uint4*>(codes + f.rec_index(g, X, Y, Z0));
       out[0] = stage[0];
       out[1] = stage[1];
       out[2] = stage[2];
@@ -803,7 +802,8 @@ __global__ void __launch_bounds__(NTHREADS, F::kDense ? 3 : 2) count_kernel(F f,
 // left out (its record stays as the host zeroed it), the others are appended to
 // units[1 ..] (units[0] counts them) for field_count_kernel.
 template <class S, class F>
-__global__ void __launch_bounds__(256) field_units_kernel(F f, Geom g, Stats* stats, int* __restrict__ units) {
+__global__ void __launch_bounds__(256) field_units_kernel(F f, Geom g, Stats* stats, int* __restrict__ units,
+                                                          int* __restrict__ umap) {
   const int lane = threadIdx.x & 31;
   const int nby = (g.c[1] + CR - 1) / CR, nbz = (g.nzc + KZ - 1) / KZ, kz = (g.nzc + nbz - 1) / nbz;
   const int64_t nunits = count_units(g), step = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -823,7 +823,9 @@ __global__ void __launch_bounds__(256) field_units_kernel(F f, Geom g, Stats* st
     if (f.classify_warp(xa, xb, ya, yb, za, zb, pads, bound, cand, all) >= 0) {
       if (xa <= xb && ya <= yb && za <= zb) publish_minmax<S>(stats, bound, bound);
     } else if (lane == 0) {
-      units[1 + atomicAdd(units, 1)] = (int)u;
+      const int at = atomicAdd(units, 1);
+      units[1 + at] = (int)u;
+      if (umap) umap[u] = at;  // the unit's block of cell records (a narrow band's DMC)
     }
   }
 }
@@ -1513,9 +1515,9 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
       if (r < KX * KY) {
         const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
         const uint32_t act = sact[wx][wy];
-        if (act & 2) c[k] = codes[g.code(X, Y, Z0 + lane)];
-        if (lane == 0 && (act & 1)) e[k] = codes[g.code(X, Y, Z0 - 1)];
-        if (lane == 31 && (act & 4)) e[k] = codes[g.code(X, Y, Z0 + TZ)];
+        if (act & 2) c[k] = codes[f.rec_index(g, X, Y, Z0 + lane)];
+        if (lane == 0 && (act & 1)) e[k] = codes[f.rec_index(g, X, Y, Z0 - 1)];
+        if (lane == 31 && (act & 4)) e[k] = codes[f.rec_index(g, X, Y, Z0 + TZ)];
       }
     }
 #pragma unroll

@@ -365,8 +365,9 @@ typedef struct diso_brick_grid {
  * bricks and absent bricks beside an absent brick of the other side (or the grid's
  * edge) allow more crossings than the 32-bit counts hold is DISO_ERR_ARG.  The count
  * classifies chunks whose bricks are all absent from the index alone.  The `seg`
- * record has the dense grid's size (8 bytes per 32-cell row segment); DMC also keeps
- * the dense cell records in the extractor's scratch (2 bytes per cell). */
+ * record has the dense grid's size (8 bytes per 32-cell row segment); DMC keeps its
+ * cell records in the extractor's scratch for the count units that hold the surface
+ * only (64 KB per unit of 8 x 32 x 128 cells; one more host round trip sizes them). */
 int diso_forward_bricks(diso_extractor* ex, const diso_brick_grid* bricks, double isovalue, double padval,
                         uint64_t* seg, int normalize, void* verts, int64_t vcap, int64_t* faces, int64_t fcap,
                         void* stream, diso_counts* counts);
