@@ -1045,7 +1045,9 @@ def run_ours(args, rank, world, device):
                 "h2d_bytes_per_step": int(sdf.numel() * 4 + deform.numel() * 4),
                 "d2h_bytes_per_step": int(d2h["bytes"]) + 4,
                 "d2h": "verts, quads, grad_sdf, grad_deform and the loss"},
-        "gpu_launches": sum(cnt for k, (cnt, _) in kernels.items() if k != "zero_grads"),
+        # the timed kernels, and the count_prep_kernel launched before every count
+        "gpu_launches": sum(cnt for k, (cnt, _) in kernels.items() if k != "zero_grads")
+        + kernels.get("count", (0, 0.0))[0],
         "clocks": clocks,
     }
     return res
