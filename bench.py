@@ -517,6 +517,71 @@ def run_band(device, n=2048, steps=10, warmup=3, dense_n=512):
     return out
 
 
+def run_configs(device, steps=5, warmup=2):
+    """The reference's other published configurations, device-resident, forward +
+    backward (loss = sum(verts * w), w ~ N(0, 1) seeded; the first configuration sums
+    the vertices): the 64^3 sphere (MC, fp32, no deform) and the 256^3 round cube and
+    U(-1, 1) random init (MC, DMC quads and DMC triangles; fp32 and fp64; deform
+    U(-0.45, 0.45)).  ms per step; the same fields as tests/test_gpu_config256.py."""
+    from diso_gb300 import DiffDMC, DiffMC
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    out = {}
+    a = torch.linspace(-1, 1, 64, device=device)
+    sphere = torch.sqrt(a.view(-1, 1, 1) ** 2 + a.view(1, -1, 1) ** 2 + a.view(1, 1, -1) ** 2) - 0.5
+    s1 = sphere.clone().requires_grad_(True)
+    mc = DiffMC(torch.float32)
+
+    def first():
+        s1.grad = None
+        v, _ = mc(s1)
+        v.sum().backward()
+
+    out["sphere64_mc_f32"] = round(timed(first), 4)
+    n = 256
+    g = torch.Generator(device=device).manual_seed(0)
+    a = torch.linspace(-1, 1, n, device=device, dtype=torch.float64)
+    X, Y, Z = a.view(-1, 1, 1), a.view(1, -1, 1), a.view(1, 1, -1)
+    q = [torch.clamp(c.abs() - 0.5, min=0) for c in (X, Y, Z)]
+    fields = {"roundcube": torch.sqrt(q[0] ** 2 + q[1] ** 2 + q[2] ** 2) - 0.1,
+              "random": torch.rand((n, n, n), device=device, dtype=torch.float64, generator=g) * 2 - 1}
+    dfm64 = (torch.rand((n, n, n, 3), device=device, dtype=torch.float64, generator=g) - 0.5) * 0.9
+    for name, f64 in fields.items():
+        for dt in (torch.float32, torch.float64):
+            sdf, dfm = f64.to(dt).contiguous(), dfm64.to(dt)
+            for method, rq in (("mc", None), ("dmc_quads", True), ("dmc_tris", False)):
+                mod = DiffMC(dt) if method == "mc" else DiffDMC(dt)
+                kw = {} if rq is None else {"return_quads": rq}
+                s = sdf.clone().requires_grad_(True)
+                d = dfm.clone().requires_grad_(True)
+                v, _ = mod(s, d, **kw)
+                w = torch.randn(v.shape, dtype=dt, device=device, generator=torch.Generator(device).manual_seed(1))
+                del v
+
+                def step():
+                    s.grad = None
+                    d.grad = None
+                    vv, _ = mod(s, d, **kw)
+                    (vv * w).sum().backward()
+
+                out[f"{name}{n}_{method}_{str(dt)[-7:]}"] = round(timed(step), 4)
+                del s, d, w
+            del sdf, dfm
+    return {"ms_per_step": out, "note": "device-resident inputs; 64^3: loss = sum(verts); 256^3: deform, "
+                                        "loss = sum(verts * w)"}
+
+
 def octahedron_mlp(device, width=64, seed=SEED):
     """A ReLU MLP SDF: |x| + |y| + |z| - 0.8 (|t| = relu(t) + relu(-t)) plus a seeded
     random ReLU branch of `width` units scaled by 0.05."""
@@ -1149,7 +1214,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the uneven-batch and served measurements")
     ap.add_argument("--requests", type=int, default=20000, help="served-trace length")
     ap.add_argument("--band-n", type=int, default=2048, help="grid size of the narrow-band measurement")
-    ap.add_argument("--only", choices=["narrow_band", "fused_field", "mesh_consumers", "mlp_field"],
+    ap.add_argument("--only", choices=["narrow_band", "fused_field", "mesh_consumers", "mlp_field", "configs"],
                     help="run one side measurement alone and print it (for profiling)")
     args = ap.parse_args()
 
@@ -1183,7 +1248,8 @@ def main():
         fn = {"narrow_band": lambda: run_band(device, args.band_n, steps=args.steps, warmup=args.warmup),
               "fused_field": lambda: run_field(device, args.n, steps=args.steps, warmup=args.warmup),
               "mesh_consumers": lambda: run_mesh(device, args.n, steps=args.steps, warmup=args.warmup),
-              "mlp_field": lambda: run_mlp(device, args.n, steps=args.steps, warmup=args.warmup)}[args.only]
+              "mlp_field": lambda: run_mlp(device, args.n, steps=args.steps, warmup=args.warmup),
+              "configs": lambda: run_configs(device, steps=args.steps, warmup=args.warmup)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
     if world > 1:
@@ -1199,7 +1265,8 @@ def main():
                          ("mesh_consumers", lambda: run_mesh(device, args.n)),
                          ("fused_field", lambda: run_field(device, args.n)),
                          ("narrow_band", lambda: run_band(device, args.band_n)),
-                         ("mlp_field", lambda: run_mlp(device, 256))):
+                         ("mlp_field", lambda: run_mlp(device, 256)),
+                         ("configs", lambda: run_configs(device))):
             try:
                 res[name] = fn()
             except Exception as e:  # report, but keep the headline line
