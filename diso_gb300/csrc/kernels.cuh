@@ -2330,7 +2330,11 @@ __device__ __forceinline__ S tri_max_cos(const S* __restrict__ V, int64_t ia, in
     S n2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
     n1 = n1 > S(1e-12) ? n1 : S(1e-12);
     n2 = n2 > S(1e-12) ? n2 : S(1e-12);
-    const S c = (e1[0] / n1) * (e2[0] / n2) + (e1[1] / n1) * (e2[1] / n2) + (e1[2] / n1) * (e2[2] / n2);
+    // the cosine of the normalised edges (the reference normalises each edge, then
+    // takes the dot product) with one division: the same value up to rounding, so
+    // the split can differ only where the two configurations' cosines tie to within
+    // it (FP64 divisions are slow on this GPU)
+    const S c = (e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2]) / (n1 * n2);
     m = (i == 0 || c > m || c != c) ? c : m;
   }
   return m;
