@@ -2326,15 +2326,16 @@ __device__ __forceinline__ S tri_max_cos(const S* __restrict__ V, int64_t ia, in
     const S* w = p[(i + 2) % 3];
     S e1[3] = {u[0] - o[0], u[1] - o[1], u[2] - o[2]};
     S e2[3] = {w[0] - o[0], w[1] - o[1], w[2] - o[2]};
-    S n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-    S n2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
-    n1 = n1 > S(1e-12) ? n1 : S(1e-12);
-    n2 = n2 > S(1e-12) ? n2 : S(1e-12);
-    // the cosine of the normalised edges (the reference normalises each edge, then
-    // takes the dot product) with one division: the same value up to rounding, so
-    // the split can differ only where the two configurations' cosines tie to within
-    // it (FP64 divisions are slow on this GPU)
-    const S c = (e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2]) / (n1 * n2);
+    // the cosine of the normalised edges (the reference normalises each edge, its
+    // norm clamped at 1e-12, then takes the dot product) from reciprocal square roots
+    // of the squared norms (clamped at 1e-24), without divisions: the same value up
+    // to rounding, so the split can differ only where the two configurations' cosines
+    // tie to within it (FP64 divisions and square roots are slow on this GPU)
+    S q1 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+    S q2 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+    q1 = q1 > S(1e-24) ? q1 : S(1e-24);
+    q2 = q2 > S(1e-24) ? q2 : S(1e-24);
+    const S c = (e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2]) * rsqrt(q1) * rsqrt(q2);
     m = (i == 0 || c > m || c != c) ? c : m;
   }
   return m;
