@@ -1338,6 +1338,7 @@ BrickField<S> make_brick_field(const diso_brick_grid* b, double iso, double padv
   f.unby = (g.c[1] + CR - 1) / CR;
   f.unbz = (g.nzc + KZ - 1) / KZ;
   f.ukz = (g.nzc + f.unbz - 1) / f.unbz;
+  f.ukz_mul = (65536u + (unsigned)f.ukz - 1u) / (unsigned)f.ukz;
   f.index = b->index;
   f.val = (const S*)b->values;
   f.def = (const S*)b->deform;

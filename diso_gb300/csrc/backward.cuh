@@ -302,6 +302,9 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
   int X0, Y0, Z0;
   ptile_coords(ptile, g, X0, Y0, Z0);
   const int zc = Z0 / TZ;
+  // a narrow band's record blocks around the window (read after the first barrier)
+  __shared__ typename F::RecTab rtab;
+  if (REC && threadIdx.x < 12) f.rec_tab_fill(rtab, g, X0, Y0, Z0, threadIdx.x);
   // segment values first, so that their loads overlap the mask loads: MC, the
   // crossing counts of chunks zc, zc + 1 of the edge rows; DMC, the scanned values of
   // chunks zc - 1 .. zc + 2 of the window cell rows (patch bases, and which chunks
@@ -374,7 +377,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
         const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
         const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
         const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
-        if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[f.rec_index(g, X, Y, Z0 + lane)];
+        if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + lane)];
       }
     }
 #pragma unroll
@@ -392,7 +395,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
       const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
       const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
       const int Z = end ? Z0 + TZ : Z0 - 1;
-      const int rec = (busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2] ? codes[f.rec_index(g, X, Y, Z)] : 0;
+      const int rec = (busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2] ? codes[f.rec_index_tab(rtab, g, X, Y, Z)] : 0;
       const int rc = rec & 0xff;
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
       sh.first[wx][wy][end ? TZ + 1 : 0] =

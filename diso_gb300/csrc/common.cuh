@@ -85,8 +85,17 @@ struct Field {
   __device__ __forceinline__ int64_t lin(int X, int Y, int Z) const {
     return ((int64_t)(X - 1) * n1 + (Y - 1)) * n2 + (Z - 1);
   }
-  // position of cell (X, Y, Z)'s DMC record (rows padded to whole chunks)
+  // position of cell (X, Y, Z)'s DMC record (rows padded to whole chunks); the per-tile
+  // table and per-unit slot forms are the same here (fields.cuh: a narrow band's differ)
   __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const { return g.code(X, Y, Z); }
+  struct RecTab {};
+  __device__ __forceinline__ void rec_tab_fill(RecTab&, const Geom&, int, int, int, int) const {}
+  __device__ __forceinline__ int64_t rec_index_tab(const RecTab&, const Geom& g, int X, int Y, int Z) const {
+    return g.code(X, Y, Z);
+  }
+  __device__ __forceinline__ int64_t rec_index_slot(int, const Geom& g, int X, int Y, int Z) const {
+    return g.code(X, Y, Z);
+  }
   // unpadded point (x, y, z) of a row in the grid whose first point is at `off`
   __device__ __forceinline__ S point(int64_t off, int, int, int z) const { return __ldg(sdf + off + z); }
   // deform at padded point (zero in the pad)

@@ -41,6 +41,14 @@ struct SphereField {
   // value at padded point (X, Y, Z); the pad value outside the grid
   __device__ __forceinline__ S at(int X, int Y, int Z) const { return inside(X, Y, Z) ? value(X - 1, Y - 1, Z - 1) : pad; }
   __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const { return g.code(X, Y, Z); }
+  struct RecTab {};
+  __device__ __forceinline__ void rec_tab_fill(RecTab&, const Geom&, int, int, int, int) const {}
+  __device__ __forceinline__ int64_t rec_index_tab(const RecTab&, const Geom& g, int X, int Y, int Z) const {
+    return g.code(X, Y, Z);
+  }
+  __device__ __forceinline__ int64_t rec_index_slot(int, const Geom& g, int X, int Y, int Z) const {
+    return g.code(X, Y, Z);
+  }
   // unpadded point (x, y, z) of a row in the grid (the row offset is not used)
   __device__ __forceinline__ S point(int64_t, int x, int y, int z) const { return value(x, y, z); }
   // deform at padded point (zero in the pad)
@@ -185,15 +193,51 @@ struct BrickField {
   // (the units of field_count_kernel: unby x unbz runs of ukz chunks per row block)
   const int* __restrict__ umap;
   int unby, unbz, ukz;
+  unsigned ukz_mul;  // ceil(2^16 / ukz): chunk / ukz = chunk * ukz_mul >> 16 (ukz <= 4, chunks < 2^15)
   static constexpr int64_t UNIT_RECS = (int64_t)CP * CR * KZ * TZ;
 
+  // offset of cell (X, Y, Z) in its unit's block, the unit along z
+  __device__ __forceinline__ int64_t rec_off(int X, int Y, int Z, int& uz) const {
+    uz = (int)(((unsigned)Z / TZ * ukz_mul) >> 16);
+    return ((int64_t)(X % CP) * CR + Y % CR) * (KZ * TZ) + (Z - uz * ukz * TZ);
+  }
   __device__ __forceinline__ int64_t rec_index(const Geom& g, int X, int Y, int Z) const {
     (void)g;
-    const int tz = Z / TZ, uz = tz / ukz;
-    const int64_t unit = ((int64_t)(X / CP) * unby + Y / CR) * unbz + uz;
-    const int slot = umap[unit];
-    const int64_t off = ((int64_t)(X % CP) * CR + Y % CR) * (KZ * TZ) + (Z - uz * ukz * TZ);
+    int uz;
+    const int64_t off = rec_off(X, Y, Z, uz);
+    const int slot = umap[((int64_t)(X / CP) * unby + Y / CR) * unbz + uz];
     return (int64_t)(slot < 0 ? 0 : slot) * UNIT_RECS + off;  // a listed unit's block (no other is read)
+  }
+  // the count's form: the unit's block is known (its place in the list of units)
+  __device__ __forceinline__ int64_t rec_index_slot(int slot, const Geom&, int X, int Y, int Z) const {
+    int uz;
+    const int64_t off = rec_off(X, Y, Z, uz);
+    return (int64_t)slot * UNIT_RECS + off;
+  }
+  // The emit's and the backward's form: the blocks of the (at most 2 x 2 x 3) units
+  // around a tile's window (cells [X0 - 1, X0 + TX] x [Y0 - 1, Y0 + TY] x [Z0 - 1,
+  // Z0 + TZ]) loaded once per tile, entry i by thread i < 12, before a barrier
+  struct RecTab {
+    int ux0, uy0, uz0;
+    int s[12];
+  };
+  __device__ __forceinline__ void rec_tab_fill(RecTab& t, const Geom& g, int X0, int Y0, int Z0, int i) const {
+    const int ux0 = (X0 > 0 ? X0 - 1 : 0) / CP, uy0 = (Y0 > 0 ? Y0 - 1 : 0) / CR;
+    const int tz = Z0 / TZ, uz0 = (int)(((unsigned)(tz > 0 ? tz - 1 : 0) * ukz_mul) >> 16);
+    if (i == 0) {
+      t.ux0 = ux0;
+      t.uy0 = uy0;
+      t.uz0 = uz0;
+    }
+    const int ux = ux0 + i / 6, uy = uy0 + (i / 3) % 2, uz = uz0 + i % 3;
+    const int nux = (g.c[0] + CP - 1) / CP;
+    t.s[i] = (ux < nux && uy < unby && uz < unbz) ? umap[((int64_t)ux * unby + uy) * unbz + uz] : -1;
+  }
+  __device__ __forceinline__ int64_t rec_index_tab(const RecTab& t, const Geom&, int X, int Y, int Z) const {
+    int uz;
+    const int64_t off = rec_off(X, Y, Z, uz);
+    const int slot = t.s[(X / CP - t.ux0) * 6 + (Y / CR - t.uy0) * 3 + (uz - t.uz0)];
+    return (int64_t)(slot < 0 ? 0 : slot) * UNIT_RECS + off;
   }
 
   __device__ __forceinline__ int entry(int x, int y, int z) const {

@@ -408,6 +408,7 @@ struct CountShared {
   int list[COUNT_LIST];
   int nlist, base;
   unsigned long long tot[2];  // the CTA's counts (both halves) in 64 bits, for Stats::sum_lo / sum_hi
+  int rec_slot;               // a narrow band's unit being counted: its block of cell records
   // the global list and its counter: tiles past COUNT_LIST go there directly (a CTA
   // that takes units from a grid-wide counter may meet more active tiles than its share)
   int* spill;
@@ -578,7 +579,7 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F&
     }
     seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
     if (codes && nt) {
-      uint4* out = reinterpret_cast<uint4*>(codes + f.rec_index(g, X, Y, Z0));
+      uint4* out = reinterpret_cast<uint4*>(codes + f.rec_index_slot(sh.rec_slot, g, X, Y, Z0));
       out[0] = stage[0];
       out[1] = stage[1];
       out[2] = stage[2];
@@ -848,8 +849,12 @@ __global__ void __launch_bounds__(NTHREADS, 2) field_count_kernel(F f, Geom g, u
   const int n = units[0];
   int64_t ck = 0;
 #pragma unroll 1
-  for (int i = blockIdx.x; i < n; i += gridDim.x)
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    // the unit's block of cell records is its place in the list (read after
+    // count_unit's first barrier; the previous unit's readers passed its last one)
+    if (threadIdx.x == 0) sh.rec_slot = i;
     count_unit<S, METHOD>(sh, f, g, seg, tile_flag, codes, stats, units[1 + i], 0, ck);
+  }
   count_flush<S, METHOD>(sh, &stats->n_active, active);
   count_totals<S, METHOD>(sh, stats);
 }
@@ -1476,9 +1481,11 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
   __shared__ uint32_t nwi, nci;
   __shared__ __align__(16) S epos[CAP][3];
+  __shared__ typename F::RecTab rtab;  // a narrow band's record blocks around the window
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
+  if (threadIdx.x < 12) f.rec_tab_fill(rtab, g, X0, Y0, Z0, threadIdx.x);
   // segment values of the window rows: activity of chunks tz-1, tz, tz+1, the bases
   if (threadIdx.x < KX * KY) {
     const int wx = threadIdx.x / KY, wy = threadIdx.x % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
@@ -1515,9 +1522,9 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
       if (r < KX * KY) {
         const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
         const uint32_t act = sact[wx][wy];
-        if (act & 2) c[k] = codes[f.rec_index(g, X, Y, Z0 + lane)];
-        if (lane == 0 && (act & 1)) e[k] = codes[f.rec_index(g, X, Y, Z0 - 1)];
-        if (lane == 31 && (act & 4)) e[k] = codes[f.rec_index(g, X, Y, Z0 + TZ)];
+        if (act & 2) c[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + lane)];
+        if (lane == 0 && (act & 1)) e[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 - 1)];
+        if (lane == 31 && (act & 4)) e[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + TZ)];
       }
     }
 #pragma unroll
