@@ -21,8 +21,9 @@
 //     memory (the same arithmetic, in the same order, as the stored backward's edge
 //     pass), and each point adds the adjoints of its at most six edges in a fixed
 //     order: deterministic and bit-identical to the stored backward;
-//   * point tiles with no crossing nearby (the forward's tile bits) only get zeros,
-//     written by another kernel on a second stream while this one runs.
+//   * point tiles with no crossing nearby (the forward's tile bits) only get zeros:
+//     bulk copies that warp 0 issues inside the active tiles (zero_column), or
+//     zero_tiles_kernel beside this one.
 //
 // Tiles whose window holds more crossing edges than the shared-memory cache compute
 // each edge's adjoint at both of its end points instead.
@@ -286,15 +287,63 @@ __device__ __forceinline__ void field_param_add(const SphereField<S>& f, double*
   }
 }
 
+// Zeros of column `col` of point tiles (the 4 x 8 rows of points (x0.., y0..) along the
+// whole z extent) where its tiles have no crossing nearby, by the calling warp: lane
+// l takes row (x0 + l / 8, y0 + l % 8); each run of such z tiles becomes bulk copies
+// of at most FB_ZBLOCK bytes from the zeroed block to the row's dL/dsdf and dL/ddeform
+// (rows of a multiple of 16 bytes at 16-byte aligned addresses, checked by the host).
+// The copies run on the TMA unit beside the fused pass; the lane commits them.
+template <class S>
+__device__ __forceinline__ void zero_column(const Geom& g, const uint8_t* __restrict__ tile_flag, int64_t col,
+                                            S* __restrict__ gsdf, S* __restrict__ gdef, const void* zblock) {
+  const int lane = threadIdx.x & 31;
+  const int x0 = (int)(col / g.ptiles_y()) * TX, y0 = (int)(col % g.ptiles_y()) * TY;
+  const int x = x0 + lane / TY, y = y0 + lane % TY;
+  const bool row = x < g.n[0] && y < g.n[1];
+  const int pz = g.ptiles_z();
+  char* srow = reinterpret_cast<char*>(gsdf + ((int64_t)x * g.n[1] + y) * g.n[2]);
+  char* drow = gdef ? reinterpret_cast<char*>(gdef + 3 * (((int64_t)x * g.n[1] + y) * g.n[2])) : nullptr;
+  bool any = false;
+  for (int base = 0; base < pz; base += 32) {
+    const int tz = base + lane;
+    bool act = true;
+    if (tz < pz) {
+      act = false;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) act = act || ptile_flag(g, tile_flag, x0, y0, tz * TZ, k) != 0;
+    }
+    uint32_t idle = __ballot_sync(0xffffffffu, !act);
+    while (idle) {
+      const int a = __ffs(idle) - 1;
+      const uint32_t rest = ~(idle >> a);
+      const int len = rest ? __ffs(rest) - 1 : 32 - a;  // idle tiles a .. a + len - 1
+      idle &= len >= 32 ? 0u : ~(((1u << len) - 1u) << a);
+      if (a + len >= 32) idle &= (1u << a) - 1u;
+      const int z0 = (base + a) * TZ, z1 = min((base + a + len) * TZ, g.n[2]);
+      if (!row || z1 <= z0) continue;
+      const int64_t sb = (int64_t)z0 * sizeof(S), se = (int64_t)z1 * sizeof(S);
+      for (int64_t o = sb; o < se; o += FB_ZBLOCK)
+        bulk_store(srow + o, zblock, (uint32_t)(se - o < FB_ZBLOCK ? se - o : FB_ZBLOCK));
+      if (drow)
+        for (int64_t o = 3 * sb; o < 3 * se; o += FB_ZBLOCK)
+          bulk_store(drow + o, zblock, (uint32_t)(3 * se - o < FB_ZBLOCK ? 3 * se - o : FB_ZBLOCK));
+      any = true;
+    }
+  }
+  if (any) bulk_commit();
+}
+
 // one active point tile (see the top of this file); for an evaluated field the
 // point gradients go to the spheres' parameters (field_param_add into `part`) and
-// only the deform's gradient is written
+// only the deform's gradient is written.  zcol >= 0: warp 0 also writes that column's
+// zeros (zero_column over the tile bits zflag) while the tile's edge adjoints run.
 template <class S, int METHOD, class F = Field<S>, bool REC = false>
 __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, const F& f, const Geom& g,
                                            const uint64_t* __restrict__ seg, int64_t ptile, const S* __restrict__ gv,
                                            int64_t V, const S scale[3], int exact, S* __restrict__ gsdf,
                                            S* __restrict__ gdef, bool& bad, double* __restrict__ part = nullptr,
-                                           const CellRec* __restrict__ codes = nullptr) {
+                                           const CellRec* __restrict__ codes = nullptr,
+                                           const uint8_t* __restrict__ zflag = nullptr, int64_t zcol = -1) {
   using SH = FusedShared<S, METHOD, REC>;
   constexpr int LO = SH::LO, CX = SH::CX, CY = SH::CY, KX = SH::KX, KY = SH::KY;
   constexpr int CAP = fb_cap<S>();
@@ -487,14 +536,20 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
   const uint32_t nwi = sh.nwi;
   const bool cached = nwi <= (uint32_t)CAP;
   if (cached) {
-    for (uint32_t i = threadIdx.x; i < nwi; i += blockDim.x) {
+    // warp 0 takes the last 32 of each round of items (the rounds are rarely full),
+    // and then writes its column of zeros (zcol) while the others finish
+    uint32_t i = (threadIdx.x + blockDim.x - 32) % blockDim.x;
+    for (; i < nwi; i += blockDim.x) {
       int x, y, j, a;
       item_decode(sh.witems[i], x, y, j, a);
       S c0[4], c1[4];
       fused_edge_adjoint<S, METHOD, F, SH>(sh, f, X0, Y0, Z0, x, y, j, a, gv, V, scale, exact, c0, c1, bad);
       store_adj<S>(&sh.adj[0][0], i, c0, c1);
     }
+    if (zcol >= 0 && warp == 0) zero_column<S>(g, zflag, zcol, gsdf, gdef, sh.zblock);
     __syncthreads();
+  } else if (zcol >= 0 && warp == 0) {
+    zero_column<S>(g, zflag, zcol, gsdf, gdef, sh.zblock);
   }
   // window slot of the edge along a owned by edge-row cell (x, y, j)
   auto slot = [&](int x, int y, int j, int a) -> int {
@@ -562,59 +617,13 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
   __syncthreads();  // the shared arrays are reused by the CTA's next tile
 }
 
-// Zeros of column `col` of point tiles (the 4 x 8 rows of points (x0.., y0..) along the
-// whole z extent) where its tiles have no crossing nearby, by the calling warp: lane
-// l takes row (x0 + l / 8, y0 + l % 8); each run of such z tiles becomes bulk copies
-// of at most FB_ZBLOCK bytes from the zeroed block to the row's dL/dsdf and dL/ddeform
-// (rows of a multiple of 16 bytes at 16-byte aligned addresses, checked by the host).
-// The copies run on the TMA unit beside the fused pass; the lane commits them.
-template <class S>
-__device__ __forceinline__ void zero_column(const Geom& g, const uint8_t* __restrict__ tile_flag, int64_t col,
-                                            S* __restrict__ gsdf, S* __restrict__ gdef, const void* zblock) {
-  const int lane = threadIdx.x & 31;
-  const int x0 = (int)(col / g.ptiles_y()) * TX, y0 = (int)(col % g.ptiles_y()) * TY;
-  const int x = x0 + lane / TY, y = y0 + lane % TY;
-  const bool row = x < g.n[0] && y < g.n[1];
-  const int pz = g.ptiles_z();
-  char* srow = reinterpret_cast<char*>(gsdf + ((int64_t)x * g.n[1] + y) * g.n[2]);
-  char* drow = gdef ? reinterpret_cast<char*>(gdef + 3 * (((int64_t)x * g.n[1] + y) * g.n[2])) : nullptr;
-  bool any = false;
-  for (int base = 0; base < pz; base += 32) {
-    const int tz = base + lane;
-    bool act = true;
-    if (tz < pz) {
-      act = false;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) act = act || ptile_flag(g, tile_flag, x0, y0, tz * TZ, k) != 0;
-    }
-    uint32_t idle = __ballot_sync(0xffffffffu, !act);
-    while (idle) {
-      const int a = __ffs(idle) - 1;
-      const uint32_t rest = ~(idle >> a);
-      const int len = rest ? __ffs(rest) - 1 : 32 - a;  // idle tiles a .. a + len - 1
-      idle &= len >= 32 ? 0u : ~(((1u << len) - 1u) << a);
-      if (a + len >= 32) idle &= (1u << a) - 1u;
-      const int z0 = (base + a) * TZ, z1 = min((base + a + len) * TZ, g.n[2]);
-      if (!row || z1 <= z0) continue;
-      const int64_t sb = (int64_t)z0 * sizeof(S), se = (int64_t)z1 * sizeof(S);
-      for (int64_t o = sb; o < se; o += FB_ZBLOCK)
-        bulk_store(srow + o, zblock, (uint32_t)(se - o < FB_ZBLOCK ? se - o : FB_ZBLOCK));
-      if (drow)
-        for (int64_t o = 3 * sb; o < 3 * se; o += FB_ZBLOCK)
-          bulk_store(drow + o, zblock, (uint32_t)(3 * se - o < FB_ZBLOCK ? 3 * se - o : FB_ZBLOCK));
-      any = true;
-    }
-  }
-  if (any) bulk_commit();
-}
-
 // Persistent over the active point tiles in list[0 .. *count) (active_ptiles_kernel
 // in kernels.cuh), CTA b taking entries b, b + gridDim.x, ...  DMC: `codes`, when
 // given, are the forward count's cell records of this grid (read instead of
 // recomputing the window cells' codes).  With zbulk, warp 0
 // also zeroes the point tiles with no crossing nearby, column b, b + gridDim.x, ...
-// of point tiles before each of its active tiles and the rest after the last (bulk
-// copies, zero_column); otherwise zero_tiles_kernel writes them beside it.  Bit 3 of
+// of point tiles, one inside each of its active tiles and the rest after the last
+// (bulk copies, zero_column); otherwise zero_tiles_kernel writes them beside it.  Bit 3 of
 // stats->error is set when an index derived from the grid falls outside the
 // forward's counts (the grid no longer matches the forward's record); no access
 // leaves its buffer.
@@ -650,12 +659,11 @@ __global__ void __launch_bounds__(NTHREADS, 3)
   const int warp = threadIdx.x >> 5;
 #pragma unroll 1
   for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
-    if (zbulk && warp == 0 && col < ncol) {
-      zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
-      col += gridDim.x;
-    }
+    // a column of zeros, written by warp 0 inside the tile
+    const int64_t zcol = zbulk && col < ncol ? col : -1;
+    if (zcol >= 0) col += gridDim.x;
     fused_tile<S, METHOD, Field<S>, REC>(sh, f, g, seg, list[i], gv, V, scale, exact, gsdf, gdef, bad, nullptr,
-                                         codes);
+                                         codes, tile_flag, zcol);
   }
   if (zbulk && warp == 0) {
     for (; col < ncol; col += gridDim.x) zero_column<S>(g, tile_flag, col, gsdf, gdef, sh.zblock);
