@@ -267,6 +267,21 @@ __device__ __forceinline__ int code8(uint64_t a, uint64_t b, uint64_t c, uint64_
   return (int)(lo | (hi << 4));
 }
 
+// position of the n-th (from 0) set bit of v, n < popc(v)
+__device__ __forceinline__ int nth_bit(uint32_t v, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w; w >>= 1) {
+    const int c = __popc(v & ((1u << w) - 1u));  // set bits among the low w
+    if (n >= c) {
+      n -= c;
+      v >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
 // The four masks of a cell row (a, b, c, d as for code8) as eight shifted copies, so
 // that the Morton code of cell j of the row (mask bits j+1 and j+2) takes one funnel
 // shift and one logic op per code bit: copy k holds mask (k & 3) shifted so that
@@ -405,6 +420,7 @@ struct CountShared {
   uint32_t act[CP], actc[CP], actf[CP];
   uint32_t mixed[3];                       // per chunk (rotating): OR of count_combine's bits
   __align__(16) CellRec code[CP][32][TZ];  // cell records of each lane's segment (staging)
+  uint32_t pfirst[CP][32];                  // DMC: the warp's patches before each segment's first (count_chunk)
   int list[COUNT_LIST];
   int nlist, base;
   unsigned long long tot[2];  // the CTA's counts (both halves) in 64 bits, for Stats::sum_lo / sum_hi
@@ -556,27 +572,69 @@ __device__ __forceinline__ void count_chunk(CountShared<S, METHOD>& sh, const F&
   uint32_t nv = 0, nf = 0, own = 0, nt = 0;
   uint4* stage = reinterpret_cast<uint4*>(sh.code[warp][lane]);
   if (codes) stage[0] = stage[1] = stage[2] = stage[3] = make_uint4(0u, 0u, 0u, 0u);
-  if (X < g.c[0] && Y < g.c[1]) {
+  const bool row = X < g.c[0] && Y < g.c[1];
+  if (row) {
     const int x = warp, y = lane;
     const uint64_t a = sh.m[x][y], b = sh.m[x + 1][y], c = sh.m[x][y + 1], d = sh.m[x + 1][y + 1];
     const RowBits rw = row_bits(a, b, c, d, zvalid(g, Z0));
     own = rw.xc | rw.yc | rw.zc;
     nt = rw.nt;
     nv = __popc(rw.xc) + __popc(rw.yc) + __popc(rw.zc);
-    uint32_t left = nt;
-    const CodeRow cr = code_row(a, b, c, d);
-    while (left) {
-      const int j = __ffs(left) - 1;
-      left &= left - 1;
-      const int code = code_at(cr, j);
-      if (METHOD == MC) {
-        nf += (uint32_t)(mc_tri(mc_from_morton(code)) & 15);
-      } else {
-        const int rcode = dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X, Y, Z0 + j, g);
-        if (codes) sh.code[warp][lane][j] = (CellRec)(rcode | ((code & 1) << 8) | (nf << 9));
-        nf += dmc_npatch(dmc_case(rcode));
+    if constexpr (METHOD == MC) {
+      uint32_t left = nt;
+      const CodeRow cr = code_row(a, b, c, d);
+      while (left) {
+        const int j = __ffs(left) - 1;
+        left &= left - 1;
+        nf += (uint32_t)(mc_tri(mc_from_morton(code_at(cr, j))) & 15);
       }
     }
+  }
+  if constexpr (METHOD == DMC) {
+    // The warp's non-trivial cells (segment-major, z order inside a segment) are dealt
+    // out to its lanes, item k to lane k mod 32: a surface along z leaves most of a
+    // warp's cells in a few segments, and each cell's ambiguity test is a chain of
+    // dependent lookups.  An item's patches-before-it in its segment is a scan over
+    // the items since the segment's first (pfirst).
+    const uint32_t cnt = __popc(nt);
+    const uint32_t base = warp_incl(cnt) - cnt;  // the lane's first item
+    const uint32_t total = __shfl_sync(0xffffffffu, base + cnt, 31);
+    if (codes) __syncwarp();  // the staging rows are zeroed before other lanes fill them
+    uint32_t carry = 0;       // patches of the rounds before
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      // the owner: the last lane whose first item is at or before k
+      int s = 0;
+#pragma unroll
+      for (int step = 16; step; step >>= 1) {
+        const int t = s + step;
+        if (__shfl_sync(0xffffffffu, base, t) <= k) s = t;
+      }
+      const uint32_t snt = __shfl_sync(0xffffffffu, nt, s), sbase = __shfl_sync(0xffffffffu, base, s);
+      const bool has = k < total;
+      int code = 0, rcode = 0, j = 0;
+      uint32_t np = 0;
+      if (has) {
+        j = nth_bit(snt, (int)(k - sbase));
+        code = code8(sh.m[warp][s], sh.m[warp + 1][s], sh.m[warp][s + 1], sh.m[warp + 1][s + 1], j + 1);
+        rcode = dmc_resolve_m<S>(sh.m, f, X0, Y0, Z0, code, X0 + warp, Y0 + s, Z0 + j, g);
+        np = (uint32_t)dmc_npatch(dmc_case(rcode));
+      }
+      const uint32_t incl = warp_incl(np);
+      const uint32_t before = carry + incl - np;  // the warp's patches before item k
+      if (has && k == sbase) sh.pfirst[warp][s] = before;
+      __syncwarp();
+      if (has && codes)
+        sh.code[warp][s][j] = (CellRec)(rcode | ((code & 1) << 8) | ((before - sh.pfirst[warp][s]) << 9));
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();  // pfirst and the staged records are complete
+    // the lane's patches: up to the next segment with items (or the warp's end)
+    const uint32_t later = __ballot_sync(0xffffffffu, cnt != 0) & ~((2u << lane) - 1u);
+    if (cnt) nf = (later ? sh.pfirst[warp][__ffs(later) - 1] : carry) - sh.pfirst[warp][lane];
+  }
+  if (row) {
     seg[g.seg(X, Y, tz)] = Counts::pack(nv, nf);
     if (codes && nt) {
       uint4* out = reinterpret_cast<uint4*>(codes + f.rec_index_slot(sh.rec_slot, g, X, Y, Z0));
