@@ -393,6 +393,35 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
     }
   }
   __syncthreads();
+  // DMC with the count's cell records: the window cells' records (resolved code,
+  // first patch inside the segment) are loaded first, so that their latency passes
+  // under the edge rows; segments with a zero count hold trivial cells only and have
+  // no records.  Warp w: rows w, w + 8, ...; threads below 2 KX KY: the row ends
+  // (cells Z0 - 1 and Z0 + TZ)
+  constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32);
+  int rec[METHOD == DMC && REC ? RPW : 1];
+  int rend = 0;
+  if constexpr (METHOD == DMC && REC) {
+#pragma unroll
+    for (int k = 0; k < RPW; ++k) {
+      const int r = warp + (NTHREADS / 32) * k;
+      rec[k] = 0;
+      if (r < KX * KY) {
+        const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+        const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+        const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+        if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + lane)];
+      }
+    }
+    if (threadIdx.x < 2 * KX * KY) {
+      const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
+      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
+      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
+      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
+      const int Z = end ? Z0 + TZ : Z0 - 1;
+      if ((busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2]) rend = codes[f.rec_index_tab(rtab, g, X, Y, Z)];
+    }
+  }
   // edge rows: crossing bits and the crossing flags of cell Z0 + TZ, one warp per row
   const uint32_t valid = zvalid(g, Z0);
   for (int r = warp; r < CX * CY; r += NTHREADS / 32) {
@@ -412,23 +441,7 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
   }
   if constexpr (METHOD == DMC) {
    if constexpr (REC) {
-    // window cells from the forward count's cell records (resolved code, first patch
-    // inside the segment), as the emit reads them; segments with a zero count hold
-    // trivial cells only and have no records
-    // a warp's rows' records are loaded together, then stored
-    constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32);
-    int rec[RPW];
-#pragma unroll
-    for (int k = 0; k < RPW; ++k) {
-      const int r = warp + (NTHREADS / 32) * k;
-      rec[k] = 0;
-      if (r < KX * KY) {
-        const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
-        const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
-        const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
-        if ((busy & 2) && Z0 + lane < g.c[2]) rec[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + lane)];
-      }
-    }
+    // the records loaded above, filed as the emit reads them
 #pragma unroll
     for (int k = 0; k < RPW; ++k) {
       const int r = warp + (NTHREADS / 32) * k;
@@ -440,12 +453,8 @@ __device__ __forceinline__ void fused_tile(FusedShared<S, METHOD, REC>& sh, cons
     }
     if (threadIdx.x < 2 * KX * KY) {
       const int r = threadIdx.x >> 1, end = threadIdx.x & 1;
-      const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
-      const bool row = X >= 0 && Y >= 0 && X < g.c[0] && Y < g.c[1];
-      const uint32_t busy = row ? sh.busy[wx][wy] : 0u;
-      const int Z = end ? Z0 + TZ : Z0 - 1;
-      const int rec = (busy & (end ? 4u : 1u)) && Z >= 0 && Z < g.c[2] ? codes[f.rec_index_tab(rtab, g, X, Y, Z)] : 0;
-      const int rc = rec & 0xff;
+      const int wx = r / KY, wy = r % KY;
+      const int rc = rend & 0xff;
       sh.rc[wx][wy][end ? TZ + 1 : 0] = (uint8_t)rc;
       sh.first[wx][wy][end ? TZ + 1 : 0] =
           (int32_t)(end ? sh.pb[wx][wy][1] : sh.pb[wx][wy][0] - (uint32_t)dmc_npatch(sh.cases[rc]));
