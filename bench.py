@@ -833,10 +833,11 @@ def active_points(sdf, iso=0.0):
         return int(act.sum()) * 4 * 8 * 32
 
 
-def read_profile_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` at the benchmark workload from the committed
-    ncu summary (lines "<kernel>: <bytes>"), None when it has no line."""
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "dram_traffic_*.txt"))):
+def read_profile_traffic(kernel, n):
+    """Per-launch DRAM bytes of `kernel` on the n^3 workload from the committed ncu
+    summary of that size (profiles/dram_traffic_*_<n>.txt, lines "<kernel>: <bytes>"),
+    None when there is none."""
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"dram_traffic_*_{n}.txt"))):
         try:
             txt = open(path).read()
         except OSError:
@@ -1064,7 +1065,7 @@ def run_ours(args, rank, world, device):
     dom = max(ours, key=lambda k: ours[k] * kernels[k][0])
     peak, peak_kind = measured_peaks()
     achieved = algo[dom] / (per_launch[dom] * 1e-3) / 1e9
-    traffic = read_profile_traffic(dom)
+    traffic = read_profile_traffic(dom, n)
     step_bytes = vol * s_b * (3 + 3) + 4 * nq * 3 * s_b + 2 * nv * 3 * s_b + 8 * nq * 4
     ms_step = ms_max / args.steps
     res = {
