@@ -1567,43 +1567,45 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
     }
   }
   __syncthreads();
-  // records of the window, one warp per row (the records of RB rows in flight
-  // together); the edge rows' crossing bits from them
-  constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32), RB = 4;
-#pragma unroll 1
-  for (int i0 = 0; i0 < RPW; i0 += RB) {
-    int c[RB], e[RB];
+  // records of the window, one warp per row, every row of the warp in flight
+  // together, and with them the rows' ends (cells Z0 - 1 and Z0 + TZ: thread t below
+  // 2 KX KY takes end t & 1 of row t >> 1); the edge rows' crossing bits from them
+  constexpr int RPW = (KX * KY + NTHREADS / 32 - 1) / (NTHREADS / 32);
+  int c[RPW], rend = 0;
 #pragma unroll
-    for (int k = 0; k < RB; ++k) {
-      const int r = warp + (NTHREADS / 32) * (i0 + k);
-      c[k] = e[k] = 0;
-      if (r < KX * KY) {
-        const int wx = r / KY, wy = r % KY, X = X0 - 1 + wx, Y = Y0 - 1 + wy;
-        const uint32_t act = sact[wx][wy];
-        if (act & 2) c[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + lane)];
-        if (lane == 0 && (act & 1)) e[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 - 1)];
-        if (lane == 31 && (act & 4)) e[k] = codes[f.rec_index_tab(rtab, g, X, Y, Z0 + TZ)];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < RB; ++k) {
-      const int r = warp + (NTHREADS / 32) * (i0 + k);
-      if (r >= KX * KY) break;
+  for (int k = 0; k < RPW; ++k) {
+    const int r = warp + (NTHREADS / 32) * k;
+    c[k] = 0;
+    if (r < KX * KY) {
       const int wx = r / KY, wy = r % KY;
-      cw[wx][wy][lane + 1] = (CellRec)c[k];
-      if (lane == 0) cw[wx][wy][0] = (CellRec)e[k];
-      if (lane == 31) cw[wx][wy][TZ + 1] = (CellRec)e[k];
-      if (wx >= 1 && wy >= 1) {
-        const int code = c[k] & 0xff, cf = cross_flags(code);
-        RowBits w;
-        w.xc = __ballot_sync(0xffffffffu, cf & 1);
-        w.yc = __ballot_sync(0xffffffffu, cf & 2);
-        w.zc = __ballot_sync(0xffffffffu, cf & 4);
-        w.nt = __ballot_sync(0xffffffffu, code != 0 && code != 255);
-        if (lane == 0) wb[wx - 1][wy - 1] = w;
-        if (lane == 31) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(e[k] & 0xff);
-      }
+      if (sact[wx][wy] & 2) c[k] = codes[f.rec_index_tab(rtab, g, X0 - 1 + wx, Y0 - 1 + wy, Z0 + lane)];
     }
+  }
+  if (threadIdx.x < 2 * KX * KY) {
+    const int r = threadIdx.x >> 1, end = threadIdx.x & 1, wx = r / KY, wy = r % KY;
+    if (sact[wx][wy] & (end ? 4u : 1u))
+      rend = codes[f.rec_index_tab(rtab, g, X0 - 1 + wx, Y0 - 1 + wy, end ? Z0 + TZ : Z0 - 1)];
+  }
+#pragma unroll
+  for (int k = 0; k < RPW; ++k) {
+    const int r = warp + (NTHREADS / 32) * k;
+    if (r >= KX * KY) break;
+    const int wx = r / KY, wy = r % KY;
+    cw[wx][wy][lane + 1] = (CellRec)c[k];
+    if (wx >= 1 && wy >= 1) {
+      const int code = c[k] & 0xff, cf = cross_flags(code);
+      RowBits w;
+      w.xc = __ballot_sync(0xffffffffu, cf & 1);
+      w.yc = __ballot_sync(0xffffffffu, cf & 2);
+      w.zc = __ballot_sync(0xffffffffu, cf & 4);
+      w.nt = __ballot_sync(0xffffffffu, code != 0 && code != 255);
+      if (lane == 0) wb[wx - 1][wy - 1] = w;
+    }
+  }
+  if (threadIdx.x < 2 * KX * KY) {
+    const int r = threadIdx.x >> 1, end = threadIdx.x & 1, wx = r / KY, wy = r % KY;
+    cw[wx][wy][end ? TZ + 1 : 0] = (CellRec)rend;
+    if (end && wx >= 1 && wy >= 1) w32[wx - 1][wy - 1] = (uint8_t)cross_flags(rend & 0xff);
   }
   __syncthreads();
   // code after the ambiguity test, and first patch relative to its row's base pb, of
