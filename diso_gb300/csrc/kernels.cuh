@@ -1344,15 +1344,18 @@ __device__ __forceinline__ void mc_emit_tile(const F& f, const Geom& g, const ui
   __shared__ uint32_t nvi, nci;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
+  // segment values (one per thread) loaded first, so that they overlap the mask loads
+  static_assert(CX * CY * 2 <= NTHREADS, "one segment value per thread");
+  const int sk = threadIdx.x & 1, sy = (threadIdx.x >> 1) % CY, sx = (threadIdx.x >> 1) / CY;
+  uint64_t sv = 0;
+  if (threadIdx.x < CX * CY * 2 && X0 + sx < g.c[0] && Y0 + sy < g.c[1] && tz + sk < g.nzc)
+    sv = seg[g.seg(X0 + sx, Y0 + sy, tz + sk)];
   S dmn, dmx;
   bool dseen = false;
   load_masks<S, WX, WY, false>(m, f, X0, Y0, Z0, dmn, dmx, dseen);
-  for (int i = threadIdx.x; i < CX * CY * 2; i += blockDim.x) {
-    const int k = i & 1, y = (i >> 1) % CY, x = (i >> 1) / CY;
-    const int X = X0 + x, Y = Y0 + y, zc = tz + k;
-    const uint64_t s = (X < g.c[0] && Y < g.c[1] && zc < g.nzc) ? seg[g.seg(X, Y, zc)] : 0ull;
-    vb[x][y][k] = Counts::lo(s);
-    if (k == 0 && x < TX && y < TY) fb[x][y] = Counts::hi(s);
+  if (threadIdx.x < CX * CY * 2) {
+    vb[sx][sy][sk] = Counts::lo(sv);
+    if (sk == 0 && sx < TX && sy < TY) fb[sx][sy] = Counts::hi(sv);
   }
   __syncthreads();
   const uint32_t valid = zvalid(g, Z0);
