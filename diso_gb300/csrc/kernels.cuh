@@ -1507,7 +1507,6 @@ __global__ void __launch_bounds__(NTHREADS) mc_emit_kernel(F f, Geom g, const ui
 constexpr int EW_ROWS = (TX + 1) * (TY + 1);
 constexpr int EW_ITEMS = EW_ROWS * 3 * (TZ + 1);
 static_assert(EW_ITEMS < (1 << 13), "window slots and flags share 16 bits");
-static_assert(EW_ITEMS >= 4 * TX * TY * TZ, "the window item list also holds a tile's patches");
 constexpr int EPOS_BYTES = 24576;
 template <class S>
 __host__ __device__ constexpr int epos_cap() {
@@ -1538,6 +1537,7 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
   __shared__ uint16_t wcell[TX + 1][TY + 1][TZ + 1];  // per edge-row cell: first window slot | flags << 13
   __shared__ uint16_t cbase[TX][TY];
   __shared__ uint16_t witems[EW_ITEMS];
+  __shared__ uint16_t pitems[4 * TX * TY * TZ];  // dual vertex items: one per patch of the tile's cells
   __shared__ uint8_t prow[TX][TY];        // patches of the own rows' segments
   __shared__ uint32_t wsum[NTHREADS / 32 + 1];
   __shared__ uint32_t nwi, nci;
@@ -1659,6 +1659,17 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
       for (int a = 0; a < 3; ++a)
         if (f32 & (1 << a)) witems[o++] = item_code(ex_, ey, TZ, a);
     }
+    // an own row's dual vertex items, one per patch in patch order: the patches of a
+    // non-trivial cell run from its record's in-segment prefix to the next
+    // non-trivial cell's (the segment's total after the last one; trivial cells have
+    // no record)
+    if (ex_ < TX && ey < TY && ((w.nt >> lane) & 1)) {
+      const int x = ex_ + 1, y = ey + 1;
+      const uint32_t later = w.nt & ~((2u << lane) - 1u);
+      const int p0 = cw[x][y][lane + 1] >> 9;
+      const int p1 = later ? cw[x][y][__ffs(later)] >> 9 : (int)prow[ex_][ey];
+      for (int q = 0; q < p1 - p0; ++q) pitems[cbase[ex_][ey] + p0 + q] = item_code(ex_, ey, lane, q);
+    }
   }
   __syncthreads();
   const bool cached = nwi <= (uint32_t)CAP;
@@ -1717,27 +1728,12 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
     const int w = wcell[x][y][j];
     return (w & 0x1fff) + __popc((w >> 13) & ((1 << a) - 1));
   };
-  // dual vertex items, one per patch in patch order, into the window item list (done
-  // with): the patches of a non-trivial cell run from its record's in-segment prefix
-  // to the next non-trivial cell's (the segment's total after the last one; trivial
-  // cells have no record)
-  for (int r = warp; r < TX * TY; r += NTHREADS / 32) {
-    const int ex_ = r / TY, ey = r % TY, x = ex_ + 1, y = ey + 1;
-    const uint32_t nt = wb[ex_][ey].nt;
-    if ((nt >> lane) & 1) {
-      const uint32_t later = nt & ~((2u << lane) - 1u);
-      const int p0 = cw[x][y][lane + 1] >> 9;
-      const int p1 = later ? cw[x][y][__ffs(later)] >> 9 : (int)prow[ex_][ey];
-      for (int q = 0; q < p1 - p0; ++q) witems[cbase[ex_][ey] + p0 + q] = item_code(ex_, ey, lane, q);
-    }
-  }
-  __syncthreads();
   // dual vertices: mean of the patch's edge vertices, edges in ascending id
   // (create_dmc_verts_kernel, src/cudualmc.cu:907-955); a patch's edges come from the
   // per-code patch masks
   for (uint32_t i = threadIdx.x; i < nci; i += blockDim.x) {
     int ix, iy, j, q;
-    item_decode(witems[i], ix, iy, j, q);
+    item_decode(pitems[i], ix, iy, j, q);
     const int x = ix + 1, y = iy + 1, X = X0 + ix, Y = Y0 + iy, Z = Z0 + j;
     const int rc = cw[x][y][j + 1];
     uint32_t m = (uint32_t)(__ldg(&g_dmc_pmask.m[rc & 0xff]) >> (12 * q)) & 0xfffu;
