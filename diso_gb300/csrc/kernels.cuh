@@ -1340,7 +1340,6 @@ __device__ __forceinline__ void mc_emit_tile(const F& f, const Geom& g, const ui
   __shared__ uint8_t fpre[TX][TY][TZ];  // triangles before the cell inside its segment
   __shared__ uint16_t vitems[EMIT_ITEMS];
   __shared__ uint16_t citems[TX * TY * TZ];
-  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
   __shared__ uint32_t nvi, nci;
   int X0, Y0, Z0, tz;
   tile_coords(tile, g, X0, Y0, Z0, tz);
@@ -1389,13 +1388,15 @@ __device__ __forceinline__ void mc_emit_tile(const F& f, const Geom& g, const ui
       run += (uint32_t)(mc_tri(mc_from_morton(code_at(cr, j))) & 15);
     }
   }
-  uint32_t tot;
-  const uint32_t off = block_excl_scan(cv | (cc << 16), wsum, tot);
-  if (threadIdx.x == 0) {
-    nvi = tot & 0xffffu;
-    nci = tot >> 16;
-  }
-  if (threadIdx.x < TX * TY) {
+  // the own rows are warp 0's lanes: their bases by a warp scan
+  static_assert(TX * TY == 32, "one own row per lane of warp 0");
+  if (threadIdx.x < 32) {
+    const uint32_t v = cv | (cc << 16), inc = warp_incl(v), tot = __shfl_sync(0xffffffffu, inc, 31);
+    const uint32_t off = inc - v;
+    if (threadIdx.x == 0) {
+      nvi = tot & 0xffffu;
+      nci = tot >> 16;
+    }
     uint32_t o = off & 0xffffu;
     // vertices in (cell, axis) order: interleave the three axes per cell
     uint32_t b = own.xc | own.yc | own.zc;
@@ -1533,14 +1534,10 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
   __shared__ uint32_t qb[TX][TY];
   __shared__ RowBits wb[TX + 1][TY + 1];  // edge rows: cells [X0, X0+TX] x [Y0, Y0+TY]
   __shared__ uint8_t w32[TX + 1][TY + 1];  // crossing flags of the row's cell Z0 + TZ
-  __shared__ uint16_t wbase[TX + 1][TY + 1];
   __shared__ uint16_t wcell[TX + 1][TY + 1][TZ + 1];  // per edge-row cell: first window slot | flags << 13
-  __shared__ uint16_t cbase[TX][TY];
   __shared__ uint16_t witems[EW_ITEMS];
   __shared__ uint16_t pitems[4 * TX * TY * TZ];  // dual vertex items: one per patch of the tile's cells
   __shared__ uint8_t prow[TX][TY];        // patches of the own rows' segments
-  __shared__ uint32_t wsum[NTHREADS / 32 + 1];
-  __shared__ uint32_t nwi, nci;
   __shared__ __align__(16) S epos[CAP][3];
   __shared__ typename F::RecTab rtab;  // a narrow band's record blocks around the window
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1619,35 +1616,39 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
     return jj ? (r >> 9) : -(int)dmc_npatch(dmc_case(r & 0xff));
   };
   // edge rows: crossing edges (window items) and, for the own rows, the patches
-  // (dual vertex items); row bases by a block scan, then one warp per row writes the
-  // row's window items
+  // (dual vertex items).  Every warp scans the rows' counts itself (rows lane and
+  // lane + 32), so that the row bases need no block-wide scan and no barrier; then one
+  // warp per row writes the row's window items and dual vertex items
+  static_assert(EW_ROWS <= 64 && EW_ROWS > 32, "two edge rows per lane");
+  uint32_t base_lo, base_hi, nwi, nci;
   {
-    uint32_t ce = 0, cc = 0;
-    const int ex_ = threadIdx.x / (TY + 1), ey = threadIdx.x % (TY + 1);
-    if (threadIdx.x < EW_ROWS) {
-      const RowBits w = wb[ex_][ey];
-      ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(w32[ex_][ey]);
-      if (ex_ < TX && ey < TY) cc = prow[ex_][ey];
+    uint32_t v[2] = {0u, 0u};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = lane + 32 * h, ex_ = r / (TY + 1), ey = r % (TY + 1);
+      if (r < EW_ROWS) {
+        const RowBits w = wb[ex_][ey];
+        const uint32_t ce = __popc(w.xc) + __popc(w.yc) + __popc(w.zc) + __popc(w32[ex_][ey]);
+        const uint32_t cc = (ex_ < TX && ey < TY) ? prow[ex_][ey] : 0u;
+        v[h] = ce | (cc << 13);
+      }
     }
-    uint32_t tot;
-    const uint32_t off = block_excl_scan(ce | (cc << 13), wsum, tot);
-    if (threadIdx.x == 0) {
-      nwi = tot & 0x1fffu;
-      nci = tot >> 13;
-    }
-    if (threadIdx.x < EW_ROWS) {
-      wbase[ex_][ey] = (uint16_t)(off & 0x1fffu);
-      if (ex_ < TX && ey < TY) cbase[ex_][ey] = (uint16_t)(off >> 13);
-    }
+    const uint32_t i0 = warp_incl(v[0]);
+    const uint32_t i1 = warp_incl(v[1]) + __shfl_sync(0xffffffffu, i0, 31);
+    const uint32_t tot = __shfl_sync(0xffffffffu, i1, 31);
+    base_lo = i0 - v[0];
+    base_hi = i1 - v[1];
+    nwi = tot & 0x1fffu;
+    nci = tot >> 13;
   }
-  __syncthreads();
   for (int r = warp; r < EW_ROWS; r += NTHREADS / 32) {
     const int ex_ = r / (TY + 1), ey = r % (TY + 1);
     const RowBits w = wb[ex_][ey];
+    const uint32_t rbase = r < 32 ? __shfl_sync(0xffffffffu, base_lo, r) : __shfl_sync(0xffffffffu, base_hi, r - 32);
     // window items in slot order: cells ascending, axes ascending per cell
     const int fl = row_flags(w, lane);
     const uint32_t before = row_prefix(w, lane);
-    uint32_t o = wbase[ex_][ey] + before;
+    uint32_t o = (rbase & 0x1fffu) + before;
     wcell[ex_][ey][lane] = (uint16_t)(o | (fl << 13));
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -1668,7 +1669,7 @@ __device__ __forceinline__ void dmc_emit_tile(const F& f, const Geom& g, const u
       const uint32_t later = w.nt & ~((2u << lane) - 1u);
       const int p0 = cw[x][y][lane + 1] >> 9;
       const int p1 = later ? cw[x][y][__ffs(later)] >> 9 : (int)prow[ex_][ey];
-      for (int q = 0; q < p1 - p0; ++q) pitems[cbase[ex_][ey] + p0 + q] = item_code(ex_, ey, lane, q);
+      for (int q = 0; q < p1 - p0; ++q) pitems[(rbase >> 13) + p0 + q] = item_code(ex_, ey, lane, q);
     }
   }
   __syncthreads();
