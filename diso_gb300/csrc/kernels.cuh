@@ -392,9 +392,10 @@ __device__ __forceinline__ int row_prefix(const RowBits& r, int j) {
 // is spliced from the ballots of three consecutive chunks (two bits of the chunk
 // below, all of the chunk, one bit of the chunk above), so every point is read once
 // per unit and the per-row cost is a load, a compare, a ballot and a store.  Each
-// lane derives its segment's crossing count from four row masks with popcounts and
-// walks only the segment's non-trivial cells for the case-table lookups (the DMC
-// ambiguity test reads a neighbour outside the unit's rows from global memory).
+// lane derives its segment's crossing count from four row masks with popcounts; the
+// case-table lookups visit only non-trivial cells (MC: the lane's own; DMC: the
+// warp's, dealt out over its lanes, since the ambiguity test is the longer chain and
+// reads a neighbour outside the unit's rows from global memory).
 //
 // Persistent: CTA b handles units b, b + gridDim.x, ... (the TMA count takes them
 // from a grid-wide counter); it keeps the list of its active tiles and publishes it
